@@ -1,0 +1,371 @@
+#!/usr/bin/env python
+"""Benchmark: batched lattice KMC on one GB300 (steps/s aggregate).
+
+Workload (per GPU): corundum 10x10x3 = 3,600 sites, 4 electrons and 4 fixed
++1 dopants on seeded sites, FP64 Ewald array (103.7 MB) built on the GPU,
+4,096 trajectories with per-trajectory Philox streams.  One bench step = one
+CUDA-graph launch of the persistent kernel advancing every trajectory by
+10,000 KMC steps (100 such chunks = the 1e6-step job).
+
+  python bench.py [--gpus N --steps K --warmup W] [--impl reference]
+
+Prints one JSON line (rank 0).  ``value`` is device-timed with inputs
+resident; ``e2e`` runs the job through the host-buffer entry point
+(``pycd_gb300.batch.run_batched``) with the array and tables copied from
+pinned host memory and the final state copied back inside the timed region.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+N_CELLS = (10, 10, 3)
+N_TRAJ = 4096
+N_CARRIERS, N_DOPANTS, Z = 4, 4, 4
+CHUNK = 10000
+# algorithmic bytes per KMC step: 8 n_c (z+1)(n_c+n_d) Ewald entries plus
+# 16 n_c (z+1) for E_rel and phi_bg
+B_STEP = 8 * N_CARRIERS * (Z + 1) * (N_CARRIERS + N_DOPANTS) + 16 * N_CARRIERS * (Z + 1)
+T_FINAL, DT = 1e30, 1e27  # time grid wide enough that no trajectory ends by time
+SEED = 20251203
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return d["hbm_gbs"], "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler(object):
+    """nvidia-smi samples of SM clock and throttle reasons while running."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index, self.rows, self.proc = index, [], None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([v.strip() for v in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown",
+                 "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4)
+                          if len(r) > 4 + i and r[4 + i].lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(self.rows)}
+
+
+def build_workload(rank=0):
+    """System, device array, tables and initial carrier sites."""
+    import torch
+    from pycd_gb300 import workloads as wl
+    system = wl.corundum(N_CELLS)
+    A = system.get_precomputed_array_device("fp64")
+    carriers0, dopants = wl.batched_uniform_sites(seed=3600)
+    tables, run = wl.batched_tables(system, A, N_CARRIERS, dopants, 1.0,
+                                    t_final=T_FINAL, time_interval=DT)
+    rng = np.random.default_rng(SEED + rank)
+    free = np.setdiff1d(np.arange(3600), dopants)
+    occ = np.stack([rng.choice(free, size=N_CARRIERS, replace=False)
+                    for _ in range(N_TRAJ)]).astype(np.int32)
+    torch.cuda.synchronize()
+    return system, A, tables, run, dopants, occ
+
+
+def time_plain(tables, occ, n_steps=20000):
+    """The plain form: one trajectory advanced alone by the same kernel."""
+    import torch
+    from pycd_gb300.kmc import KmcBatch, KmcEngine
+    eng = KmcEngine(tables)
+    b = KmcBatch(occ[:1])
+    eng.advance(b, 2000, eng.rng_struct(seed=SEED))
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    eng.advance(b, n_steps, eng.rng_struct(seed=SEED))
+    e1.record()
+    torch.cuda.synchronize()
+    return n_steps / (e0.elapsed_time(e1) / 1e3)
+
+
+def cpu_port_steps(args):
+    """Oracle port (the reference's algorithm, NumPy) on one trajectory;
+    returns steps done and seconds."""
+    a_path, tab_path, occ, n_steps, seed = args
+    sys.path.insert(0, str(ROOT))
+    import pickle
+    from oracle import kmc_oracle as ko
+    from oracle import philox
+    A = np.load(a_path, mmap_mode="r")
+    with open(tab_path, "rb") as fh:
+        t = pickle.load(fh)
+    u = np.array([v for s in range(n_steps) for v in philox.step_uniforms(seed, 0, s)])
+    t0 = time.perf_counter()
+    o = ko.run(A, t["tables"], list(occ), t["q_fixed"], -1.0, t["e_rel"], t["vn"],
+               t["kT"], u, t["dt"], t["n_path"], max_steps=n_steps)
+    return o["steps"], time.perf_counter() - t0
+
+
+def write_cpu_inputs(system, run, dopants, tmpdir):
+    """Oracle-side inputs: the oracle's own array (translation classes) and
+    the oracle's process tables over the hop-neighbour list."""
+    import pickle
+    from oracle import ewald_oracle as eo
+    from oracle import kmc_oracle as ko
+    m = system.material
+    A = eo.class_array(m.cartesian_unit_cell_coords, m.lattice_matrix, N_CELLS,
+                       system.alpha, system.r_cut, system.k_cut,
+                       m.dielectric_constant)
+    a_path = Path(tmpdir) / "A.npy"
+    np.save(a_path, A)
+    q = np.zeros(3600)
+    q[dopants] = 1.0
+    tab = {"tables": ko.Tables(system.hop_neighbor_list, "Fe:Fe", np.zeros(3600, int),
+                               12, 0, 12, m.lambda_values["Fe:Fe"], m.v_ab["Fe:Fe"]),
+           "q_fixed": q, "e_rel": np.zeros(3600), "vn": m.vn, "kT": run.temp,
+           "dt": run.time_interval, "n_path": int(run.t_final / run.time_interval) + 1}
+    tab_path = Path(tmpdir) / "tables.pkl"
+    with open(tab_path, "wb") as fh:
+        pickle.dump(tab, fh)
+    return str(a_path), str(tab_path)
+
+
+def reference_arm(args):
+    """--impl reference: the reference's algorithm (oracle port) on all host
+    cores, one trajectory per process as the reference's 'parallel' mode."""
+    import multiprocessing as mp
+    import tempfile
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    from pycd_gb300 import workloads as wl
+    system = wl.corundum(N_CELLS)
+    run = wl.run_for(system, N_CARRIERS, T_FINAL, DT)
+    _, dopants = wl.batched_uniform_sites(seed=3600)
+    tmp = tempfile.mkdtemp()
+    a_path, tab_path = write_cpu_inputs(system, run, dopants, tmp)
+    cores = os.cpu_count() or 1
+    rng = np.random.default_rng(SEED)
+    free = np.setdiff1d(np.arange(3600), dopants)
+    ctx = mp.get_context("spawn")
+    budget = 150.0 / max(1, args.steps + args.warmup)  # seconds per bench step
+    with ctx.Pool(cores) as pool:
+        # calibrate the per-step sample so the whole run stays within minutes
+        jobs = [(a_path, tab_path, rng.choice(free, N_CARRIERS, replace=False),
+                 200, SEED + i) for i in range(cores)]
+        res = pool.map(cpu_port_steps, jobs)
+        per_step = max(r[1] / r[0] for r in res)
+        m = max(50, int(0.8 * budget / per_step))
+        total_steps, total_s = 0, 0.0
+        for it in range(args.warmup + args.steps):
+            jobs = [(a_path, tab_path, rng.choice(free, N_CARRIERS, replace=False),
+                     m, SEED + 1000 * it + i) for i in range(cores)]
+            t0 = time.perf_counter()
+            res = pool.map(cpu_port_steps, jobs)
+            dt = time.perf_counter() - t0
+            if it >= args.warmup:
+                total_steps += sum(r[0] for r in res)
+                total_s += dt
+    value = total_steps / total_s
+    line = {"metric": "KMC steps/s (batched uniform, 3,600 sites, 4 e- + 4 dopants)",
+            "value": value, "unit": "steps/s", "impl": "reference", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * total_s / max(1, args.steps),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "batched uniform corundum 10x10x3 (3,600 sites), "
+                                   "4 electrons + 4 fixed +1 dopants, FP64 array",
+                       "sample_per_step": f"{cores} trajectories x {m} KMC steps"},
+            "cpu_baseline": {"value": value, "unit": "steps/s", "cores": cores,
+                             "kind": "port",
+                             "sample": f"{cores} trajectories x {m} steps per bench "
+                                       f"step, {args.steps} timed steps"},
+            "e2e": {"value": value, "unit": "steps/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def cpu_baseline_1core(system, run, dopants, occ, seconds=10.0):
+    import tempfile
+    tmp = tempfile.mkdtemp()
+    a_path, tab_path = write_cpu_inputs(system, run, dopants, tmp)
+    s, t = cpu_port_steps((a_path, tab_path, occ[0], 200, SEED))
+    n = max(200, int(seconds * s / t))
+    s, t = cpu_port_steps((a_path, tab_path, occ[1], n, SEED + 1))
+    return {"value": s / t, "unit": "steps/s", "cores": 1, "kind": "port",
+            "sample": f"1 trajectory x {s} KMC steps of this workload, NumPy port "
+                      "of the reference loop"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--traj", type=int, default=N_TRAJ)
+    ap.add_argument("--chunk", type=int, default=CHUNK)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--lanes", type=int, default=0)
+    ap.add_argument("--warps", type=int, default=0)
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return reference_arm(args)
+
+    import torch
+    import torch.distributed as dist
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    from pycd_gb300 import _native as nat
+    from pycd_gb300.batch import BatchedKmc, run_batched
+    nat.require_device()
+    global N_TRAJ
+    N_TRAJ = args.traj
+    system, A, tables, run, dopants, occ = build_workload(rank)
+    launch = {}
+    if args.lanes:
+        launch["lanes_per_traj"] = args.lanes
+    if args.warps:
+        launch["warps_per_block"] = args.warps
+    bk = BatchedKmc(tables, occ, seed=SEED, chunk_steps=args.chunk,
+                    traj_offset=rank * N_TRAJ, launch=launch)
+    flush = torch.empty(256 * 2 ** 20, dtype=torch.uint8, device="cuda")
+    for _ in range(args.warmup):
+        bk.step_chunk()
+    torch.cuda.synchronize()
+    steps0 = bk.batch.step.sum().item()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(args.steps)]
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clocks:
+        t0 = time.perf_counter()
+        for i in range(args.steps):
+            flush.fill_(i & 0xFF)  # write 256 MiB (> L2) between chunks
+            ev[i][0].record()
+            bk.step_chunk()
+            ev[i][1].record()
+        torch.cuda.synchronize()
+        if world > 1:
+            dist.barrier()
+        wall = time.perf_counter() - t0
+    kernel_ms = [a.elapsed_time(b) for a, b in ev]
+    steps_done = bk.batch.step.sum().item() - steps0
+    status = bk.status_counts()
+    elapsed = torch.tensor([wall, steps_done], dtype=torch.float64, device="cuda")
+    if world > 1:
+        gathered = [torch.zeros_like(elapsed) for _ in range(world)]
+        dist.all_gather(gathered, elapsed)
+        wall_max = max(float(g[0]) for g in gathered)
+        total_steps = sum(float(g[1]) for g in gathered)
+    else:
+        wall_max, total_steps = wall, float(steps_done)
+    value = total_steps / wall_max
+
+    # plain one-trajectory form (same kernel, same events)
+    plain = time_plain(tables, occ)
+
+    # end to end through the host-buffer entry point
+    e2e = None
+    if not args.no_e2e:
+        A_host = A.cpu().numpy()
+        th = {"nbr": run.site_nbr, "hop": run.site_hop, "lam": run.site_lam,
+              "vab": run.site_vab, "e_rel": run.system_relative_energies,
+              "q_fixed": np.where(np.isin(np.arange(3600), dopants), 1.0, 0.0),
+              "carrier_charge": -1.0, "n_carriers": N_CARRIERS, "vn": run.material.vn,
+              "kT": run.temp, "time_interval": run.time_interval,
+              "n_path_steps": int(run.t_final / run.time_interval) + 1}
+        e2e_steps = args.chunk * args.steps
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        res = run_batched(A_host, th, occ, e2e_steps, seed=SEED + 1,
+                          chunk_steps=args.chunk, launch=launch)
+        torch.cuda.synchronize()
+        e2e_wall = time.perf_counter() - t0
+        e2e = {"value": float(res["step"].sum()) * world / e2e_wall, "unit": "steps/s",
+               "h2d_bytes_per_step": res["h2d_bytes"] / max(1, res["launches"]),
+               "d2h_bytes_per_step": res["d2h_bytes"] / max(1, res["launches"]),
+               "wall_s": e2e_wall}
+
+    hbm, peak_kind = peaks()
+    launch_ms = float(np.mean(kernel_ms))
+    bytes_per_launch = B_STEP * steps_done / max(1, args.steps)
+    achieved = bytes_per_launch / (launch_ms / 1e3) / 1e9
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cpu = cpu_baseline_1core(system, run, dopants, occ)
+    if rank == 0:
+        line = {
+            "metric": "KMC steps/s (batched uniform, 3,600 sites, 4 e- + 4 dopants)",
+            "value": value, "unit": "steps/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * wall_max / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "batched uniform: corundum 10x10x3 = 3,600 sites, "
+                                   "4 electrons + 4 fixed +1 dopants, FP64 Ewald array "
+                                   "(103.7 MB), Philox streams",
+                       "trajectories_per_gpu": N_TRAJ, "steps_per_chunk": args.chunk,
+                       "chunk": "one CUDA-graph launch of the persistent kernel",
+                       "l2": "256 MiB buffer written between timed chunks",
+                       "parallelism": f"replicas x{world}"},
+            "plain_steps_per_s": plain, "batched_over_plain": value / world / plain,
+            "status_counts": status,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm,
+                         "unit": "GB/s", "frac": achieved / hbm, "traffic": None,
+                         "peak_kind": peak_kind,
+                         "bytes_per_step": B_STEP, "launch_ms": launch_ms},
+            "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": args.steps,
+            "clocks": clocks.summary()}
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,276 @@
+/*
+ * pycd_gb300.h - C ABI of the GB300 (sm_103a) lattice-KMC hot path.
+ *
+ * Two parts of PyCD are replaced:
+ *   1. the Ewald precomputed pairwise-energy array,
+ *      System.get_precomputed_array            (PyCD/core.py:1611-1679)
+ *      with pot_r_ewald                        (PyCD/core.py:799-814)
+ *      get_effective_k_vectors                 (PyCD/core.py:816-838)
+ *      pot_k_ewald                             (PyCD/core.py:853-878)
+ *      and the self term                       (PyCD/core.py:1659-1661);
+ *   2. the KMC loop, Run.do_kmc_steps          (PyCD/core.py:2647-2917)
+ *      with get_process_attributes             (PyCD/core.py:1946-1987)
+ *      get_process_rates                       (PyCD/core.py:1989-2050)
+ *      selection / residence time / update     (PyCD/core.py:2796-2830)
+ *      and the path-grid output rows           (PyCD/core.py:2847-2861).
+ *
+ * Conventions
+ *   - Every entry point returns PYCD_OK (0) or a negative PycdStatus.  No C++
+ *     exception crosses this boundary.  pycd_last_error() returns a
+ *     thread-local message for the most recent failure on the calling thread.
+ *   - Pointers named d_* are device pointers owned by the caller; the library
+ *     never frees caller memory.  Pointers named h_* are host pointers.
+ *   - `stream` is a cudaStream_t passed as void* (NULL = legacy default).
+ *     Launches are asynchronous on that stream unless stated otherwise.
+ *   - Units are Hartree atomic units (bohr, Hartree, a.u. time), as in PyCD.
+ *   - Thread safety: distinct calls on distinct streams and buffers are
+ *     independent; the library keeps no global mutable state except the
+ *     per-thread error string.
+ */
+#ifndef PYCD_GB300_H
+#define PYCD_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PYCD_ABI_VERSION 1
+
+#if defined(__GNUC__)
+#define PYCD_API __attribute__((visibility("default")))
+#else
+#define PYCD_API
+#endif
+
+typedef enum PycdStatus {
+  PYCD_OK = 0,
+  PYCD_ERR_INVALID_ARG = -1,   /* bad size, null pointer, unsupported mode  */
+  PYCD_ERR_CUDA = -2,          /* a CUDA runtime call failed                */
+  PYCD_ERR_STALLED = -3,       /* some trajectory had k_total 0 or not finite */
+  PYCD_ERR_BAD_INDEX = -4,     /* a device gather index fell outside its table */
+  PYCD_ERR_NO_DEVICE = -5,     /* no CUDA device / wrong architecture       */
+  PYCD_ERR_WORKSPACE = -6      /* workspace smaller than the required size   */
+} PycdStatus;
+
+/* Per-trajectory status codes written by the KMC kernels (d_status). */
+typedef enum PycdTrajStatus {
+  PYCD_TRAJ_RUNNING = 0,       /* can be advanced further                    */
+  PYCD_TRAJ_DONE = 1,          /* time grid full: end_path_index reached     */
+  PYCD_TRAJ_NEED_UNIFORMS = 2, /* injected uniform stream exhausted; refill  */
+  PYCD_TRAJ_STALLED = 3,       /* k_total == 0 or not finite (core.py:2800)  */
+  PYCD_TRAJ_BAD_INDEX = 4,     /* neighbour / site index out of range        */
+  PYCD_TRAJ_NO_EVENT = 5       /* u1 at or above the last cumulative rate    */
+} PycdTrajStatus;
+
+/* ------------------------------------------------------------------------ */
+/* Library                                                                   */
+/* ------------------------------------------------------------------------ */
+
+/* Thread-local text of the last error on this thread ("" if none). */
+PYCD_API const char* pycd_last_error(void);
+
+/* ABI version compiled into the library (== PYCD_ABI_VERSION). */
+PYCD_API int pycd_abi_version(void);
+
+/* Device properties used by the launch heuristics: SM count, CC major/minor.
+ * Fails with PYCD_ERR_NO_DEVICE when no sm_103 device is current. */
+PYCD_API int pycd_device_info(int32_t* sm_count, int32_t* cc_major, int32_t* cc_minor);
+
+/* ------------------------------------------------------------------------ */
+/* Ewald pairwise-energy array                                               */
+/* ------------------------------------------------------------------------ */
+
+/* Precision / algorithm of the reciprocal-space sum. */
+typedef enum PycdEwaldMode {
+  /* Per-pair sum over k of cos(k . d_ij), d_ij taken from d_pmiv (or the
+   * minimum image of the coordinates when d_pmiv is NULL).  Exactly the
+   * reference's formula for any pmiv; O(N^2 K) FP64.                      */
+  PYCD_EWALD_FP64_DIRECT = 0,
+  /* Feature contraction F F^T with F = [sqrt(w) cos(k.r), sqrt(w) sin(k.r)]
+   * (N x 2K), FP64 throughout.  Valid when every pmiv_ij is r_j - r_i plus
+   * a supercell translation and k . T is a multiple of 2 pi.              */
+  PYCD_EWALD_FP64_GEMM = 1,
+  /* Same contraction on tcgen05 tensor cores: F split into BF16 hi + lo,
+   * three products (hi.hi + hi.lo + lo.hi), FP32 accumulation in TMEM per
+   * K-chunk, FP64 sum across chunks.                                       */
+  PYCD_EWALD_BF16X3 = 2,
+  /* As BF16X3 with TF32 operands (hi + lo split, three products).         */
+  PYCD_EWALD_TF32X3 = 3
+} PycdEwaldMode;
+
+typedef struct PycdEwaldDesc {
+  int64_t n_sites;              /* N                                         */
+  int64_t n_kvec;               /* K: half-space k-vectors kept (k^2<k_cut^2) */
+  const double* d_cart;         /* N x 3 site coordinates (bohr)             */
+  const double* d_pmiv;         /* N x N x 3 min-image vectors, or NULL      */
+  const int32_t* d_kvec;        /* K x 3 integer multiples of the rec. basis */
+  double recip[9];              /* reciprocal basis rows (bohr^-1), includes 2 pi/V */
+  double sim_cell[9];           /* simulation-cell rows for the min image    */
+  double sim_cell_inv[9];       /* inverse of sim_cell                       */
+  int32_t pbc[3];               /* periodic flags                            */
+  double alpha;                 /* Ewald alpha as used by PyCD (bohr^-2)     */
+  double r_cut;                 /* real-space cutoff (bohr), strict <        */
+  double volume;                /* cell volume used by the Fourier prefactor */
+  double dielectric;            /* relative permittivity                     */
+} PycdEwaldDesc;
+
+/* Enumerate the half-space k-vector list of PyCD/core.py:816-838 filtered by
+ * k^2 < k_cut^2 (PyCD/core.py:868), in the reference's order, on the host.
+ * h_kvec may be NULL to query the count only (returned in *n_out).          */
+PYCD_API int pycd_ewald_kvectors(const double recip[9], const int32_t k_max[3],
+                        double k_cut, int32_t* h_kvec, int64_t capacity,
+                        int64_t* n_out);
+
+/* Bytes of device workspace pycd_ewald_build needs for (desc, mode).       */
+PYCD_API int pycd_ewald_workspace_size(const PycdEwaldDesc* desc, int mode,
+                              size_t* bytes);
+
+/* Build the N x N FP64 array (row-major, Hartree) into d_out:
+ *   A = A_real + A_fourier + A_self          (PyCD/core.py:1659-1661)
+ * Replaces System.get_precomputed_array (PyCD/core.py:1611-1679).
+ * d_workspace must hold pycd_ewald_workspace_size bytes (may be NULL when 0).
+ * Timings of the real and Fourier phases are returned in ms when the
+ * pointers are non-NULL (this synchronises the stream).                   */
+PYCD_API int pycd_ewald_build(const PycdEwaldDesc* desc, int mode, double* d_out,
+                     void* d_workspace, size_t workspace_bytes, void* stream,
+                     float* real_ms, float* fourier_ms);
+
+/* phi = A q for a dense charge vector (lattice charges with dopants
+ * overwritten): the background part of np.dot(charge, A[n]-A[o])
+ * (PyCD/core.py:2004-2008).  Also returns E = q^T A q in *d_energy when
+ * d_energy is non-NULL.                                                    */
+PYCD_API int pycd_potential_gemv(const double* d_A, int64_t n_sites,
+                        const double* d_q, double* d_phi, double* d_energy,
+                        void* stream);
+
+/* ------------------------------------------------------------------------ */
+/* KMC                                                                       */
+/* ------------------------------------------------------------------------ */
+
+/* One lattice system: tables shared by every trajectory that runs on it.
+ * Process p of a trajectory is (carrier c = p / n_slots, slot s = p % n_slots)
+ * which is the reference's process order for one carrier species
+ * (PyCD/core.py:1946-1987, 1861-1927).                                      */
+typedef struct PycdKmcSystem {
+  const double* d_A;            /* N x N precomputed array (Hartree)         */
+  const double* d_phi_bg;       /* N: A . q_fixed (lattice + dopant charges) */
+  const double* d_e_rel;        /* N: relative site energies (Hartree)       */
+  const int32_t* d_nbr;         /* N x S: destination site of slot s, -1 none */
+  const double* d_hop;          /* N x S x 3: hop vector of slot s (bohr)    */
+  const double* d_lam;          /* N x S: reorganisation energy lambda       */
+  const double* d_vab;          /* N x S: coupling V_ab                      */
+  const double* d_field_shift;  /* N x S: 0.5 E . hop (or NULL for zero)     */
+  int64_t n_sites;              /* N                                         */
+  int32_t n_slots;              /* S: processes per carrier                  */
+  int32_t n_carriers;           /* carriers per trajectory (one species)     */
+  double carrier_charge;        /* species charge in e (e.g. -1)             */
+  double vn;                    /* attempt frequency (1/a.u. time)           */
+  double kT;                    /* k_B T in Hartree                          */
+  double time_interval;         /* path-grid spacing (a.u. time)             */
+  int64_t n_path_steps;         /* rows of the path grid: int(t_final/dt)+1  */
+} PycdKmcSystem;
+
+/* Trajectory state, structure-of-arrays over T trajectories.  All device
+ * arrays; the kernels read and update them in place so a run can be resumed
+ * chunk by chunk (and snapshotted between chunks).                          */
+typedef struct PycdKmcState {
+  int32_t n_traj;               /* T                                         */
+  int32_t max_carriers;         /* row stride of d_occ and d_disp / 3        */
+  const int32_t* d_sys_index;   /* T: system of each trajectory (NULL = 0)   */
+  int32_t* d_occ;               /* T x max_carriers: current site per carrier */
+  double* d_time;               /* T: simulation time (a.u.)                 */
+  int64_t* d_step;              /* T: KMC steps done                         */
+  int64_t* d_path_index;        /* T: start_path_index of core.py:2781       */
+  double* d_disp;               /* T x 3*max_carriers: displacement since the
+                                   last path row (core.py:2784)             */
+  double* d_last_row;           /* T x 3*max_carriers: path row start-1      */
+  double* d_energy;             /* T: current_state_energy (or NULL)         */
+  int32_t* d_status;            /* T: PycdTrajStatus                          */
+  int64_t* d_u_cursor;          /* T: uniforms consumed (injected mode)      */
+} PycdKmcState;
+
+/* Optional per-trajectory outputs.  Each pointer may be NULL.               */
+typedef struct PycdKmcOutputs {
+  double* d_unwrapped;          /* T x n_path_steps x 3*max_carriers rows     */
+  int64_t unwrapped_stride;     /* elements between trajectories (0 = dense) */
+  double* d_energy_grid;        /* T x n_path_steps                          */
+  double* d_delg0_grid;         /* T x n_path_steps                          */
+  double* d_step_time;          /* T x step_capacity: sim_time after step i  */
+  int32_t* d_step_proc;         /* T x step_capacity: selected process of step i */
+  int64_t step_capacity;        /* columns of d_step_time / d_step_proc      */
+  int64_t step_offset;          /* step i is stored in column i - step_offset */
+  double* d_drift;              /* T x max_carriers x 3: sum hop * k_sel     */
+} PycdKmcOutputs;
+
+/* Source of the two uniforms (u1, u2) each step consumes
+ * (PyCD/core.py:2799, 2802).                                                */
+typedef struct PycdKmcRng {
+  /* Injected stream: T x u_stride doubles, u_count valid per trajectory.
+   * Step i of a trajectory uses u[2*i] then u[2*i+1] (counted from the
+   * cursor).  When it runs out the trajectory stops with
+   * PYCD_TRAJ_NEED_UNIFORMS and resumes after a refill.                     */
+  const double* d_uniforms;
+  int64_t u_stride;
+  int64_t u_count;
+  /* Counter-based stream used when d_uniforms is NULL: Philox4x32-10 with
+   * key = seed and counter = (step, trajectory id + traj_offset).           */
+  uint64_t seed;
+  uint64_t traj_offset;
+} PycdKmcRng;
+
+/* Launch shape of the persistent kernel (0 fields = heuristic).  The two
+ * shape maxima are filled by pycd_kmc_upload_systems and are required by
+ * pycd_kmc_advance_uploaded (pycd_kmc_advance computes them itself).       */
+typedef struct PycdKmcLaunch {
+  int32_t lanes_per_traj;       /* 1..32 (power of two); 0 = from processes  */
+  int32_t warps_per_block;      /* 1..8; 0 = 4                               */
+  int32_t blocks;               /* grid size; 0 = cover all trajectories     */
+  int32_t max_processes;        /* max n_carriers * n_slots over the systems */
+  int32_t max_carriers;         /* max n_carriers over the systems           */
+  int32_t reserved;
+} PycdKmcLaunch;
+
+/* Advance every trajectory by up to max_steps KMC steps, or until its path
+ * grid is full (core.py:2787), its injected uniforms run out, or it stalls.
+ * `systems` is an array of n_systems host descriptors (copied to a device
+ * table in d_workspace); each trajectory runs on systems[d_sys_index[t]].
+ * The same device step function serves the one-trajectory (plain) form and
+ * the batched form, so their event streams are identical.
+ * Workspace: pycd_kmc_workspace_size(n_systems).                            */
+PYCD_API int pycd_kmc_workspace_size(int32_t n_systems, size_t* bytes);
+
+PYCD_API int pycd_kmc_advance(const PycdKmcSystem* systems, int32_t n_systems,
+                     const PycdKmcState* state, const PycdKmcOutputs* out,
+                     const PycdKmcRng* rng, int64_t max_steps,
+                     const PycdKmcLaunch* launch, void* d_workspace,
+                     size_t workspace_bytes, void* stream);
+
+/* Upload `systems` into d_workspace without launching (for CUDA-graph
+ * capture of pycd_kmc_advance_uploaded, which then does no host->device
+ * copy).  Synchronous with respect to `stream`.  Fills the shape maxima of
+ * *launch (its other fields are left as they are).                          */
+PYCD_API int pycd_kmc_upload_systems(const PycdKmcSystem* systems, int32_t n_systems,
+                            void* d_workspace, size_t workspace_bytes,
+                            void* stream, PycdKmcLaunch* launch);
+
+/* As pycd_kmc_advance, with the system table already in d_workspace.       */
+PYCD_API int pycd_kmc_advance_uploaded(int32_t n_systems, const PycdKmcState* state,
+                              const PycdKmcOutputs* out, const PycdKmcRng* rng,
+                              int64_t max_steps, const PycdKmcLaunch* launch,
+                              void* d_workspace, size_t workspace_bytes,
+                              void* stream);
+
+/* Philox4x32-10 uniforms exactly as the kernels draw them (for tests and
+ * for replaying a batched trajectory in another form): fills
+ * h_or_d_out[2*i + {0,1}] for steps [step0, step0 + n_steps) of trajectory
+ * `traj`.  d_out is a device pointer.                                      */
+PYCD_API int pycd_philox_uniforms(uint64_t seed, uint64_t traj, int64_t step0,
+                         int64_t n_steps, double* d_out, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PYCD_GB300_H */

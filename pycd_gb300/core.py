@@ -1,0 +1,549 @@
+"""Drop-in ``Material`` / ``Neighbors`` / ``System`` / ``Run`` for the PyCD
+lattice-KMC hot path.
+
+``System.get_precomputed_array`` (PyCD/core.py:1611-1679) builds the N x N
+FP64 Ewald array on the GPU; ``Run.do_kmc_steps`` (PyCD/core.py:2647-2917)
+runs every trajectory in the GPU KMC kernel and writes the reference's output
+files.  Host code here only prepares tables, restores the per-trajectory
+MT19937 streams (``random``, as PyCD/core.py:2566-2580, 2694-2695) and writes
+files; there is no CPU compute path.
+"""
+import pickle
+import random as rnd
+from datetime import datetime
+from pathlib import Path
+
+import numpy as np
+
+from . import constants
+from . import _native as nat
+from .io import generate_report
+from .lattice import Material, Neighbors, ReturnValues  # noqa: F401
+
+
+class System(object):
+    """Ewald geometry and parameters (PyCD/core.py:671-797)."""
+
+    def __init__(self, material_info, material_neighbors, hop_neighbor_list,
+                 pairwise_min_image_vector_data, alpha, r_cut, k_cut,
+                 precision_parameters=None, step_system_size_array=(),
+                 step_hop_neighbor_master_list=()):
+        self.start_time = datetime.now()
+        self.material = material_info
+        self.neighbors = material_neighbors
+        self.hop_neighbor_list = hop_neighbor_list
+        self.step_system_size_array = step_system_size_array
+        self.step_hop_neighbor_master_list = step_hop_neighbor_master_list
+        self.pbc = self.neighbors.pbc
+        self.system_size = self.neighbors.system_size
+        self.num_cells = self.system_size.prod()
+        self.pairwise_min_image_vector_data = pairwise_min_image_vector_data
+        # Ewald cell: np.multiply(system_size, lattice) scales COLUMNS
+        # (core.py:709-710); it equals the supercell only when s_i = s_j
+        # wherever lattice[i][j] != 0.  Kept as the reference has it.
+        self.translational_matrix = np.multiply(self.system_size,
+                                                self.material.lattice_matrix)
+        T = self.translational_matrix
+        self.system_volume = abs(np.dot(T[0], np.cross(T[1], T[2])))
+        self.reciprocal_lattice_matrix = (
+            2 * np.pi / self.system_volume
+            * np.array([np.cross(T[1], T[2]), np.cross(T[2], T[0]),
+                        np.cross(T[0], T[1])]))
+        self.translational_vector_length = np.linalg.norm(T, axis=1)
+        self.reciprocal_lattice_vector_length = np.linalg.norm(
+            self.reciprocal_lattice_matrix, axis=1)
+        self.system_class_index_list = np.tile(
+            self.material.unit_cell_class_list, self.num_cells)
+        m = self.material
+        self.num_neighbors = np.zeros(m.num_species_types, int)
+        for si, sp in enumerate(m.species_types):
+            key = m.hop_element_types[sp][0]
+            if key in m.neighbor_cutoff_dist and hop_neighbor_list is not None \
+                    and key in hop_neighbor_list:
+                for t in range(len(m.neighbor_cutoff_dist[key][0])):
+                    self.num_neighbors[si] += \
+                        hop_neighbor_list[key][0][t].num_neighbors[0]
+        # alpha, r_cut, k_cut unit conversions (core.py:767-784); alpha is
+        # used as eta^2 in bohr^-2 throughout
+        self.alpha = alpha / constants.ANG2BOHR if np.isreal(alpha) else alpha
+        self.r_cut = r_cut * constants.ANG2BOHR if np.isreal(r_cut) else r_cut
+        if isinstance(k_cut, list):
+            self.k_cut = k_cut
+        elif np.isreal(k_cut):
+            self.k_cut = k_cut / constants.ANG2BOHR
+        else:
+            self.k_cut = k_cut
+        self.precision_parameters = precision_parameters
+        self.last_build_info = None
+
+    def _ewald_parameters(self):
+        """Numeric alpha / r_cut / k_cut (user-specified, or a k_max list as
+        core.py:1377-1382).  The automatic choices ('optimal', 'converge',
+        'simulation_cell') are parameter searches outside this hot path."""
+        if not (np.isreal(self.alpha) and np.isreal(self.r_cut)):
+            raise NotImplementedError(
+                "automatic Ewald parameter selection is not part of this "
+                "package; give numeric alpha and r_cut")
+        if isinstance(self.k_cut, list):
+            k_cut = 1.10 * max(np.asarray(self.k_cut)
+                               * self.reciprocal_lattice_vector_length)
+            choice = "user-specified (k_max)"
+        elif np.isreal(self.k_cut):
+            k_cut, choice = self.k_cut, "user-specified"
+        else:
+            raise NotImplementedError("automatic k_cut selection is not part "
+                                      "of this package")
+        return float(self.alpha), float(self.r_cut), float(k_cut), choice
+
+    def get_precomputed_array_device(self, precision="auto", pmiv="system",
+                                     stream=None):
+        """Build the array on the GPU and keep it there (CUDA float64)."""
+        from .ewald import build_device_array
+        alpha, r_cut, k_cut, _ = self._ewald_parameters()
+        A, info = build_device_array(self, alpha, r_cut, k_cut, precision,
+                                     pmiv, stream)
+        self.last_build_info = info
+        return A
+
+    def get_precomputed_array(self, dst_path, compute_energy_contributions=0,
+                              return_k_vector_data=0, precision="auto"):
+        """(A, dst_path) with A the (N, N) float64 host array, plus the
+        ``precomputed_array.log`` report of PyCD/core.py:1675-1678."""
+        import torch
+        alpha, r_cut, k_cut, kchoice = self._ewald_parameters()
+        A_dev = self.get_precomputed_array_device(precision)
+        torch.cuda.synchronize()
+        A = A_dev.cpu().numpy()
+        info = self.last_build_info
+        k_max = info["k_max"]
+        num_k_vectors = int(np.ceil(np.prod(2 * k_max + 1) * np.pi / 6 - 1))
+        n = self.neighbors.num_system_elements
+        tau_r = info["real_ms"] / max(1, n * n)
+        tau_f = info["fourier_ms"] / max(1, n * n * max(1, info["n_kvec"]))
+        lines = [
+            f"tau_ratio, (tau_r/tau_f): {tau_r / tau_f if tau_f else 0.0:.3e}\n",
+            f"time_ratio, (time_r/time_f): "
+            f"{info['real_ms'] / info['fourier_ms'] if info['fourier_ms'] else 0.0:.3e}\n\n",
+            f"alpha: {alpha * constants.ANG2BOHR:.3e} / angstrom (user-specified)\n",
+            f"r_cut: {r_cut / constants.ANG2BOHR:.3e} angstrom (user-specified)\n",
+            f"k_cut: {k_cut * constants.ANG2BOHR:.3e} / angstrom ({kchoice})\n",
+            f"k_max: [{k_max[0]}, {k_max[1]}, {k_max[2]}]\n",
+            f"number of k-vectors: {num_k_vectors}\n",
+            f"k-vectors used: {info['n_kvec']}\n",
+            f"build: {info['mode']} on the GPU\n\n",
+        ]
+        if compute_energy_contributions:
+            m = self.material
+            q = np.tile(np.array([m.charge_types["full"][m.element_types[e]]
+                                  for e in m.element_type_index_list]),
+                        self.num_cells)
+            total = float(q @ A @ q)
+            lines.append(f"Total system energy (neutral): "
+                         f"{total / constants.EV2HARTREE} eV\n\n")
+        if dst_path is not None:
+            Path(dst_path).mkdir(parents=True, exist_ok=True)
+            generate_report(self.start_time, Path(dst_path), "precomputed_array",
+                            1, "".join(lines))
+        return (A, dst_path)
+
+
+class Run(object):
+    """KMC run (PyCD/core.py:1682-1933 set-up, 2647-2917 loop)."""
+
+    # steps per kernel launch in the drop-in path; each launch consumes at
+    # most this many pairs of host-generated MT19937 uniforms
+    UNIFORM_BLOCK = 1 << 16
+
+    def __init__(self, system, precomputed_array, temp, ion_charge_type,
+                 species_charge_type, n_traj, t_final, time_interval,
+                 species_count, initial_occupancy, relative_energies,
+                 external_field, doping):
+        self.start_time = datetime.now()
+        self.system = system
+        self.material = m = system.material
+        self.neighbors = system.neighbors
+        self.precomputed_array = precomputed_array
+        self.temp = temp * constants.K2AUTEMP
+        self.ion_charge_type = ion_charge_type
+        self.species_charge_type = species_charge_type
+        self.n_traj = int(n_traj)
+        self.t_final = t_final * constants.SEC2AUTIME
+        self.time_interval = time_interval * constants.SEC2AUTIME
+        self.species_count = np.asarray(species_count)
+        self.initial_occupancy = initial_occupancy
+        self.system_size = system.system_size
+        self.relative_energies = relative_energies
+        # per-site relative energies (core.py:1716-1730)
+        uc_rel = np.zeros(m.total_elements_per_unit_cell)
+        start = 0
+        for ei in range(m.num_element_types):
+            end = start + m.n_elements_per_unit_cell[ei]
+            if m.num_classes[ei] != 1:
+                et = m.element_types[ei]
+                uc_rel[start:end] += [
+                    relative_energies["class_index"][et][ci] * constants.EV2HARTREE
+                    for ci in m.unit_cell_class_list[start:end]]
+            start = end
+        self.undoped_system_relative_energies = np.tile(uc_rel, system.num_cells)
+        self.system_relative_energies = np.copy(self.undoped_system_relative_energies)
+        self.n_proc = int(np.dot(self.species_count, system.num_neighbors))
+        self.head_start_n_elements_per_unit_cell_cum_sum = [
+            m.n_elements_per_unit_cell[:e].sum()
+            for e in self.neighbors.element_type_indices]
+        # electric field (core.py:1748-1761)
+        ef = external_field["electric"]
+        self.electric_field_mag = ef["mag"]
+        if ef["active"]:
+            self.electric_field_active = 1
+            fdir = np.asarray(ef["dir"])
+            if ef["ld"] == 1:
+                fdir = np.dot(fdir, m.lattice_matrix)
+            self.electric_field = ef["mag"] * (fdir / np.linalg.norm(fdir))
+        else:
+            self.electric_field_active = 0
+            self.electric_field = np.zeros(self.neighbors.n_dim)
+        # doping (core.py:1763-1781)
+        self.doping = doping
+        self.doping_active = int(bool(np.any(doping["num_dopants"])))
+        if self.doping_active:
+            self.dopant_element_types, self.substitution_element_types = [], []
+            self.dopant_species_types = []
+            for mp in doping["doping_element_map"]:
+                sub, dop = mp.split(m.element_type_delimiter)
+                self.dopant_element_types.append(dop)
+                self.substitution_element_types.append(sub)
+                self.dopant_species_types.append(
+                    m.element_type_to_species_map[sub][0])
+        # one active carrier species: the reference's process bookkeeping
+        # restarts its species index per type (core.py:1876-1878), so only
+        # single-species runs are meaningful there
+        active = [i for i, c in enumerate(self.species_count) if c]
+        if len(active) > 1:
+            raise NotImplementedError(
+                "runs with more than one carrier species type are not "
+                "supported (the reference's per-species process indices "
+                "restart at 0 for each type)")
+        self.active_species_index = active[0] if active else None
+        self.total_species = int(self.species_count.sum())
+        self.species_charge_list = [
+            m.species_charge_list[species_charge_type][i]
+            for i, c in enumerate(self.species_count) for _ in range(c)]
+        self._build_site_tables()
+
+    # -- per-(site, slot) process tables (core.py:1823-1927) ----------------
+    def _build_site_tables(self):
+        m, sysm = self.material, self.system
+        N = self.neighbors.num_system_elements
+        si = self.active_species_index
+        if si is None:
+            self.n_slots = 0
+            return
+        sp = m.species_types[si]
+        key = m.hop_element_types[sp][0]
+        et = m.species_to_element_type_map[sp][0]
+        eti = m.element_types.index(et)
+        S = int(sysm.num_neighbors[si])
+        self.n_slots = S
+        self.hop_element_type = key
+        nbr = np.full((N, S), -1, np.int32)
+        hop = np.zeros((N, S, 3))
+        lam = np.zeros((N, S))
+        vab = np.zeros((N, S))
+        shift = np.zeros((N, S))
+        tpc = m.total_elements_per_unit_cell
+        per_cell = m.n_elements_per_unit_cell[eti]
+        head = m.n_elements_per_unit_cell[:eti].sum()
+        hl = sysm.hop_neighbor_list[key]
+        for cell in range(int(self.system.num_cells)):
+            for e in range(per_cell):
+                site = cell * tpc + head + e
+                eei = cell * per_cell + e
+                ci = sysm.system_class_index_list[site]
+                s = 0
+                for t, obj in enumerate(hl[ci][:len(m.neighbor_cutoff_dist[key][ci])]):
+                    idx = obj.neighbor_system_element_indices[eei]
+                    vecs = obj.displacement_vector_list[eei]
+                    for j in range(len(idx)):
+                        if s >= S:
+                            raise ValueError("site %d has more hop neighbours "
+                                             "than the %d processes per carrier"
+                                             % (site, S))
+                        nbr[site, s] = idx[j]
+                        hop[site, s] = vecs[j]
+                        lam[site, s] = m.lambda_values[key][ci][t]
+                        vab[site, s] = m.v_ab[key][ci][t]
+                        if self.electric_field_active:
+                            shift[site, s] = 0.5 * np.dot(self.electric_field, vecs[j])
+                        s += 1
+                if s != S:
+                    raise ValueError("site %d has %d hop neighbours, expected %d"
+                                     % (site, s, S))
+        self.site_nbr, self.site_hop = nbr, hop
+        self.site_lam, self.site_vab = lam, vab
+        self.site_field_shift = shift if self.electric_field_active else None
+        self.carrier_charge = float(
+            m.species_charge_list[self.species_charge_type][si])
+
+    # -- charges (core.py:2530-2564) ----------------------------------------
+    def base_charge_config(self):
+        m = self.material
+        uc = np.array([m.charge_types[self.ion_charge_type][m.element_types[e]]
+                       for e in m.element_type_index_list])
+        return np.tile(uc, self.system.num_cells)[:, np.newaxis]
+
+    def fixed_charge_config(self, dopant_site_indices):
+        """Lattice charges with dopant sites overwritten (no carriers)."""
+        q = self.base_charge_config()
+        if self.doping_active:
+            for dop, sites in dopant_site_indices.items():
+                q[sites] = self.doping["charge"][self.ion_charge_type][dop]
+        return q
+
+    def charge_config(self, occupancy, dopant_site_indices):
+        q = self.fixed_charge_config(dopant_site_indices)
+        for sti in range(self.material.num_species_types):
+            s0 = self.species_count[:sti].sum()
+            s1 = s0 + self.species_count[sti]
+            q[list(occupancy[s0:s1])] += \
+                self.material.species_charge_list[self.species_charge_type][sti]
+        return q
+
+    # -- initial occupancy (core.py:2478-2528), MT19937 semantics -----------
+    def generate_initial_occupancy(self, dopant_site_indices):
+        m = self.material
+        occupancy = []
+        for sti, num in enumerate(self.species_count):
+            sp = m.species_types[sti]
+            if self.doping_active:
+                for mi, dsp in enumerate(self.dopant_species_types):
+                    nd = self.doping["num_dopants"][mi]
+                    if (self.doping["site_charge_initiation"][mi] == "yes"
+                            and dsp == sp and nd and num):
+                        de = self.dopant_element_types[mi]
+                        occupancy.extend(rnd.sample(dopant_site_indices[de], num)[:])
+                        num -= len(dopant_site_indices[de][:num])
+            if sp in self.initial_occupancy:
+                occupancy.extend([i for i in self.initial_occupancy[sp]])
+                num -= len(self.initial_occupancy[sp])
+            if num:
+                sites = []
+                for el in m.species_to_element_type_map[sp]:
+                    ei = m.element_types.index(el)
+                    offs = np.repeat(np.arange(0, m.total_elements_per_unit_cell
+                                               * self.system.num_cells,
+                                               m.total_elements_per_unit_cell),
+                                     m.n_elements_per_unit_cell[ei])
+                    idx = (np.tile(m.n_elements_per_unit_cell[:ei].sum()
+                                   + np.arange(m.n_elements_per_unit_cell[ei]),
+                                   self.system.num_cells) + offs)
+                    sites.extend(list(idx))
+                    sites = [i for i in sites if i not in occupancy]
+                occupancy.extend(rnd.sample(sites, num)[:])
+        return occupancy
+
+    # -- per-trajectory seeds (core.py:2566-2580) ---------------------------
+    def preproduction(self, dst_path, random_seed):
+        dst_path = Path(dst_path)
+        rnd.seed(random_seed)
+        seeds = [rnd.random() for _ in range(self.n_traj)]
+        for ti in range(self.n_traj):
+            d = dst_path / f"traj{ti + 1}"
+            d.mkdir(parents=True, exist_ok=True)
+            rnd.seed(seeds[ti])
+            with open(d / "initial_rnd_state.dump", "wb") as fh:
+                pickle.dump(rnd.getstate(), fh)
+        if self.doping_active:
+            for ti in range(self.n_traj):
+                d = dst_path / f"traj{ti + 1}"
+                if not (d / "site_indices.npy").exists() and \
+                        not (dst_path / "site_indices.npy").exists():
+                    raise NotImplementedError(
+                        "dopant placement is not part of this package; write "
+                        "site_indices.npy (see pycd_gb300.doping) first")
+        return None
+
+    def _load_doping(self, traj_dir):
+        """Dopant sites and per-site energy shifts from site_indices.npy
+        (core.py:2723-2764)."""
+        self.system_relative_energies = np.copy(self.undoped_system_relative_energies)
+        if not self.doping_active:
+            return {}
+        pairwise = ("pairwise" in self.doping["insertion_type"] and
+                    self.doping["num_dopants"][
+                        self.doping["insertion_type"].index("pairwise")] != 0)
+        path = (traj_dir.parent if pairwise else traj_dir) / "site_indices.npy"
+        data = np.load(path)
+        sites, types, shells = data[:, 0], data[:, 1], data[:, 3]
+        dopant_site_indices = {}
+        for ai in np.where(shells == 0)[0]:
+            de = self.dopant_element_types[types[ai]]
+            dopant_site_indices.setdefault(de, []).append(int(sites[ai]))
+        for i in range(len(types)):
+            de = self.dopant_element_types[types[i]]
+            mi = self.dopant_element_types.index(de)
+            sub = self.substitution_element_types[mi]
+            if shells[i] < len(self.relative_energies["doping"][sub][mi]):
+                self.system_relative_energies[sites[i]] += (
+                    self.relative_energies["doping"][sub][mi][shells[i]]
+                    * constants.EV2HARTREE)
+        return dopant_site_indices
+
+    def device_tables(self, A_device=None, dopant_site_indices=None):
+        """KmcTables for the current doping (A may already be on the GPU)."""
+        from .kmc import KmcTables
+        A = self.precomputed_array if A_device is None else A_device
+        q_fixed = self.fixed_charge_config(dopant_site_indices or {})[:, 0]
+        num_path = int(self.t_final / self.time_interval) + 1
+        return KmcTables(
+            A, self.site_nbr, self.site_hop, self.site_lam, self.site_vab,
+            self.system_relative_energies, q_fixed, self.carrier_charge,
+            self.total_species, self.material.vn, self.temp, self.time_interval,
+            num_path, field_shift=self.site_field_shift)
+
+    # -- the KMC loop -------------------------------------------------------
+    def do_kmc_steps(self, dst_path, output_data, random_seed, compute_mode):
+        """Run every trajectory on the GPU and write the reference's files
+        (core.py:2863-2906) with the same 'ab' append semantics."""
+        import torch
+        from .kmc import KmcBatch, KmcEngine
+        nat.require_device()
+        dst_path = Path(dst_path)
+        if compute_mode != "parallel":
+            self.preproduction(dst_path, random_seed)
+        num_path = int(self.t_final / self.time_interval) + 1
+        ue = output_data["unwrapped_traj"]
+        if not ue["write"]:
+            raise ValueError("output_data['unwrapped_traj']['write'] must be 1")
+        every_step = bool(ue.get("write_every_step", 0))
+        want = lambda k: k in output_data and output_data[k]["write"]
+        system_charge = np.dot(self.species_count,
+                               self.material.species_charge_list[self.species_charge_type])
+        ewald_neut = -(np.pi * system_charge ** 2
+                       / (2 * self.system.system_volume * self.system.alpha))
+        A_dev = torch.as_tensor(np.ascontiguousarray(self.precomputed_array,
+                                                     np.float64)).cuda()
+        drift = np.zeros((self.n_traj, self.total_species, 3)) \
+            if self.electric_field_active else None
+        self.last_run_steps = []
+        for ti in range(self.n_traj):
+            traj_dir = (dst_path / f"traj{ti + 1}") if compute_mode != "parallel" \
+                else dst_path
+            traj_dir.mkdir(parents=True, exist_ok=True)
+            with open(traj_dir / "initial_rnd_state.dump", "rb") as fh:
+                rnd.setstate(pickle.load(fh))
+            dopants = self._load_doping(traj_dir)
+            occ = self.generate_initial_occupancy(dopants)
+            occupancy_list = [list(occ)] if self.doping_active else None
+            q = self.charge_config(occ, dopants)
+            qq = np.multiply(q.transpose(), q)
+            energy0 = ewald_neut + np.sum(np.multiply(qq, self.precomputed_array))
+            tables = self.device_tables(A_dev, dopants)
+            batch = KmcBatch(np.asarray(occ)[None, :], energy0=[energy0],
+                             unwrapped_rows=num_path,
+                             step_capacity=self.UNIFORM_BLOCK,
+                             energy_grid_rows=num_path if want("energy") else None,
+                             delg0_grid_rows=num_path if want("delg_0") else None,
+                             drift=self.electric_field_active)
+            engine = KmcEngine(tables)
+            times, procs = [], []
+            ubuf = torch.empty((1, 2 * self.UNIFORM_BLOCK), dtype=torch.float64,
+                               device="cuda")
+            while True:
+                u = np.fromiter((rnd.random() for _ in range(2 * self.UNIFORM_BLOCK)),
+                                dtype=np.float64, count=2 * self.UNIFORM_BLOCK)
+                ubuf.copy_(torch.from_numpy(u)[None, :])
+                batch.u_cursor.zero_()
+                batch.step_offset = int(batch.step.item())
+                engine.advance(batch, self.UNIFORM_BLOCK,
+                               engine.rng_struct(ubuf))
+                torch.cuda.synchronize()
+                n_done = int(batch.step.item()) - batch.step_offset
+                times.append(batch.step_time[0, :n_done].cpu().numpy().copy())
+                procs.append(batch.step_proc[0, :n_done].cpu().numpy().copy())
+                status = int(batch.status.item())
+                if status == nat.TRAJ_NEED_UNIFORMS:
+                    batch.status.zero_()
+                    continue
+                if status == nat.TRAJ_DONE:
+                    break
+                raise nat.NativeError(
+                    nat.ERR_STALLED if status == nat.TRAJ_STALLED else nat.ERR_BAD_INDEX,
+                    "trajectory %d stopped with status %d after %d steps "
+                    "(k_total zero/not finite, or no event selected)"
+                    % (ti + 1, status, int(batch.step.item())))
+            step_proc = np.concatenate(procs) if procs else np.zeros(0, np.int32)
+            self.last_run_steps.append(step_proc)
+            time_data = np.concatenate([[0.0]] + times)
+            if self.doping_active:
+                occupancy_list.extend(self._replay_occupancy(occ, step_proc)[1:])
+            if every_step:
+                unwrapped = self._every_step_rows(occ, step_proc)
+            else:
+                unwrapped = batch.unwrapped[0, :, :3 * self.total_species].cpu().numpy()
+            if drift is not None:
+                drift[ti] = batch.drift[0, :self.total_species].cpu().numpy()
+            arrays = {"unwrapped_traj": unwrapped, "time": time_data,
+                      "wrapped_traj": np.zeros((num_path, self.total_species * 3)),
+                      "potential": np.zeros((num_path, self.total_species))}
+            if want("energy"):
+                arrays["energy"] = batch.energy_grid[0].cpu().numpy()
+            if want("delg_0"):
+                arrays["delg_0"] = batch.delg0_grid[0].cpu().numpy()
+            for kind, attrs in output_data.items():
+                if attrs.get("write") and kind in arrays:
+                    with open(traj_dir / attrs["file_name"], "ab") as fh:
+                        np.save(fh, arrays[kind])
+            if self.doping_active:
+                np.save(traj_dir / "occupancy.npy",
+                        np.asarray(occupancy_list, dtype=int))
+        prefix = ""
+        if self.electric_field_active:
+            prefix = self._drift_mobility_report(drift, dst_path)
+        generate_report(self.start_time, dst_path, "Run", 1, prefix)
+        return None
+
+    def _replay_occupancy(self, occ0, step_proc):
+        occ = list(occ0)
+        out = [list(occ)]
+        S = self.n_slots
+        for p in step_proc:
+            c, s = divmod(int(p), S)
+            occ[c] = int(self.site_nbr[occ[c], s])
+            out.append(list(occ))
+        return out
+
+    def _every_step_rows(self, occ0, step_proc):
+        """write_every_step rows: row 0 is zero and the first hop is not
+        recorded, as core.py:2832-2843 does."""
+        S = self.n_slots
+        occ = list(occ0)
+        rows = np.zeros((max(1, len(step_proc)), 3 * self.total_species))
+        for i, p in enumerate(step_proc):
+            c, s = divmod(int(p), S)
+            h = self.site_hop[occ[c], s]
+            occ[c] = int(self.site_nbr[occ[c], s])
+            if i > 0:
+                rows[i] = rows[i - 1]
+                rows[i, 3 * c:3 * c + 3] += h
+        return rows
+
+    def _drift_mobility_report(self, drift_velocity_array, dst_path):
+        mob_au = (np.dot(drift_velocity_array, self.electric_field)
+                  / self.electric_field_mag ** 2)
+        mob = mob_au * (constants.BOHR2CM ** 2 * constants.SEC2AUTIME
+                        * constants.V2AUPOT)
+        with open(Path(dst_path) / "drift_mobility.dat", "wb") as fh:
+            np.savetxt(fh, mob)
+        lines = []
+        start = 0
+        for si, num in enumerate(self.species_count):
+            end = start + num
+            if num:
+                sp = self.material.species_types[si]
+                avg = np.mean(mob[:, start:end], axis=1)
+                lines.append(f"Estimated value of {sp} drift mobility is: "
+                             f"{np.mean(avg):4.3e} cm2/V.s.\n")
+                lines.append(f"Standard error of mean in {sp} drift mobility is: "
+                             f"{np.std(avg) / np.sqrt(self.n_traj):4.3e} cm2/V.s.\n")
+            start = end
+        return "".join(lines)

@@ -1,0 +1,308 @@
+// extern "C" entry points of libpycd_gb300 (declared in include/pycd_gb300.h).
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <vector>
+
+#include "common.cuh"
+
+namespace pycd {
+
+static thread_local char g_err[1024] = {0};
+
+void set_error(const char* fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_err, sizeof(g_err), fmt, ap);
+  va_end(ap);
+}
+
+void clear_error() { g_err[0] = 0; }
+
+int cuda_fail(cudaError_t e, const char* what, const char* file, int line) {
+  set_error("%s failed at %s:%d: %s (%s)", what, file, line,
+            cudaGetErrorName(e), cudaGetErrorString(e));
+  return PYCD_ERR_CUDA;
+}
+
+// defined in ewald.cu / kmc.cu
+int ewald_validate(const PycdEwaldDesc* d, int mode);
+size_t ewald_workspace_bytes(const PycdEwaldDesc* d, int mode);
+size_t ewald_split_workspace_bytes(const PycdEwaldDesc* d, int mode);
+int ewald_build(const PycdEwaldDesc* d, int mode, double* out, void* ws,
+                size_t ws_bytes, cudaStream_t s, float* real_ms,
+                float* fourier_ms);
+int potential_gemv(const double* A, int64_t n, const double* q, double* phi,
+                   double* energy, cudaStream_t s);
+
+struct KmcArgs {
+  const PycdKmcSystem* systems;
+  int32_t n_systems;
+  PycdKmcState st;
+  PycdKmcOutputs out;
+  PycdKmcRng rng;
+  int64_t max_steps;
+};
+int kmc_launch(const KmcArgs& a, int max_np, int max_nc,
+               const PycdKmcLaunch* launch, cudaStream_t s);
+int philox_launch(uint64_t seed, uint64_t traj, int64_t step0, int64_t n,
+                  double* out, cudaStream_t s);
+int kmc_preload();
+
+}  // namespace pycd
+
+using namespace pycd;
+
+// Header of the device-resident system table kept in the KMC workspace: the
+// shape maxima the launch heuristic needs, then the descriptor array.
+struct KmcTableHeader {
+  int32_t n_systems;
+  int32_t max_np;
+  int32_t max_nc;
+  int32_t pad;
+};
+static_assert(sizeof(KmcTableHeader) == 16, "header layout");
+
+static size_t kmc_ws_bytes(int32_t n_systems) {
+  return 256 + sizeof(PycdKmcSystem) * (size_t)(n_systems > 0 ? n_systems : 1);
+}
+
+extern "C" {
+
+const char* pycd_last_error(void) { return g_err; }
+
+int pycd_abi_version(void) { return PYCD_ABI_VERSION; }
+
+int pycd_device_info(int32_t* sm_count, int32_t* cc_major, int32_t* cc_minor) {
+  clear_error();
+  int dev = 0, n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (e != cudaSuccess || n == 0) {
+    set_error("no CUDA device: %s", cudaGetErrorString(e));
+    return PYCD_ERR_NO_DEVICE;
+  }
+  PYCD_CUDA(cudaGetDevice(&dev));
+  cudaDeviceProp p;
+  PYCD_CUDA(cudaGetDeviceProperties(&p, dev));
+  if (sm_count) *sm_count = p.multiProcessorCount;
+  if (cc_major) *cc_major = p.major;
+  if (cc_minor) *cc_minor = p.minor;
+  if (!(p.major == 10 && p.minor == 3)) {
+    set_error("device %s is sm_%d%d; this library is built for sm_103a",
+              p.name, p.major, p.minor);
+    return PYCD_ERR_NO_DEVICE;
+  }
+  return PYCD_OK;
+}
+
+// Half-space k-vector list of PyCD/core.py:816-838 with the k^2 < k_cut^2
+// filter of core.py:868: grid points (m0, m1, m2) in C order over
+// [-k_max, k_max]^3, excluding 0, keeping the first member of every +-m
+// pair, i.e. exactly the points that precede the origin in that order.
+int pycd_ewald_kvectors(const double recip[9], const int32_t k_max[3],
+                        double k_cut, int32_t* h_kvec, int64_t capacity,
+                        int64_t* n_out) {
+  clear_error();
+  PYCD_REQUIRE(recip && k_max && n_out, "pycd_ewald_kvectors: NULL argument");
+  for (int c = 0; c < 3; ++c)
+    PYCD_REQUIRE(k_max[c] >= 0 && k_max[c] < 100000, "bad k_max[%d]", c);
+  const double kc2 = k_cut * k_cut;
+  int64_t n = 0;
+  for (int a = -k_max[0]; a <= k_max[0]; ++a)
+    for (int b = -k_max[1]; b <= k_max[1]; ++b)
+      for (int c = -k_max[2]; c <= k_max[2]; ++c) {
+        // first-of-pair: strictly before the origin in C order
+        if (a > 0 || (a == 0 && (b > 0 || (b == 0 && c >= 0)))) goto done;
+        {
+          double v[3];
+          for (int j = 0; j < 3; ++j)
+            v[j] = (a * recip[0 * 3 + j] + b * recip[1 * 3 + j]) +
+                   c * recip[2 * 3 + j];
+          const double k2 = fma(v[2], v[2], fma(v[1], v[1], v[0] * v[0]));
+          if (k2 < kc2) {
+            if (h_kvec) {
+              if (n >= capacity) {
+                set_error("k-vector capacity %lld exceeded", (long long)capacity);
+                return PYCD_ERR_INVALID_ARG;
+              }
+              h_kvec[3 * n] = a;
+              h_kvec[3 * n + 1] = b;
+              h_kvec[3 * n + 2] = c;
+            }
+            ++n;
+          }
+        }
+      }
+done:
+  *n_out = n;
+  return PYCD_OK;
+}
+
+int pycd_ewald_workspace_size(const PycdEwaldDesc* desc, int mode,
+                              size_t* bytes) {
+  clear_error();
+  PYCD_REQUIRE(bytes != nullptr, "bytes is NULL");
+  int rc = ewald_validate(desc, mode);
+  if (rc) return rc;
+  size_t b = ewald_workspace_bytes(desc, mode);
+  if (mode == PYCD_EWALD_BF16X3 || mode == PYCD_EWALD_TF32X3)
+    b += ewald_split_workspace_bytes(desc, mode);
+  *bytes = b;
+  return PYCD_OK;
+}
+
+int pycd_ewald_build(const PycdEwaldDesc* desc, int mode, double* d_out,
+                     void* d_workspace, size_t workspace_bytes, void* stream,
+                     float* real_ms, float* fourier_ms) {
+  clear_error();
+  PYCD_REQUIRE(d_out != nullptr, "d_out is NULL");
+  return ewald_build(desc, mode, d_out, d_workspace, workspace_bytes,
+                     (cudaStream_t)stream, real_ms, fourier_ms);
+}
+
+int pycd_potential_gemv(const double* d_A, int64_t n_sites, const double* d_q,
+                        double* d_phi, double* d_energy, void* stream) {
+  clear_error();
+  return potential_gemv(d_A, n_sites, d_q, d_phi, d_energy,
+                        (cudaStream_t)stream);
+}
+
+int pycd_kmc_workspace_size(int32_t n_systems, size_t* bytes) {
+  clear_error();
+  PYCD_REQUIRE(bytes && n_systems > 0, "bad arguments");
+  *bytes = kmc_ws_bytes(n_systems);
+  return PYCD_OK;
+}
+
+static int validate_systems(const PycdKmcSystem* systems, int32_t n_systems,
+                            int32_t max_carriers, int* max_np, int* max_nc) {
+  PYCD_REQUIRE(systems && n_systems > 0, "no systems");
+  int np = 0, nc = 0;
+  for (int i = 0; i < n_systems; ++i) {
+    const PycdKmcSystem& s = systems[i];
+    PYCD_REQUIRE(s.d_A && s.d_phi_bg && s.d_e_rel && s.d_nbr && s.d_hop &&
+                     s.d_lam && s.d_vab,
+                 "system %d: a required table pointer is NULL", i);
+    PYCD_REQUIRE(s.n_sites > 0 && s.n_sites < (1LL << 31),
+                 "system %d: n_sites out of range", i);
+    PYCD_REQUIRE(s.n_slots > 0 && s.n_carriers > 0 && s.n_carriers <= 32,
+                 "system %d: need 1..32 carriers and >=1 slot", i);
+    PYCD_REQUIRE(s.n_carriers <= max_carriers,
+                 "system %d: %d carriers exceed state stride %d", i,
+                 s.n_carriers, max_carriers);
+    PYCD_REQUIRE(s.kT > 0.0 && s.time_interval > 0.0 && s.n_path_steps >= 1,
+                 "system %d: kT, time_interval, n_path_steps must be > 0", i);
+    const int p = s.n_carriers * s.n_slots;
+    if (p > np) np = p;
+    if (s.n_carriers > nc) nc = s.n_carriers;
+  }
+  *max_np = np;
+  *max_nc = nc;
+  return PYCD_OK;
+}
+
+static int validate_state(const PycdKmcState* st, const PycdKmcOutputs* out,
+                          const PycdKmcRng* rng) {
+  PYCD_REQUIRE(st && out && rng, "NULL state/outputs/rng");
+  PYCD_REQUIRE(st->n_traj > 0 && st->max_carriers > 0, "empty state");
+  PYCD_REQUIRE(st->d_occ && st->d_time && st->d_step && st->d_path_index &&
+                   st->d_disp && st->d_last_row && st->d_status,
+               "a required state array is NULL");
+  PYCD_REQUIRE(!rng->d_uniforms || st->d_u_cursor,
+               "injected uniforms need d_u_cursor");
+  PYCD_REQUIRE(!rng->d_uniforms || rng->u_stride >= rng->u_count,
+               "u_stride < u_count");
+  PYCD_REQUIRE(!out->d_step_time == !out->d_step_proc,
+               "d_step_time and d_step_proc go together");
+  return PYCD_OK;
+}
+
+int pycd_kmc_upload_systems(const PycdKmcSystem* systems, int32_t n_systems,
+                            void* d_workspace, size_t workspace_bytes,
+                            void* stream, PycdKmcLaunch* launch) {
+  clear_error();
+  int np = 0, nc = 0;
+  int rc = validate_systems(systems, n_systems, 32, &np, &nc);
+  if (rc) return rc;
+  if (!d_workspace || workspace_bytes < kmc_ws_bytes(n_systems)) {
+    set_error("KMC workspace too small (%zu < %zu)", workspace_bytes,
+              kmc_ws_bytes(n_systems));
+    return PYCD_ERR_WORKSPACE;
+  }
+  std::vector<char> host(kmc_ws_bytes(n_systems), 0);
+  KmcTableHeader h{n_systems, np, nc, 0};
+  memcpy(host.data(), &h, sizeof(h));
+  memcpy(host.data() + 256, systems, sizeof(PycdKmcSystem) * n_systems);
+  cudaStream_t s = (cudaStream_t)stream;
+  PYCD_CUDA(cudaMemcpyAsync(d_workspace, host.data(), host.size(),
+                            cudaMemcpyHostToDevice, s));
+  PYCD_CUDA(cudaStreamSynchronize(s));
+  rc = kmc_preload();
+  if (rc) return rc;
+  if (launch) {
+    launch->max_processes = np;
+    launch->max_carriers = nc;
+  }
+  return PYCD_OK;
+}
+
+int pycd_kmc_advance_uploaded(int32_t n_systems, const PycdKmcState* state,
+                              const PycdKmcOutputs* out, const PycdKmcRng* rng,
+                              int64_t max_steps, const PycdKmcLaunch* launch,
+                              void* d_workspace, size_t workspace_bytes,
+                              void* stream) {
+  clear_error();
+  int rc = validate_state(state, out, rng);
+  if (rc) return rc;
+  PYCD_REQUIRE(max_steps >= 0, "max_steps < 0");
+  if (!d_workspace || workspace_bytes < kmc_ws_bytes(n_systems)) {
+    set_error("KMC workspace too small");
+    return PYCD_ERR_WORKSPACE;
+  }
+  PYCD_REQUIRE(launch && launch->max_processes > 0 && launch->max_carriers > 0,
+               "launch shape maxima missing (call pycd_kmc_upload_systems)");
+  PYCD_REQUIRE(launch->max_carriers <= state->max_carriers,
+               "carriers exceed the state stride");
+  KmcArgs a;
+  a.systems = (const PycdKmcSystem*)((const char*)d_workspace + 256);
+  a.n_systems = n_systems;
+  a.st = *state;
+  a.out = *out;
+  a.rng = *rng;
+  a.max_steps = max_steps;
+  if (max_steps == 0) return PYCD_OK;
+  return kmc_launch(a, launch->max_processes, launch->max_carriers, launch,
+                    (cudaStream_t)stream);
+}
+
+int pycd_kmc_advance(const PycdKmcSystem* systems, int32_t n_systems,
+                     const PycdKmcState* state, const PycdKmcOutputs* out,
+                     const PycdKmcRng* rng, int64_t max_steps,
+                     const PycdKmcLaunch* launch, void* d_workspace,
+                     size_t workspace_bytes, void* stream) {
+  clear_error();
+  int rc = validate_state(state, out, rng);
+  if (rc) return rc;
+  int np = 0, nc = 0;
+  rc = validate_systems(systems, n_systems, state->max_carriers, &np, &nc);
+  if (rc) return rc;
+  PycdKmcLaunch l{};
+  if (launch) l = *launch;
+  rc = pycd_kmc_upload_systems(systems, n_systems, d_workspace,
+                               workspace_bytes, stream, &l);
+  if (rc) return rc;
+  return pycd_kmc_advance_uploaded(n_systems, state, out, rng, max_steps, &l,
+                                   d_workspace, workspace_bytes, stream);
+}
+
+int pycd_philox_uniforms(uint64_t seed, uint64_t traj, int64_t step0,
+                         int64_t n_steps, double* d_out, void* stream) {
+  clear_error();
+  PYCD_REQUIRE(d_out && n_steps >= 0 && step0 >= 0, "bad arguments");
+  return philox_launch(seed, traj, step0, n_steps, d_out, (cudaStream_t)stream);
+}
+
+}  // extern "C"

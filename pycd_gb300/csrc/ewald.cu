@@ -1,0 +1,452 @@
+// Ewald pairwise-energy array on sm_103a (System.get_precomputed_array,
+// PyCD/core.py:1611-1679).
+//
+//   A = A_real + A_fourier + A_self
+//   A_real[i,j]    = erfc(sqrt(alpha) r_ij) / (2 r_ij) / eps, r_ij < r_cut,
+//                    diagonal keeps erfc(0)/2 (no division)   core.py:799-814
+//   A_fourier[i,j] = 2/eps sum_k c_k cos(k . d_ij) / k^2,
+//                    c_k = (2 pi / V) exp(-k^2 / (4 alpha))    core.py:853-878
+//   A_self         = -sqrt(alpha/pi)/eps on the diagonal       core.py:1659
+//
+// FP64_DIRECT evaluates the Fourier sum per pair from the caller's
+// minimum-image vectors (any pmiv, the reference's exact semantics).
+// FP64_GEMM factorises cos(k.(r_j - r_i)) = cos_i cos_j + sin_i sin_j and
+// contracts N x 2K feature rows with themselves (symmetric, upper tiles
+// computed, lower tiles mirrored).
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+
+#include "common.cuh"
+
+namespace pycd {
+
+struct Mat3 {
+  double m[9];
+};
+
+__device__ __forceinline__ void min_image(const Mat3& cell, const Mat3& inv,
+                                          const int32_t pbc[3], double d[3]) {
+  // fractional displacement, nearest image, then the 26 neighbours of that
+  // image; first strictly shorter candidate wins (core.py:304-361)
+  double f[3], base[3];
+#pragma unroll
+  for (int c = 0; c < 3; ++c)
+    f[c] = __dadd_rn(__dadd_rn(__dmul_rn(d[0], inv.m[0 * 3 + c]),
+                               __dmul_rn(d[1], inv.m[1 * 3 + c])),
+                     __dmul_rn(d[2], inv.m[2 * 3 + c]));
+#pragma unroll
+  for (int c = 0; c < 3; ++c) base[c] = pbc[c] ? -rint(f[c]) : 0.0;
+  double best[3], bestd;
+  {
+    double w[3] = {f[0] + base[0], f[1] + base[1], f[2] + base[2]};
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+      best[c] = __dadd_rn(__dadd_rn(__dmul_rn(w[0], cell.m[0 * 3 + c]),
+                                    __dmul_rn(w[1], cell.m[1 * 3 + c])),
+                          __dmul_rn(w[2], cell.m[2 * 3 + c]));
+    bestd = __dadd_rn(__dadd_rn(__dmul_rn(best[0], best[0]),
+                                __dmul_rn(best[1], best[1])),
+                      __dmul_rn(best[2], best[2]));
+  }
+  for (int dx = -1; dx <= 1; ++dx)
+    for (int dy = -1; dy <= 1; ++dy)
+      for (int dz = -1; dz <= 1; ++dz) {
+        if (dx == 0 && dy == 0 && dz == 0) continue;
+        const int ox = pbc[0] ? dx : 0, oy = pbc[1] ? dy : 0, oz = pbc[2] ? dz : 0;
+        if (ox == 0 && oy == 0 && oz == 0) continue;
+        double w[3] = {f[0] + (base[0] + ox), f[1] + (base[1] + oy),
+                       f[2] + (base[2] + oz)};
+        double cnd[3];
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+          cnd[c] = __dadd_rn(__dadd_rn(__dmul_rn(w[0], cell.m[0 * 3 + c]),
+                                       __dmul_rn(w[1], cell.m[1 * 3 + c])),
+                             __dmul_rn(w[2], cell.m[2 * 3 + c]));
+        const double cd = __dadd_rn(__dadd_rn(__dmul_rn(cnd[0], cnd[0]),
+                                              __dmul_rn(cnd[1], cnd[1])),
+                                    __dmul_rn(cnd[2], cnd[2]));
+        if (cd < bestd) {
+          bestd = cd;
+          best[0] = cnd[0]; best[1] = cnd[1]; best[2] = cnd[2];
+        }
+      }
+  d[0] = best[0]; d[1] = best[1]; d[2] = best[2];
+}
+
+struct EwaldGeom {
+  const double* cart;
+  const double* pmiv;
+  Mat3 cell, inv;
+  int32_t pbc[3];
+  int64_t n;
+};
+
+__device__ __forceinline__ void pair_vector(const EwaldGeom& g, int64_t i,
+                                            int64_t j, double d[3]) {
+  if (g.pmiv) {
+    const double* p = g.pmiv + (i * g.n + j) * 3;
+    d[0] = p[0]; d[1] = p[1]; d[2] = p[2];
+  } else {
+    d[0] = __dsub_rn(g.cart[j * 3 + 0], g.cart[i * 3 + 0]);
+    d[1] = __dsub_rn(g.cart[j * 3 + 1], g.cart[i * 3 + 1]);
+    d[2] = __dsub_rn(g.cart[j * 3 + 2], g.cart[i * 3 + 2]);
+    min_image(g.cell, g.inv, g.pbc, d);
+  }
+}
+
+// Per-k constants: Cartesian k, k^2 and c_k = (2 pi / V) exp(-k^2 / 4 alpha).
+__global__ void kvec_prepare_kernel(const int32_t* __restrict__ kv, int64_t K,
+                                    Mat3 recip, double coeff, double alpha4,
+                                    double* __restrict__ kc,
+                                    double* __restrict__ k2,
+                                    double* __restrict__ ck) {
+  int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= K) return;
+  const double m0 = kv[k * 3], m1 = kv[k * 3 + 1], m2 = kv[k * 3 + 2];
+  double v[3];
+#pragma unroll
+  for (int c = 0; c < 3; ++c)
+    v[c] = __dadd_rn(__dadd_rn(__dmul_rn(m0, recip.m[0 * 3 + c]),
+                               __dmul_rn(m1, recip.m[1 * 3 + c])),
+                     __dmul_rn(m2, recip.m[2 * 3 + c]));
+  const double kk = fma(v[2], v[2], fma(v[1], v[1], __dmul_rn(v[0], v[0])));
+  kc[k * 3] = v[0]; kc[k * 3 + 1] = v[1]; kc[k * 3 + 2] = v[2];
+  k2[k] = kk;
+  ck[k] = __dmul_rn(coeff, exp(__ddiv_rn(-kk, alpha4)));
+}
+
+// A_real + A_self, and (direct mode) A_fourier, one thread per pair.
+template <bool DIRECT>
+__global__ void __launch_bounds__(256)
+    ewald_pair_kernel(EwaldGeom g, double sqrt_alpha, double r_cut,
+                      double eps, double self_term,
+                      const double* __restrict__ kc,
+                      const double* __restrict__ k2,
+                      const double* __restrict__ ck, int64_t K,
+                      double* __restrict__ out) {
+  extern __shared__ double sk[];  // DIRECT: staged k data, 5 doubles per k
+  const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t i = blockIdx.y;
+  double d[3] = {0.0, 0.0, 0.0};
+  const bool valid = j < g.n;
+  if (valid) pair_vector(g, i, j, d);
+  double four = 0.0;
+  if (DIRECT) {
+    const int64_t TILE = 512;
+    for (int64_t k0 = 0; k0 < K; k0 += TILE) {
+      const int64_t nk = (K - k0) < TILE ? (K - k0) : TILE;
+      __syncthreads();
+      for (int64_t t = threadIdx.x; t < nk; t += blockDim.x) {
+        sk[t * 5 + 0] = kc[(k0 + t) * 3 + 0];
+        sk[t * 5 + 1] = kc[(k0 + t) * 3 + 1];
+        sk[t * 5 + 2] = kc[(k0 + t) * 3 + 2];
+        sk[t * 5 + 3] = ck[k0 + t];
+        sk[t * 5 + 4] = k2[k0 + t];
+      }
+      __syncthreads();
+      if (valid) {
+        for (int64_t t = 0; t < nk; ++t) {
+          const double th = fma(d[2], sk[t * 5 + 2],
+                                fma(d[1], sk[t * 5 + 1], __dmul_rn(d[0], sk[t * 5 + 0])));
+          four = __dadd_rn(four,
+                           __ddiv_rn(__dmul_rn(sk[t * 5 + 3], cos(th)), sk[t * 5 + 4]));
+        }
+      }
+    }
+    four = __ddiv_rn(__dmul_rn(four, 2.0), eps);
+  }
+  if (!valid) return;
+  const double r = sqrt(__dadd_rn(__dadd_rn(__dmul_rn(d[0], d[0]),
+                                            __dmul_rn(d[1], d[1])),
+                                  __dmul_rn(d[2], d[2])));
+  double real = 0.0;
+  if (r < r_cut) {
+    real = __ddiv_rn(erfc(__dmul_rn(sqrt_alpha, r)), 2.0);
+    if (i != j) real = __ddiv_rn(real, r);
+  }
+  real = __ddiv_rn(real, eps);
+  double v = __dadd_rn(real, four);
+  if (i == j) v = __dadd_rn(v, self_term);
+  out[i * g.n + j] = v;
+}
+
+// Feature rows F[i] = [sqrt(w_k) cos(k.r_i), sqrt(w_k) sin(k.r_i)]_k with
+// w_k = 2 c_k / (k^2 eps); rows padded with zeros to `ld` columns.
+__global__ void ewald_features_kernel(const double* __restrict__ cart,
+                                      int64_t n, const double* __restrict__ kc,
+                                      const double* __restrict__ k2,
+                                      const double* __restrict__ ck, int64_t K,
+                                      double eps, int64_t ld,
+                                      double* __restrict__ F) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t i = blockIdx.y;
+  if (i >= n) return;
+  if (k >= K) {
+    const int64_t c = 2 * k;
+    if (c < ld) F[i * ld + c] = 0.0;
+    if (c + 1 < ld) F[i * ld + c + 1] = 0.0;
+    return;
+  }
+  const double w = sqrt(2.0 * ck[k] / (k2[k] * eps));
+  const double th = kc[k * 3] * cart[i * 3] + kc[k * 3 + 1] * cart[i * 3 + 1] +
+                    kc[k * 3 + 2] * cart[i * 3 + 2];
+  double s, c;
+  sincos(th, &s, &c);
+  F[i * ld + 2 * k] = w * c;
+  F[i * ld + 2 * k + 1] = w * s;
+}
+
+// out += F F^T for the upper block tiles; each off-diagonal tile is also
+// written transposed.  BM = BN = 64, BK = 16, 256 threads, 4 x 4 per thread.
+constexpr int GB = 64, GK = 16;
+__global__ void __launch_bounds__(256)
+    syrk_fp64_kernel(const double* __restrict__ F, int64_t n, int64_t ld,
+                     int64_t kdim, double* __restrict__ out) {
+  __shared__ double As[GK][GB + 1];
+  __shared__ double Bs[GK][GB + 1];
+  const int bi = blockIdx.y, bj = blockIdx.x;
+  if (bi > bj) return;  // lower tiles are written by their mirror
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+  double acc[4][4] = {};
+  const int64_t row0 = (int64_t)bi * GB, col0 = (int64_t)bj * GB;
+  for (int64_t k0 = 0; k0 < kdim; k0 += GK) {
+    // 64 rows x 16 cols per operand: 1024 values, 4 per thread
+#pragma unroll
+    for (int l = 0; l < 4; ++l) {
+      const int idx = threadIdx.x + l * 256;
+      const int r = idx >> 4, c = idx & 15;
+      const int64_t ga = row0 + r, gb = col0 + r, gk = k0 + c;
+      As[c][r] = (ga < n && gk < kdim) ? F[ga * ld + gk] : 0.0;
+      Bs[c][r] = (gb < n && gk < kdim) ? F[gb * ld + gk] : 0.0;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < GK; ++kk) {
+      double a[4], b[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        a[u] = As[kk][ty * 4 + u];
+        b[u] = Bs[kk][tx * 4 + u];
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int v = 0; v < 4; ++v) acc[u][v] = fma(a[u], b[v], acc[u][v]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int u = 0; u < 4; ++u)
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+      const int64_t r = row0 + ty * 4 + u, c = col0 + tx * 4 + v;
+      if (r < n && c < n) {
+        out[r * n + c] += acc[u][v];
+        if (bi != bj) out[c * n + r] += acc[u][v];
+      }
+    }
+}
+
+// phi = A q (one warp per row) and, optionally, E = q . phi.
+__global__ void gemv_rows_kernel(const double* __restrict__ A, int64_t n,
+                                 const double* __restrict__ q,
+                                 double* __restrict__ phi) {
+  const int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (row >= n) return;
+  double s = 0.0;
+  for (int64_t c = lane; c < n; c += 32) s = fma(A[row * n + c], q[c], s);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+  if (lane == 0) phi[row] = s;
+}
+
+__global__ void dot_kernel(const double* __restrict__ a,
+                           const double* __restrict__ b, int64_t n,
+                           double* __restrict__ out) {
+  __shared__ double red[32];
+  double s = 0.0;
+  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) s = fma(a[i], b[i], s);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    s = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if (threadIdx.x == 0) *out = s;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+static size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
+
+struct EwaldWs {
+  double* kc;
+  double* k2;
+  double* ck;
+  double* F;
+  int64_t ld;
+};
+
+static int64_t feature_ld(int64_t K) { return ((2 * K + GK - 1) / GK) * GK; }
+
+static size_t ewald_ws_layout(const PycdEwaldDesc* d, int mode, EwaldWs* ws,
+                              char* base) {
+  const int64_t K = d->n_kvec, n = d->n_sites;
+  size_t off = 0;
+  auto take = [&](size_t bytes) {
+    char* p = base ? base + off : nullptr;
+    off += align256(bytes);
+    return p;
+  };
+  EwaldWs w{};
+  w.kc = (double*)take(sizeof(double) * 3 * (K > 0 ? K : 1));
+  w.k2 = (double*)take(sizeof(double) * (K > 0 ? K : 1));
+  w.ck = (double*)take(sizeof(double) * (K > 0 ? K : 1));
+  if (mode == PYCD_EWALD_FP64_GEMM) {
+    w.ld = feature_ld(K);
+    w.F = (double*)take(sizeof(double) * (size_t)n * (size_t)w.ld);
+  }
+  if (ws) *ws = w;
+  return off;
+}
+
+int ewald_validate(const PycdEwaldDesc* d, int mode) {
+  PYCD_REQUIRE(d != nullptr, "desc is NULL");
+  PYCD_REQUIRE(d->n_sites > 0, "n_sites must be positive");
+  PYCD_REQUIRE(d->n_kvec >= 0, "n_kvec must be >= 0");
+  PYCD_REQUIRE(d->n_kvec == 0 || d->d_kvec != nullptr, "d_kvec is NULL");
+  PYCD_REQUIRE(d->d_cart != nullptr || d->d_pmiv != nullptr,
+               "need d_cart or d_pmiv");
+  PYCD_REQUIRE(d->alpha > 0.0 && d->volume > 0.0 && d->dielectric != 0.0,
+               "alpha, volume must be > 0 and dielectric != 0");
+  PYCD_REQUIRE(mode >= PYCD_EWALD_FP64_DIRECT && mode <= PYCD_EWALD_TF32X3,
+               "unknown Ewald mode %d", mode);
+  if (mode != PYCD_EWALD_FP64_DIRECT)
+    PYCD_REQUIRE(d->d_cart != nullptr, "feature modes need d_cart");
+  PYCD_REQUIRE(d->n_sites <= 65535, "n_sites above 65535 is not supported");
+  return PYCD_OK;
+}
+
+size_t ewald_workspace_bytes(const PycdEwaldDesc* d, int mode) {
+  return ewald_ws_layout(d, mode, nullptr, nullptr);
+}
+
+int ewald_build_split(const PycdEwaldDesc* d, int mode, double* out,
+                      const double* kc, const double* k2, const double* ck,
+                      void* ws, size_t ws_bytes, cudaStream_t s);
+size_t ewald_split_workspace_bytes(const PycdEwaldDesc* d, int mode);
+
+int ewald_build(const PycdEwaldDesc* d, int mode, double* out, void* ws,
+                size_t ws_bytes, cudaStream_t s, float* real_ms,
+                float* fourier_ms) {
+  int rc = ewald_validate(d, mode);
+  if (rc) return rc;
+  const size_t need = ewald_workspace_bytes(d, mode) +
+                      ((mode == PYCD_EWALD_BF16X3 || mode == PYCD_EWALD_TF32X3)
+                           ? ewald_split_workspace_bytes(d, mode)
+                           : 0);
+  if (ws_bytes < need) {
+    set_error("workspace too small: %zu < %zu bytes", ws_bytes, need);
+    return PYCD_ERR_WORKSPACE;
+  }
+  EwaldWs w;
+  ewald_ws_layout(d, mode, &w, (char*)ws);
+  const int64_t n = d->n_sites, K = d->n_kvec;
+  Mat3 recip, cell, inv;
+  for (int c = 0; c < 9; ++c) {
+    recip.m[c] = d->recip[c];
+    cell.m[c] = d->sim_cell[c];
+    inv.m[c] = d->sim_cell_inv[c];
+  }
+  const double coeff = 2.0 * M_PI / d->volume;
+  cudaEvent_t e0 = nullptr, e1 = nullptr, e2 = nullptr;
+  const bool timing = real_ms || fourier_ms;
+  if (timing) {
+    PYCD_CUDA(cudaEventCreate(&e0));
+    PYCD_CUDA(cudaEventCreate(&e1));
+    PYCD_CUDA(cudaEventCreate(&e2));
+    PYCD_CUDA(cudaEventRecord(e0, s));
+  }
+  if (K > 0) {
+    kvec_prepare_kernel<<<(unsigned)((K + 255) / 256), 256, 0, s>>>(
+        d->d_kvec, K, recip, coeff, 4.0 * d->alpha, w.kc, w.k2, w.ck);
+    PYCD_CUDA(cudaGetLastError());
+  }
+  EwaldGeom g{};
+  g.cart = d->d_cart;
+  g.pmiv = d->d_pmiv;
+  g.cell = cell;
+  g.inv = inv;
+  g.pbc[0] = d->pbc[0]; g.pbc[1] = d->pbc[1]; g.pbc[2] = d->pbc[2];
+  g.n = n;
+  const double sqrt_alpha = sqrt(d->alpha);
+  const double self_term = -(sqrt(d->alpha / M_PI)) / d->dielectric;
+  dim3 grid((unsigned)((n + 255) / 256), (unsigned)n);
+  if (mode == PYCD_EWALD_FP64_DIRECT) {
+    ewald_pair_kernel<true><<<grid, 256, 512 * 5 * sizeof(double), s>>>(
+        g, sqrt_alpha, d->r_cut, d->dielectric, self_term, w.kc, w.k2,
+        w.ck, K, out);
+    PYCD_CUDA(cudaGetLastError());
+    if (timing) {
+      PYCD_CUDA(cudaEventRecord(e1, s));
+      PYCD_CUDA(cudaEventRecord(e2, s));
+    }
+  } else {
+    ewald_pair_kernel<false><<<grid, 256, 0, s>>>(
+        g, sqrt_alpha, d->r_cut, d->dielectric, self_term, w.kc, w.k2,
+        w.ck, 0, out);
+    PYCD_CUDA(cudaGetLastError());
+    if (timing) PYCD_CUDA(cudaEventRecord(e1, s));
+    if (K > 0) {
+      if (mode == PYCD_EWALD_FP64_GEMM) {
+        dim3 fg((unsigned)((w.ld / 2 + 127) / 128), (unsigned)n);
+        ewald_features_kernel<<<fg, 128, 0, s>>>(d->d_cart, n, w.kc, w.k2,
+                                                 w.ck, K, d->dielectric, w.ld,
+                                                 w.F);
+        PYCD_CUDA(cudaGetLastError());
+        const unsigned nb = (unsigned)((n + GB - 1) / GB);
+        syrk_fp64_kernel<<<dim3(nb, nb), 256, 0, s>>>(w.F, n, w.ld, w.ld, out);
+        PYCD_CUDA(cudaGetLastError());
+      } else {
+        const size_t base = ewald_workspace_bytes(d, mode);
+        rc = ewald_build_split(d, mode, out, w.kc, w.k2, w.ck,
+                               (char*)ws + base, ws_bytes - base, s);
+        if (rc) return rc;
+      }
+    }
+    if (timing) PYCD_CUDA(cudaEventRecord(e2, s));
+  }
+  if (timing) {
+    PYCD_CUDA(cudaEventSynchronize(e2));
+    float a = 0.f, b = 0.f;
+    PYCD_CUDA(cudaEventElapsedTime(&a, e0, e1));
+    PYCD_CUDA(cudaEventElapsedTime(&b, e1, e2));
+    if (real_ms) *real_ms = a;
+    if (fourier_ms) *fourier_ms = b;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaEventDestroy(e2);
+  }
+  return PYCD_OK;
+}
+
+int potential_gemv(const double* A, int64_t n, const double* q, double* phi,
+                   double* energy, cudaStream_t s) {
+  PYCD_REQUIRE(A && q && phi && n > 0, "potential_gemv: bad arguments");
+  const int64_t threads = n * 32;
+  gemv_rows_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(A, n, q, phi);
+  PYCD_CUDA(cudaGetLastError());
+  if (energy) {
+    dot_kernel<<<1, 1024, 0, s>>>(q, phi, n, energy);
+    PYCD_CUDA(cudaGetLastError());
+  }
+  return PYCD_OK;
+}
+
+}  // namespace pycd

@@ -1,0 +1,145 @@
+"""Device build of the Ewald precomputed array (System.get_precomputed_array,
+PyCD/core.py:1611-1679) through ``pycd_ewald_build``.
+
+Host work here is the k-vector list (integer, PyCD/core.py:816-838 with the
+k^2 < k_cut^2 filter of core.py:868) and the choice of algorithm:
+
+* ``fp64_direct`` - per-pair cos(k . d_ij) from the pairwise minimum-image
+  vectors; the reference's exact formula for any pmiv.
+* ``fp64``        - feature contraction F F^T in FP64.  Valid when every
+  pmiv_ij equals r_j - r_i plus a supercell translation and the Ewald cell
+  (``System.translational_matrix``) is that supercell.
+* ``bf16x3`` / ``tf32x3`` - the same contraction on tcgen05 tensor cores.
+"""
+import numpy as np
+
+from . import _native as nat
+
+
+def k_max_for(system, k_cut):
+    """k_max = ceil(k_cut / |b_i|) (PyCD/core.py:1599)."""
+    return np.ceil(k_cut / system.reciprocal_lattice_vector_length).astype(int)
+
+
+def effective_k_vectors(recip, k_max, k_cut):
+    """Half-space integer k list kept by the reference, in its order.
+
+    The grid [-k_max, k_max]^3 in C order with the first member of every +-m
+    pair kept is exactly the set of points before the origin; the filter is
+    k^2 < k_cut^2 with k = m . recip.  k^2 is compared vectorised and every
+    vector within rounding of the cut is re-evaluated with the reference's
+    per-vector ``np.dot`` so the kept set is the reference's.
+    """
+    k_max = np.asarray(k_max, dtype=int)
+    g = np.mgrid[-k_max[0]:k_max[0] + 1, -k_max[1]:k_max[1] + 1,
+                 -k_max[2]:k_max[2] + 1].reshape(3, -1).T
+    half = g[: len(g) // 2]  # points strictly before the origin
+    kv = np.dot(half.astype(np.float64), recip)
+    k2 = np.einsum("ij,ij->i", kv, kv)
+    kc2 = k_cut ** 2
+    keep = k2 < kc2
+    near = np.abs(k2 - kc2) <= 1e-12 * kc2
+    for i in np.nonzero(near)[0]:
+        kk = np.dot(half[i], recip)
+        keep[i] = np.dot(kk, kk) < kc2
+    return np.ascontiguousarray(half[keep].astype(np.int32))
+
+
+def pmiv_is_lattice_consistent(system, pmiv, tol=1e-8):
+    """True when pmiv_ij - (r_j - r_i) is a supercell translation for all
+    pairs and the Ewald cell equals the supercell (no column-broadcast quirk),
+    i.e. cos(k . pmiv_ij) = cos(k . r_j - k . r_i) for every kept k."""
+    if not ewald_cell_matches_supercell(system):
+        return False
+    coords = system.neighbors.bulk_sites.cell_coordinates
+    inv = system.neighbors.simulation_cell_matrix_inv
+    n = len(coords)
+    chunk = max(1, 2_000_000 // max(1, n))
+    for s in range(0, n, chunk):
+        e = min(n, s + chunk)
+        d = pmiv[s:e] - (coords[None, :, :] - coords[s:e, None, :])
+        f = np.dot(d.reshape(-1, 3), inv)
+        if np.abs(f - np.round(f)).max() > tol:
+            return False
+    return True
+
+
+def ewald_cell_matches_supercell(system, rtol=1e-12):
+    a = system.translational_matrix
+    b = system.neighbors.simulation_cell_matrix
+    return bool(np.allclose(a, b, rtol=rtol, atol=rtol * np.abs(b).max()))
+
+
+def choose_mode(system, pmiv, requested="auto"):
+    if requested != "auto":
+        if requested not in nat.EWALD_MODES:
+            raise ValueError("unknown Ewald precision %r" % (requested,))
+        if requested != "fp64_direct":
+            ok = (pmiv_is_lattice_consistent(system, pmiv) if pmiv is not None
+                  else ewald_cell_matches_supercell(system))
+            if not ok:
+                raise ValueError(
+                    "precision %r needs a lattice-consistent pmiv and an Ewald "
+                    "cell equal to the supercell; use 'fp64_direct'" % requested)
+        return requested
+    if pmiv is not None:
+        return "fp64" if pmiv_is_lattice_consistent(system, pmiv) else "fp64_direct"
+    return "fp64" if ewald_cell_matches_supercell(system) else "fp64_direct"
+
+
+def build_device_array(system, alpha, r_cut, k_cut, precision="auto",
+                       pmiv="system", stream=None, out=None):
+    """Build the N x N FP64 array on the current CUDA device.
+
+    Returns ``(A, info)``: ``A`` a CUDA float64 tensor, ``info`` a dict with
+    ``mode``, ``k_max``, ``n_kvec`` and the real / Fourier phase times (ms).
+    ``pmiv='system'`` uses ``system.pairwise_min_image_vector_data``.
+    """
+    import torch
+    nat.require_device()
+    if isinstance(pmiv, str) and pmiv == "system":
+        pmiv = system.pairwise_min_image_vector_data
+    n = int(system.neighbors.num_system_elements)
+    mode = choose_mode(system, pmiv, precision)
+    k_max = k_max_for(system, k_cut)
+    kv = effective_k_vectors(system.reciprocal_lattice_matrix, k_max, k_cut)
+    dev = torch.device("cuda", torch.cuda.current_device())
+    cart = torch.as_tensor(system.neighbors.bulk_sites.cell_coordinates,
+                           dtype=torch.float64).contiguous().to(dev)
+    d_pmiv = None
+    if pmiv is not None:  # the real-space term uses |pmiv_ij| as given
+        d_pmiv = torch.as_tensor(np.ascontiguousarray(pmiv, dtype=np.float64)
+                                 ).to(dev)
+    d_kv = torch.as_tensor(kv).to(dev) if len(kv) else torch.zeros(
+        (1, 3), dtype=torch.int32, device=dev)
+    desc = nat.EwaldDesc()
+    desc.n_sites = n
+    desc.n_kvec = len(kv)
+    desc.d_cart = cart.data_ptr()
+    desc.d_pmiv = d_pmiv.data_ptr() if d_pmiv is not None else None
+    desc.d_kvec = d_kv.data_ptr()
+    desc.recip[:] = [float(v) for v in np.asarray(
+        system.reciprocal_lattice_matrix, dtype=np.float64).ravel()]
+    desc.sim_cell[:] = [float(v) for v in system.neighbors.simulation_cell_matrix.ravel()]
+    desc.sim_cell_inv[:] = [float(v) for v in system.neighbors.simulation_cell_matrix_inv.ravel()]
+    desc.pbc[:] = [int(v) for v in system.pbc]
+    desc.alpha = float(alpha)
+    desc.r_cut = float(r_cut)
+    desc.volume = float(system.system_volume)
+    desc.dielectric = float(system.material.dielectric_constant)
+    L = nat.lib()
+    code = nat.EWALD_MODES[mode]
+    ws_bytes = nat.C.c_size_t()
+    nat.check(L.pycd_ewald_workspace_size(nat.C.byref(desc), code,
+                                          nat.C.byref(ws_bytes)))
+    ws = torch.empty(max(1, ws_bytes.value), dtype=torch.uint8, device=dev)
+    if out is None:
+        out = torch.empty((n, n), dtype=torch.float64, device=dev)
+    rms, fms = nat.C.c_float(), nat.C.c_float()
+    nat.check(L.pycd_ewald_build(nat.C.byref(desc), code, out.data_ptr(),
+                                 ws.data_ptr(), ws_bytes.value,
+                                 nat.stream_handle(stream), nat.C.byref(rms),
+                                 nat.C.byref(fms)))
+    info = {"mode": mode, "k_max": k_max, "n_kvec": int(len(kv)),
+            "real_ms": rms.value, "fourier_ms": fms.value}
+    return out, info

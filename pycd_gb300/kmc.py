@@ -1,0 +1,220 @@
+"""Device-side KMC: per-system tables, trajectory state and the engine that
+advances them through ``pycd_kmc_advance`` (the Run.do_kmc_steps loop,
+PyCD/core.py:2787-2861).
+
+``KmcTables`` holds one lattice system in HBM: the N x N FP64 array, the
+background potential phi_bg = A q_fixed, relative site energies, and the
+per-(site, slot) neighbour, hop-vector, lambda, V_ab and field-shift tables
+(the reference's per-process tables of core.py:1823-1927, laid out by site).
+``KmcBatch`` is the structure-of-arrays state of T trajectories that may run
+on different systems; the same kernel advances one trajectory (plain form) or
+thousands (batched form).
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import _native as nat
+
+
+def _dev():
+    import torch
+    return torch.device("cuda", torch.cuda.current_device())
+
+
+class KmcTables(object):
+    """Device tables of one system (see module docstring)."""
+
+    def __init__(self, A, nbr, hop, lam, vab, e_rel, q_fixed, carrier_charge,
+                 n_carriers, vn, kT, time_interval, n_path_steps,
+                 field_shift=None, phi_bg=None):
+        import torch
+        nat.require_device()
+        dev = _dev()
+        self.n_sites = int(nbr.shape[0])
+        self.n_slots = int(nbr.shape[1])
+        if isinstance(A, torch.Tensor):
+            self.A = A.to(dev, torch.float64).contiguous()
+        else:
+            self.A = torch.as_tensor(np.ascontiguousarray(A, np.float64)).to(dev)
+        assert tuple(self.A.shape) == (self.n_sites, self.n_sites)
+        f64 = lambda x: torch.as_tensor(np.ascontiguousarray(x, np.float64)).to(dev)
+        self.nbr = torch.as_tensor(np.ascontiguousarray(nbr, np.int32)).to(dev)
+        self.hop = f64(hop)
+        self.lam = f64(lam)
+        self.vab = f64(vab)
+        self.e_rel = f64(e_rel)
+        self.field_shift = None if field_shift is None else f64(field_shift)
+        if phi_bg is None:
+            self.q_fixed = f64(q_fixed)
+            self.phi_bg = torch.empty(self.n_sites, dtype=torch.float64, device=dev)
+            nat.check(nat.lib().pycd_potential_gemv(
+                self.A.data_ptr(), self.n_sites, self.q_fixed.data_ptr(),
+                self.phi_bg.data_ptr(), None, nat.stream_handle()))
+        else:
+            self.phi_bg = f64(phi_bg)
+        self.carrier_charge = float(carrier_charge)
+        self.n_carriers = int(n_carriers)
+        self.vn = float(vn)
+        self.kT = float(kT)
+        self.time_interval = float(time_interval)
+        self.n_path_steps = int(n_path_steps)
+
+    def descriptor(self):
+        d = nat.KmcSystem()
+        d.d_A = self.A.data_ptr()
+        d.d_phi_bg = self.phi_bg.data_ptr()
+        d.d_e_rel = self.e_rel.data_ptr()
+        d.d_nbr = self.nbr.data_ptr()
+        d.d_hop = self.hop.data_ptr()
+        d.d_lam = self.lam.data_ptr()
+        d.d_vab = self.vab.data_ptr()
+        d.d_field_shift = (self.field_shift.data_ptr()
+                           if self.field_shift is not None else None)
+        d.n_sites = self.n_sites
+        d.n_slots = self.n_slots
+        d.n_carriers = self.n_carriers
+        d.carrier_charge = self.carrier_charge
+        d.vn = self.vn
+        d.kT = self.kT
+        d.time_interval = self.time_interval
+        d.n_path_steps = self.n_path_steps
+        return d
+
+
+class KmcBatch(object):
+    """State of T trajectories (device SoA) plus optional outputs."""
+
+    def __init__(self, occupancy, sys_index=None, max_carriers=None,
+                 energy0=None, unwrapped_rows=None, step_capacity=0,
+                 energy_grid_rows=None, delg0_grid_rows=None, drift=False):
+        import torch
+        dev = _dev()
+        occ = np.asarray(occupancy, dtype=np.int32)
+        if occ.ndim == 1:
+            occ = occ[None, :]
+        T, nc = occ.shape
+        mc = max_carriers or nc
+        self.n_traj, self.max_carriers = T, mc
+        occ_full = np.zeros((T, mc), np.int32)
+        occ_full[:, :nc] = occ
+        z64 = lambda *s: torch.zeros(*s, dtype=torch.float64, device=dev)
+        self.occ = torch.as_tensor(occ_full).to(dev)
+        self.sys_index = (None if sys_index is None else
+                          torch.as_tensor(np.asarray(sys_index, np.int32)).to(dev))
+        self.time = z64(T)
+        self.step = torch.zeros(T, dtype=torch.int64, device=dev)
+        self.path_index = torch.ones(T, dtype=torch.int64, device=dev)
+        self.disp = z64(T, mc * 3)
+        self.last_row = z64(T, mc * 3)
+        self.energy = z64(T)
+        if energy0 is not None:
+            self.energy.copy_(torch.as_tensor(np.asarray(energy0, np.float64)))
+        self.status = torch.zeros(T, dtype=torch.int32, device=dev)
+        self.u_cursor = torch.zeros(T, dtype=torch.int64, device=dev)
+        self.unwrapped = (None if unwrapped_rows is None
+                          else z64(T, unwrapped_rows, mc * 3))
+        self.energy_grid = (None if energy_grid_rows is None
+                            else z64(T, energy_grid_rows))
+        if self.energy_grid is not None and energy0 is not None:
+            self.energy_grid[:, 0] = self.energy
+        self.delg0_grid = (None if delg0_grid_rows is None
+                           else z64(T, delg0_grid_rows))
+        self.step_capacity = int(step_capacity)
+        self.step_time = z64(T, max(1, self.step_capacity)) if step_capacity else None
+        self.step_proc = (torch.zeros(T, max(1, self.step_capacity),
+                                      dtype=torch.int32, device=dev)
+                          if step_capacity else None)
+        self.step_offset = 0
+        self.drift = z64(T, mc, 3) if drift else None
+
+    def state_struct(self):
+        s = nat.KmcState()
+        s.n_traj = self.n_traj
+        s.max_carriers = self.max_carriers
+        s.d_sys_index = nat.ptr(self.sys_index)
+        s.d_occ = self.occ.data_ptr()
+        s.d_time = self.time.data_ptr()
+        s.d_step = self.step.data_ptr()
+        s.d_path_index = self.path_index.data_ptr()
+        s.d_disp = self.disp.data_ptr()
+        s.d_last_row = self.last_row.data_ptr()
+        s.d_energy = self.energy.data_ptr()
+        s.d_status = self.status.data_ptr()
+        s.d_u_cursor = self.u_cursor.data_ptr()
+        return s
+
+    def outputs_struct(self):
+        o = nat.KmcOutputs()
+        o.d_unwrapped = nat.ptr(self.unwrapped)
+        o.unwrapped_stride = (0 if self.unwrapped is None
+                              else self.unwrapped.shape[1] * self.unwrapped.shape[2])
+        o.d_energy_grid = nat.ptr(self.energy_grid)
+        o.d_delg0_grid = nat.ptr(self.delg0_grid)
+        o.d_step_time = nat.ptr(self.step_time)
+        o.d_step_proc = nat.ptr(self.step_proc)
+        o.step_capacity = self.step_capacity
+        o.step_offset = self.step_offset
+        o.d_drift = nat.ptr(self.drift)
+        return o
+
+    def snapshot(self):
+        """Host copy of the resumable state (checkpoint between chunks)."""
+        keys = ("occ", "time", "step", "path_index", "disp", "last_row",
+                "energy", "status", "u_cursor")
+        return {k: getattr(self, k).cpu().numpy().copy() for k in keys}
+
+    def restore(self, snap):
+        import torch
+        for k, v in snap.items():
+            getattr(self, k).copy_(torch.as_tensor(v))
+
+
+class KmcEngine(object):
+    """Launches ``pycd_kmc_advance`` for a set of systems and a batch."""
+
+    def __init__(self, tables, launch=None):
+        import torch
+        self.tables = list(tables) if isinstance(tables, (list, tuple)) else [tables]
+        self._descs = (nat.KmcSystem * len(self.tables))(
+            *[t.descriptor() for t in self.tables])
+        nbytes = C.c_size_t()
+        nat.check(nat.lib().pycd_kmc_workspace_size(len(self.tables),
+                                                    C.byref(nbytes)))
+        self.workspace = torch.empty(nbytes.value, dtype=torch.uint8,
+                                     device=_dev())
+        self.launch = nat.KmcLaunch()
+        if launch:
+            for k, v in launch.items():
+                setattr(self.launch, k, int(v))
+        self._uploaded = False
+
+    def upload(self, stream=None):
+        nat.check(nat.lib().pycd_kmc_upload_systems(
+            self._descs, len(self.tables), self.workspace.data_ptr(),
+            self.workspace.numel(), nat.stream_handle(stream),
+            C.byref(self.launch)))
+        self._uploaded = True
+
+    @staticmethod
+    def rng_struct(uniforms=None, u_count=None, seed=0, traj_offset=0):
+        r = nat.KmcRng()
+        if uniforms is not None:
+            r.d_uniforms = uniforms.data_ptr()
+            r.u_stride = uniforms.shape[-1]
+            r.u_count = uniforms.shape[-1] if u_count is None else int(u_count)
+        r.seed = int(seed)
+        r.traj_offset = int(traj_offset)
+        return r
+
+    def advance(self, batch, max_steps, rng, stream=None):
+        """Advance every running trajectory by up to ``max_steps`` steps.
+        Asynchronous on ``stream``; the structs are passed by value."""
+        if not self._uploaded:
+            self.upload(stream)
+        st = batch.state_struct()
+        out = batch.outputs_struct()
+        nat.check(nat.lib().pycd_kmc_advance_uploaded(
+            len(self.tables), C.byref(st), C.byref(out), C.byref(rng),
+            int(max_steps), C.byref(self.launch), self.workspace.data_ptr(),
+            self.workspace.numel(), nat.stream_handle(stream)))

@@ -1,0 +1,484 @@
+"""Generate the golden fixtures under tests/golden/ from the reference PyCD.
+
+Run in a container where the reference checkout exists (default
+/root/reference, or $PYCD_REFERENCE):
+
+    python tests/golden/make_golden.py
+
+The reference is imported with test-only shims (stub matplotlib / yaml
+modules, ``np.in1d = np.isin``, a ragged-list ``asarray`` for multi-element
+POSCARs) and driven through its own classes.  Every fixture written here was
+produced by the reference's code or ships with it:
+
+  hematite.json/.npz, bvo.json/.npz
+      examples/{Hematite,BVO}: shipped precomputed_array.npy and pmiv (the
+      array is rebuilt by the reference's pot_r_ewald/pot_k_ewald and checked
+      against the shipped one), the shipped hop-neighbour list, the shipped
+      initial MT19937 state, and the shipped unwrapped_traj.npy /
+      time_data.npy (re-run here through do_kmc_steps and checked).
+  corundum324.json/.npz
+      the 324-site corundum lattice (3x3x3 cells of the 12-site Fe sublattice
+      of examples/Hematite): the reference's own hop-neighbour list, pmiv
+      digest and Ewald array rows, and its event stream for 1e5 steps driven
+      by injected uniforms np.random.default_rng(0).random(2e5).
+  corundum3600.json/.npz
+      the 3,600-site lattice with 4 electrons and 4 fixed +1 dopants: the
+      reference's event stream for a 2,000-step prefix of two trajectories,
+      run on the oracle's array and our hop list (both pinned above).
+"""
+import hashlib
+import json
+import os
+import pickle
+import shutil
+import sys
+import tempfile
+import time
+import types
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+REPO = HERE.parent.parent
+REF = Path(os.environ.get("PYCD_REFERENCE", "/root/reference"))
+
+
+# ---------------------------------------------------------------- shims
+def install_shims():
+    for name in ("matplotlib", "matplotlib.pyplot", "matplotlib.offsetbox", "yaml"):
+        sys.modules.setdefault(name, types.ModuleType(name))
+    sys.modules["matplotlib"].pyplot = sys.modules["matplotlib.pyplot"]
+    sys.modules["matplotlib.pyplot"].switch_backend = lambda *a, **k: None
+    sys.modules["matplotlib.offsetbox"].AnchoredText = object
+    if not hasattr(np, "in1d"):
+        np.in1d = np.isin
+    sys.path.insert(0, str(REF))
+    import PyCD.core as core
+
+    class _NumpyProxy:
+        def __getattr__(self, name):
+            return getattr(np, name)
+
+        @staticmethod
+        def asarray(x, *a, **k):
+            try:
+                return np.asarray(x, *a, **k)
+            except ValueError:
+                out = np.empty(len(x), dtype=object)
+                for i, row in enumerate(x):
+                    out[i] = np.asarray(row)
+                return out
+
+    core.np = _NumpyProxy()
+    return core
+
+
+def sha(a):
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+# ---------------------------------------------------------------- configs
+PRECISION = dict(lower_bound_real=0.75, lower_bound_rcut=0.0, upper_bound_rcut=0.9999,
+                 lower_bound_kcut=0.0, upper_bound_kcut=10.0, threshold_fraction=0.9,
+                 precise_r_cut=0, err_tol=2.585e-3, step_increase_tol=2.585e-10,
+                 num_data_points_low=10.0, num_data_points_high=50.0,
+                 step_change_data_points=10.0)
+
+HEMATITE = dict(
+    name="Fe2O3", species_types=["electron", "hole"],
+    species_charge_list={"full": [-1, 1], "partial": [-0.5, 0.5]},
+    species_to_element_type_map={"electron": ["Fe"], "hole": ["O"]},
+    charge_types={"full": {"Fe": 3.0, "O": -2.0},
+                  "partial": {"Fe": 1.6349, "O": -1.0899}},
+    neighbor_cutoff_dist={"Fe:Fe": [[2.971, 2.901]]},
+    neighbor_cutoff_dist_tol={"Fe:Fe": [[0.0020, 0.0020]]},
+    vn=1.85e13, lambda_values={"Fe:Fe": [[1.74533, 1.88683]]},
+    v_ab={"Fe:Fe": [[0.184, 0.028]]},
+    class_list={"Fe": [1] * 12, "O": [1] * 18}, element_type_delimiter=":",
+    dielectric_constant=9.355, alpha=2.667e-01, r_cut=4.618e+00, k_cut=6.998e+00,
+    precision_parameters=PRECISION)
+
+BVO = dict(
+    name="BVO", species_types=["electron", "hole"],
+    species_charge_list={"full": [-1, 1], "partial": [-0.5, 0.5]},
+    species_to_element_type_map={"electron": ["V"], "hole": ["O"]},
+    charge_types={"full": {"Bi": 3.0, "O": -2.0, "V": 5.0},
+                  "partial": {"Bi": 2.0311, "O": -1.0352, "V": 2.1098}},
+    neighbor_cutoff_dist={
+        "V:V": [[3.8474, 3.9447, 5.0935, 5.1956]],
+        "O:O": [[2.7450, 2.8541, 2.8600, 2.9573, 2.9723, 3.0033, 3.0076, 3.0205,
+                 3.0473, 3.6123, 3.6845],
+                [2.7962, 2.8541, 2.8600, 2.9123, 2.9707, 2.9678, 3.0076, 3.0205,
+                 2.9958, 3.6123, 3.6845]]},
+    neighbor_cutoff_dist_tol={
+        "V:V": [[0.0020] * 4],
+        "O:O": [[0.0020, 0.0020, 0.0020, 0.0020, 0.0010, 0.0020, 0.0020, 0.0020,
+                 0.0020, 0.0020, 0.0020]] * 2},
+    vn=1.00e13,
+    lambda_values={"V:V": [[1.4768, 1.4964, 1.4652, 1.4932]],
+                   "O:O": [[1.4668, 0.7552, 0.7552, 1.6419, 0.9952, 1.5667, 1.4887,
+                            1.4887, 2.3456, 1.4863, 1.4863]] * 2},
+    v_ab={"V:V": [[0.0] * 4], "O:O": [[0.0] * 11] * 2},
+    class_list={"O": [2, 1] * 8, "V": [1] * 4, "Bi": [1] * 4},
+    element_type_delimiter=":", dielectric_constant=38.299,
+    alpha=2.051e-01, r_cut=4.669e+00, k_cut=5.298e+00,
+    precision_parameters=dict(PRECISION, upper_bound_kcut=100.0,
+                              step_increase_tol=2.585e-07))
+
+RUN_COMMON = dict(
+    temp=300, ion_charge_type="full", species_charge_type="full",
+    species_count=[1, 0], time_interval=1.0e-08,
+    initial_occupancy={"electron": [], "hole": []},
+    relative_energies={"class_index": {"O": [0.0, 0.0406]},
+                       "doping": {"V": [[0.6596, -0.0168, -0.0154],
+                                        [0.0791, -0.0024, -0.0188]]}},
+    external_field={"electric": {"active": 0, "dir": [1, 0, 0], "ld": 0, "mag": 0.0001}},
+    doping={"num_dopants": [0, 0], "doping_element_map": ["V:W", "V:Mo"],
+            "insertion_type": ["random", "random"], "charge": {"full": {"Mo": 5, "W": 5}},
+            "site_charge_initiation": ["no", "no"], "min_shell_separation": [4, 4],
+            "max_attempts": 100},
+    output_data={
+        "delg_0": {"file_name": "delG0_traj.npy", "write": 0},
+        "energy": {"file_name": "energy_traj.npy", "write": 0},
+        "potential": {"file_name": "potential_traj.npy", "write": 0},
+        "time": {"file_name": "time_data.npy", "write": 1},
+        "unwrapped_traj": {"file_name": "unwrapped_traj.npy", "write": 1,
+                           "write_every_step": 0},
+        "wrapped_traj": {"file_name": "wrapped_traj.npy", "write": 0}},
+    random_seed=2)
+
+# synthetic corundum (Fe sublattice of hematite, R-centred 12c sites)
+CORUNDUM_LATTICE = [[5.038, 0.0, 0.0], [-2.519, 4.363036, 0.0], [0.0, 0.0, 13.772]]
+
+
+def corundum_frac(z=0.3553):
+    base = [(0, 0, z), (0, 0, -z), (0, 0, 0.5 + z), (0, 0, 0.5 - z)]
+    cent = [(0, 0, 0), (2 / 3, 1 / 3, 1 / 3), (1 / 3, 2 / 3, 2 / 3)]
+    out = []
+    for c in cent:
+        for b in base:
+            out.append([(b[i] + c[i]) % 1.0 for i in range(3)])
+    return np.array(out)
+
+
+CORUNDUM = dict(
+    name="corundum", species_types=["electron"],
+    species_charge_list={"full": [-1]},
+    species_to_element_type_map={"electron": ["Fe"]},
+    charge_types={"full": {"Fe": 0.0}},
+    neighbor_cutoff_dist={"Fe:Fe": [[2.90, 2.97]]},
+    neighbor_cutoff_dist_tol={"Fe:Fe": [[0.01, 0.01]]},
+    vn=1.85e13, lambda_values={"Fe:Fe": [[0.9, 0.9]]}, v_ab={"Fe:Fe": [[0.2, 0.2]]},
+    class_list={"Fe": [1] * 12}, element_type_delimiter=":",
+    dielectric_constant=12.0, alpha=0.25, r_cut=6.4, k_cut=1.6,
+    precision_parameters=PRECISION)
+
+
+def poscar_text(comment, lattice, types_, counts, frac):
+    out = [comment, "1.0"]
+    for row in lattice:
+        out.append("  ".join(f"{v:20.10f}" for v in row))
+    out.append("   ".join(types_))
+    out.append("   ".join(str(c) for c in counts))
+    out.append("Direct")
+    for row in frac:
+        out.append("  ".join(f"{v:18.12f}" for v in row))
+    return "\n".join(out) + "\n"
+
+
+# ---------------------------------------------------------------- helpers
+def hop_to_arrays(hop):
+    meta, arrs = {}, {}
+    for key, per_class in hop.items():
+        meta[key] = []
+        for ci, per_type in enumerate(per_class):
+            meta[key].append(len(per_type))
+            for ti, rv in enumerate(per_type):
+                tag = f"hop|{key}|{ci}|{ti}"
+                arrs[tag + "|count"] = np.asarray(rv.num_neighbors, np.int64)
+                idx = [np.asarray(x, np.int64) for x in rv.neighbor_system_element_indices]
+                vec = [np.asarray(x, np.float64).reshape(-1, 3)
+                       for x in rv.displacement_vector_list]
+                arrs[tag + "|idx"] = np.concatenate(idx) if idx else np.zeros(0, np.int64)
+                arrs[tag + "|vec"] = np.concatenate(vec) if vec else np.zeros((0, 3))
+    return meta, arrs
+
+
+def material_objects(core, params, poscar, system_size, pbc, tmp):
+    p = dict(params)
+    p.pop("precision_parameters", None)
+    path = Path(tmp) / "POSCAR"
+    path.write_text(poscar)
+    p["input_coord_file_location"] = path
+    mat = core.Material(core.ReturnValues(**p))
+    nb = core.Neighbors(mat, np.asarray(system_size), np.asarray(pbc))
+    return mat, nb
+
+
+def make_system(core, mat, nb, hop, pmiv, params):
+    return core.System(mat, nb, hop, pmiv, params["alpha"], params["r_cut"],
+                       params["k_cut"], params["precision_parameters"], [], [])
+
+
+def ref_array(system, mat, nb):
+    Ar = system.get_precomputed_array_real(system.alpha, system.r_cut)
+    Af, _, _ = system.get_precomputed_array_fourier(system.alpha, system.k_cut)
+    As = -np.eye(nb.num_system_elements) * np.sqrt(system.alpha / np.pi) \
+        / mat.dielectric_constant
+    return Ar + Af + As
+
+
+# ---------------------------------------------------------------- examples
+def example(core, name, params, t_final):
+    ex = REF / "examples" / name
+    poscar = (ex / "InputFiles" / "POSCAR").read_text()
+    tmp = tempfile.mkdtemp()
+    mat, nb = material_objects(core, params, poscar, [2, 2, 1], [1, 1, 1], tmp)
+    hop = np.load(ex / "InputFiles" / "hop_neighbor_list.npy", allow_pickle=True)[()]
+    pmiv = np.load(ex / "InputFiles" / "pairwise_min_image_vector_data.npy")
+    A_shipped = np.load(ex / "InputFiles" / "precomputed_array.npy")
+    system = make_system(core, mat, nb, hop, pmiv, params)
+    A = ref_array(system, mat, nb)
+    err = float(np.abs(A - A_shipped).max())
+    print(f"{name}: reference rebuild vs shipped array max |dA| = {err:.3e} Ha")
+    assert err < 1e-15
+    run_p = dict(RUN_COMMON, t_final=t_final)
+    run = core.Run(system, A_shipped, run_p["temp"], run_p["ion_charge_type"],
+                   run_p["species_charge_type"], 1, t_final, run_p["time_interval"],
+                   np.asarray(run_p["species_count"]), run_p["initial_occupancy"],
+                   run_p["relative_energies"], run_p["external_field"], run_p["doping"])
+    d = Path(tempfile.mkdtemp())
+    shutil.copy(ex / "traj1" / "initial_rnd_state.dump", d / "initial_rnd_state.dump")
+    t0 = time.time()
+    run.do_kmc_steps(d, run_p["output_data"], run_p["random_seed"], "parallel")
+    dt = time.time() - t0
+    u_ship = np.load(ex / "traj1" / "unwrapped_traj.npy")
+    t_ship = np.load(ex / "traj1" / "time_data.npy")
+    u_ref = np.load(d / "unwrapped_traj.npy")
+    t_ref = np.load(d / "time_data.npy")
+    assert np.array_equal(u_ref, u_ship)
+    rel = float(np.abs(t_ref[1:] / t_ship[1:] - 1).max())
+    print(f"{name}: re-run {len(t_ref) - 1} steps in {dt:.1f} s, unwrapped "
+          f"bit-identical, time max rel {rel:.2e}")
+    with open(ex / "traj1" / "initial_rnd_state.dump", "rb") as fh:
+        state = pickle.load(fh)
+    meta, arrs = hop_to_arrays(hop)
+    stride_u = 1 if len(u_ship) <= 20001 else 10
+    stride_t = 1 if len(t_ship) <= 40001 else 16
+    cfg = {"name": name, "params": params, "poscar": poscar, "system_size": [2, 2, 1],
+           "pbc": [1, 1, 1], "run": run_p, "hop_meta": meta,
+           "rnd_state": [state[0], list(state[1]), state[2]],
+           "n_steps": int(len(t_ship) - 1), "unwrapped_stride": stride_u,
+           "time_stride": stride_t, "unwrapped_sha256": sha(u_ship),
+           "reference_seconds": dt,
+           "array_rebuild_max_abs_ha": err}
+    np.savez_compressed(HERE / f"{name.lower()}.npz", A=A_shipped, pmiv=pmiv,
+                        unwrapped=u_ship[::stride_u], time=t_ship[::stride_t],
+                        time_last=t_ship[-1:], **arrs)
+    (HERE / f"{name.lower()}.json").write_text(json.dumps(cfg, indent=1))
+
+
+# ---------------------------------------------------------------- injected run
+class Injected:
+    """random-module stand-in: random() pops injected uniforms, sample()
+    delegates (only used when no initial occupancy is given)."""
+
+    def __init__(self, u):
+        self.u, self.i = u, 0
+
+    def random(self):
+        if self.i >= len(self.u):
+            raise StopIteration
+        v = self.u[self.i]
+        self.i += 1
+        return float(v)
+
+    def sample(self, *a):
+        raise RuntimeError("sample() not expected")
+
+
+def injected_run(core, run, A, occ, uniforms, n_steps_expected):
+    """Run do_kmc_steps' loop with injected uniforms; returns (proc, time)
+    reconstructed from the recorded rates with the reference's expressions."""
+    rec_rates = []
+    orig_rates = core.Run.get_process_rates
+
+    def rates(self, attrs, q):
+        r = orig_rates(self, attrs, q)
+        rec_rates.append(r[0].copy())
+        return r
+
+    saved_rnd = core.rnd
+    core.rnd = Injected(uniforms)
+    core.Run.get_process_rates = rates
+    d = Path(tempfile.mkdtemp())
+    pickle.dump(saved_rnd.getstate(), open(d / "initial_rnd_state.dump", "wb"))
+    core.rnd.setstate = lambda s: None
+    try:
+        run.initial_occupancy = {"electron": list(occ)}
+        out = {k: dict(v) for k, v in RUN_COMMON["output_data"].items()}
+        run.do_kmc_steps(d, out, 0, "parallel")
+    except StopIteration:
+        pass
+    finally:
+        core.rnd = saved_rnd
+        core.Run.get_process_rates = orig_rates
+    # rates recorded for the step that ran out of uniforms are dropped
+    n = min(len(rec_rates), len(uniforms) // 2)
+    procs, times = [], [0.0]
+    t = 0
+    for i in range(n):
+        k = rec_rates[i]
+        k_total = sum(k)
+        cum = (k / k_total).cumsum()
+        procs.append(int(np.where(cum > uniforms[2 * i])[0][0]))
+        t -= np.log(uniforms[2 * i + 1]) / k_total
+        times.append(t)
+    assert n == n_steps_expected, (n, n_steps_expected)
+    return np.asarray(procs, np.uint8), np.asarray(times)
+
+
+def corundum324(core):
+    frac = corundum_frac()
+    poscar = poscar_text("corundum Fe sublattice", CORUNDUM_LATTICE, ["Fe"], [12], frac)
+    tmp = tempfile.mkdtemp()
+    mat, nb = material_objects(core, CORUNDUM, poscar, [3, 3, 3], [1, 1, 1], tmp)
+    t0 = time.time()
+    nb.generate_neighbor_list(Path(tmp), np.array([3, 3, 3]))
+    hop = np.load(Path(tmp) / "hop_neighbor_list.npy", allow_pickle=True)[()]
+    nb.get_pairwise_min_image_vector_data(Path(tmp))
+    pmiv = np.load(Path(tmp) / "pairwise_min_image_vector_data.npy")
+    print(f"corundum324: reference neighbour list + pmiv in {time.time() - t0:.1f} s")
+    system = make_system(core, mat, nb, hop, pmiv, CORUNDUM)
+    t0 = time.time()
+    A = ref_array(system, mat, nb)
+    t_ewald = time.time() - t0
+    site = int(np.random.default_rng(0).integers(324))
+    U = np.random.default_rng(0).random(200000)
+    run = core.Run(system, A, 300, "full", "full", 1, 1e-6, 1e-9, np.array([1]),
+                   {"electron": [site]}, {"class_index": {}, "doping": {}},
+                   RUN_COMMON["external_field"], {"num_dopants": [0]})
+    t0 = time.time()
+    procs, times = injected_run(core, run, A, [site], U, 100000)
+    t_kmc = time.time() - t0
+    print(f"corundum324: Ewald {t_ewald:.2f} s, 1e5 KMC steps {t_kmc:.1f} s")
+    meta, arrs = hop_to_arrays(hop)
+    rows = np.array([0, 1, 161, 323])
+    cfg = {"name": "corundum324", "params": CORUNDUM, "poscar": poscar,
+           "system_size": [3, 3, 3], "pbc": [1, 1, 1], "hop_meta": meta,
+           "carrier_site": site, "uniform_seed": 0, "n_steps": 100000,
+           "t_final": 1e-6, "time_interval": 1e-9, "A_sha256": sha(A),
+           "pmiv_sha256": sha(pmiv), "A_rows": rows.tolist(),
+           "reference_ewald_seconds": t_ewald, "reference_kmc_seconds": t_kmc}
+    np.savez_compressed(HERE / "corundum324.npz", A_rows=A[rows], A_diag=np.diag(A),
+                        proc=procs, time=times[::8], time_last=times[-1:], **arrs)
+    (HERE / "corundum324.json").write_text(json.dumps(cfg, indent=1))
+    return mat
+
+
+def corundum3600(core):
+    sys.path.insert(0, str(REPO))
+    from oracle import ewald_oracle as eo
+    import pycd_gb300.lattice as ml
+    frac = corundum_frac()
+    poscar = poscar_text("corundum Fe sublattice", CORUNDUM_LATTICE, ["Fe"], [12], frac)
+    tmp = tempfile.mkdtemp()
+    params = dict(CORUNDUM)
+    mat, nb = material_objects(core, params, poscar, [10, 10, 3], [1, 1, 1], tmp)
+    p = dict(params)
+    p.pop("precision_parameters")
+    (Path(tmp) / "P2").write_text(poscar)
+    p["input_coord_file_location"] = Path(tmp) / "P2"
+    mm = ml.Material(ml.ReturnValues(**p))
+    mn = ml.Neighbors(mm, np.array([10, 10, 3]), np.array([1, 1, 1]))
+    t0 = time.time()
+    hop = mn.generate_neighbor_list(None, (3, 3, 3), save=False)
+    print(f"corundum3600: hop list (this package) {time.time() - t0:.1f} s")
+    lat = mm.lattice_matrix
+    # units as System: alpha / ANG2BOHR, r_cut * ANG2BOHR, k_cut / ANG2BOHR
+    from pycd_gb300 import constants as K
+    alpha = params["alpha"] / K.ANG2BOHR
+    t0 = time.time()
+    A = eo.class_array(mm.cartesian_unit_cell_coords, lat, [10, 10, 3], alpha,
+                       params["r_cut"] * K.ANG2BOHR, params["k_cut"] / K.ANG2BOHR,
+                       params["dielectric_constant"])
+    print(f"corundum3600: oracle class array {time.time() - t0:.1f} s")
+    system = core.System(mat, nb, hop, None, params["alpha"], params["r_cut"],
+                         params["k_cut"], params["precision_parameters"], [], [])
+    rng = np.random.default_rng(3600)
+    sites = rng.choice(3600, size=8, replace=False)
+    carriers, dopants = sites[:4].tolist(), sites[4:].tolist()
+    # dopants: lattice charge 0 overwritten by +1 (charge_config, core.py:2550-2554)
+    doping = {"num_dopants": [4], "doping_element_map": ["Fe:D"],
+              "insertion_type": ["manual"], "charge": {"full": {"D": 1.0}},
+              "site_charge_initiation": ["no"], "min_shell_separation": [0],
+              "max_attempts": 1}
+    relE = {"class_index": {}, "doping": {"Fe": [[0.0]]}}
+    procs_all, times_all = [], []
+    for traj in range(2):
+        # carriers trapped on +1 dopants have residence times of ~1e14 s, so
+        # the time grid spans 1e30 s to keep the run going for 2,000 steps
+        run = core.Run(system, A, 300, "full", "full", 1, 1e30, 1e27, np.array([4]),
+                       {"electron": carriers}, relE, RUN_COMMON["external_field"], doping)
+        U = np.random.default_rng(1000 + traj).random(4000)
+        d = Path(tempfile.mkdtemp())
+        # site_indices.npy: [site, dopant type, unused, shell]
+        si = np.array([[s, 0, 0, 0] for s in dopants])
+        rec = []
+        orig = core.Run.get_process_rates
+
+        def rates(self, attrs, q):
+            r = orig(self, attrs, q)
+            rec.append(r[0].copy())
+            return r
+
+        saved = core.rnd
+        core.rnd = Injected(U)
+        core.rnd.setstate = lambda s: None
+        core.Run.get_process_rates = rates
+        pickle.dump(saved.getstate(), open(d / "initial_rnd_state.dump", "wb"))
+        np.save(d / "site_indices.npy", si)
+        t0 = time.time()
+        try:
+            out = {k: dict(v) for k, v in RUN_COMMON["output_data"].items()}
+            run.do_kmc_steps(d, out, 0, "parallel")
+        except StopIteration:
+            pass
+        finally:
+            core.rnd = saved
+            core.Run.get_process_rates = orig
+        print(f"corundum3600 traj {traj}: 2000 steps in {time.time() - t0:.1f} s")
+        procs, times, t = [], [0.0], 0
+        for i in range(2000):
+            k = rec[i]
+            kt = sum(k)
+            procs.append(int(np.where((k / kt).cumsum() > U[2 * i])[0][0]))
+            t -= np.log(U[2 * i + 1]) / kt
+            times.append(t)
+        procs_all.append(procs)
+        times_all.append(times)
+    cfg = {"name": "corundum3600", "params": params, "poscar": poscar,
+           "system_size": [10, 10, 3], "pbc": [1, 1, 1], "carriers": carriers,
+           "dopants": dopants, "dopant_charge": 1.0, "uniform_seeds": [1000, 1001],
+           "n_steps": 2000, "t_final": 1e30, "time_interval": 1e27}
+    np.savez_compressed(HERE / "corundum3600.npz", proc=np.asarray(procs_all, np.uint8),
+                        time=np.asarray(times_all),
+                        A_rows=A[np.array(carriers + dopants)])
+    (HERE / "corundum3600.json").write_text(json.dumps(cfg, indent=1))
+
+
+def main(parts):
+    core = install_shims()
+    if "hematite" in parts:
+        example(core, "Hematite", HEMATITE, 1e-4)
+    if "bvo" in parts:
+        example(core, "BVO", BVO, 1e-3)
+    if "corundum324" in parts:
+        corundum324(core)
+    if "corundum3600" in parts:
+        corundum3600(core)
+
+
+if __name__ == "__main__":
+    main(sys.argv[1:] or ["hematite", "bvo", "corundum324", "corundum3600"])

@@ -1,0 +1,81 @@
+"""GPU: the Ewald array built by the CUDA kernels against the reference's
+arrays and the oracle.  Tolerance: every entry within 1e-10 eV."""
+import numpy as np
+import pytest
+
+import golden_io as gio
+from oracle import ewald_oracle as eo
+from pycd_gb300 import constants as K
+from pycd_gb300 import workloads as wl
+from pycd_gb300.core import System
+
+pytestmark = pytest.mark.gpu
+TOL_HA = 1e-10 * K.EV2HARTREE  # 1e-10 eV
+
+
+def _system(name, pmiv):
+    cfg, arr = gio.load(name)
+    mat, nb = gio.material(cfg)
+    p = cfg["params"]
+    return System(mat, nb, gio.hop_list(cfg, arr), pmiv, p["alpha"], p["r_cut"],
+                  p["k_cut"]), cfg, arr
+
+
+@pytest.mark.parametrize("name", ["hematite", "bvo"])
+def test_direct_build_matches_shipped_array(cuda_ready, name):
+    cfg, arr = gio.load(name)
+    sysm, cfg, arr = _system(name, arr["pmiv"])
+    A, dst = sysm.get_precomputed_array(None)
+    assert sysm.last_build_info["mode"] == "fp64_direct"
+    assert A.shape == arr["A"].shape and A.dtype == np.float64
+    assert np.abs(A - arr["A"]).max() < TOL_HA
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp64_direct"])
+def test_corundum324_build_matches_oracle_and_reference(cuda_ready, precision):
+    cfg, arr = gio.load("corundum324")
+    mat, nb = gio.material(cfg)
+    pmiv = nb.get_pairwise_min_image_vector_data(None)
+    p = cfg["params"]
+    sysm = System(mat, nb, gio.hop_list(cfg, arr), pmiv, p["alpha"], p["r_cut"],
+                  p["k_cut"])
+    A, _ = sysm.get_precomputed_array(None, precision=precision)
+    assert sysm.last_build_info["mode"] == precision
+    assert sysm.last_build_info["n_kvec"] == 280
+    ref = eo.precomputed_array(pmiv, sysm.reciprocal_lattice_matrix,
+                               sysm.system_volume, sysm.alpha, sysm.r_cut,
+                               sysm.k_cut, mat.dielectric_constant)
+    assert np.abs(A - ref).max() < TOL_HA
+    rows = np.asarray(cfg["A_rows"])
+    assert np.abs(A[rows] - arr["A_rows"]).max() < TOL_HA
+    assert np.abs(np.diag(A) - arr["A_diag"]).max() < TOL_HA
+
+
+def test_build_without_pmiv_uses_device_min_image(cuda_ready):
+    cfg, arr = gio.load("corundum324")
+    mat, nb = gio.material(cfg)
+    p = cfg["params"]
+    sysm = System(mat, nb, gio.hop_list(cfg, arr), None, p["alpha"], p["r_cut"],
+                  p["k_cut"])
+    A_gemm = sysm.get_precomputed_array_device("fp64").cpu().numpy()
+    A_dir = sysm.get_precomputed_array_device("fp64_direct").cpu().numpy()
+    rows = np.asarray(cfg["A_rows"])
+    assert np.abs(A_gemm[rows] - arr["A_rows"]).max() < TOL_HA
+    assert np.abs(A_dir - A_gemm).max() < TOL_HA
+
+
+def test_corundum3600_build_properties_and_oracle_rows(cuda_ready):
+    sysm = wl.corundum((10, 10, 3))
+    A = sysm.get_precomputed_array_device("fp64")
+    assert sysm.last_build_info["n_kvec"] == 3151
+    An = A.cpu().numpy()
+    # symmetric, equal diagonal, translation invariant (size-independent)
+    assert np.abs(An - An.T).max() < TOL_HA
+    assert np.ptp(np.diag(An)) < TOL_HA
+    mat = sysm.material
+    rng = np.random.default_rng(7)
+    rows = rng.choice(3600, size=12, replace=False)
+    ref = eo.class_array(mat.cartesian_unit_cell_coords, mat.lattice_matrix,
+                         (10, 10, 3), sysm.alpha, sysm.r_cut, sysm.k_cut,
+                         mat.dielectric_constant, rows=rows)
+    assert np.abs(An[rows] - ref).max() < TOL_HA

@@ -1,0 +1,195 @@
+"""GPU: the KMC kernel against the reference's trajectories, the oracle, and
+itself (one trajectory alone vs inside a batch).
+
+Events and carrier sites must match bit-exactly; residence times within
+1e-12 relative; unwrapped displacement rows bit-identical."""
+import hashlib
+import pickle
+import tempfile
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import golden_io as gio
+from oracle import kmc_oracle as ko
+from oracle import philox
+from pycd_gb300 import _native as nat
+from pycd_gb300 import constants as K
+from pycd_gb300 import workloads as wl
+from pycd_gb300.core import Run, System
+from pycd_gb300.kmc import KmcBatch, KmcEngine
+
+pytestmark = pytest.mark.gpu
+TIME_RTOL = 1e-12
+
+
+def _example_run(name):
+    cfg, arr = gio.load(name)
+    mat, nb = gio.material(cfg)
+    p, r = cfg["params"], cfg["run"]
+    sysm = System(mat, nb, gio.hop_list(cfg, arr), arr["pmiv"], p["alpha"],
+                  p["r_cut"], p["k_cut"])
+    run = Run(sysm, arr["A"], r["temp"], r["ion_charge_type"],
+              r["species_charge_type"], 1, r["t_final"], r["time_interval"],
+              np.asarray(r["species_count"]), r["initial_occupancy"],
+              r["relative_energies"], r["external_field"], r["doping"])
+    return cfg, arr, run
+
+
+@pytest.mark.parametrize("name", ["bvo", "hematite"])
+def test_do_kmc_steps_reproduces_shipped_trajectory(cuda_ready, name):
+    cfg, arr, run = _example_run(name)
+    d = Path(tempfile.mkdtemp())
+    st = cfg["rnd_state"]
+    with open(d / "initial_rnd_state.dump", "wb") as fh:
+        pickle.dump((st[0], tuple(st[1]), st[2]), fh)
+    run.do_kmc_steps(d, cfg["run"]["output_data"], cfg["run"]["random_seed"],
+                     "parallel")
+    u = np.load(d / "unwrapped_traj.npy")
+    t = np.load(d / "time_data.npy")
+    assert len(t) == cfg["n_steps"] + 1
+    assert hashlib.sha256(u.tobytes()).hexdigest() == cfg["unwrapped_sha256"]
+    ts = t[::cfg["time_stride"]]
+    assert np.abs(ts[1:] / arr["time"][1:] - 1).max() < TIME_RTOL
+    assert abs(t[-1] / arr["time_last"][0] - 1) < TIME_RTOL
+    assert (d / "Run.log").exists()
+
+
+def _corundum324_engine(cfg, arr):
+    import torch
+    mat, nb = gio.material(cfg)
+    sysm = System(mat, nb, gio.hop_list(cfg, arr), None, cfg["params"]["alpha"],
+                  cfg["params"]["r_cut"], cfg["params"]["k_cut"])
+    A = sysm.get_precomputed_array_device("fp64")
+    tables, run = wl.batched_tables(sysm, A, 1, [], t_final=cfg["t_final"],
+                                    time_interval=cfg["time_interval"])
+    return tables, run
+
+
+def test_plain_events_match_reference_corundum324(cuda_ready):
+    import torch
+    cfg, arr = gio.load("corundum324")
+    tables, run = _corundum324_engine(cfg, arr)
+    n = cfg["n_steps"]
+    u = torch.as_tensor(np.random.default_rng(cfg["uniform_seed"]).random(2 * n)
+                        ).cuda()[None, :]
+    batch = KmcBatch([[cfg["carrier_site"]]], step_capacity=n,
+                     unwrapped_rows=tables.n_path_steps)
+    eng = KmcEngine(tables)
+    eng.advance(batch, n + 10, eng.rng_struct(u))
+    torch.cuda.synchronize()
+    assert int(batch.status.item()) == nat.TRAJ_NEED_UNIFORMS
+    assert int(batch.step.item()) == n
+    proc = batch.step_proc[0].cpu().numpy()
+    assert np.array_equal(proc, arr["proc"].astype(np.int32))
+    t = batch.step_time[0].cpu().numpy()[7::8]
+    assert np.abs(t / arr["time"][1:len(t) + 1] - 1).max() < TIME_RTOL
+
+
+def _corundum3600(n_carriers=4):
+    sysm = wl.corundum((10, 10, 3))
+    A = sysm.get_precomputed_array_device("fp64")
+    cfg, arr = gio.load("corundum3600")
+    tables, run = wl.batched_tables(sysm, A, n_carriers, cfg["dopants"],
+                                    cfg["dopant_charge"], t_final=cfg["t_final"],
+                                    time_interval=cfg["time_interval"])
+    return sysm, tables, run, cfg, arr
+
+
+def test_batched_events_match_reference_corundum3600(cuda_ready):
+    import torch
+    sysm, tables, run, cfg, arr = _corundum3600()
+    n = cfg["n_steps"]
+    U = np.stack([np.random.default_rng(s).random(2 * n) for s in cfg["uniform_seeds"]])
+    batch = KmcBatch([cfg["carriers"]] * 2, step_capacity=n)
+    eng = KmcEngine(tables)
+    eng.advance(batch, n, eng.rng_struct(torch.as_tensor(U).cuda()))
+    torch.cuda.synchronize()
+    assert batch.step.cpu().tolist() == [n, n]
+    assert np.array_equal(batch.step_proc.cpu().numpy(), arr["proc"].astype(np.int32))
+    t = batch.step_time.cpu().numpy()
+    assert np.abs(t / arr["time"][:, 1:] - 1).max() < TIME_RTOL
+
+
+def test_batch_equals_plain_and_oracle_on_sampled_trajectories(cuda_ready):
+    """512 Philox trajectories advanced together; 8 of them re-run alone
+    (plain form) must give identical events and times, and the oracle, fed
+    the same Philox uniforms, the same events for a prefix."""
+    import torch
+    sysm, tables, run, cfg, arr = _corundum3600()
+    T, n, seed = 512, 20000, 12345
+    rng = np.random.default_rng(99)
+    occ = np.stack([rng.choice(3600, size=4, replace=False) for _ in range(T)])
+    eng = KmcEngine(tables)
+    batch = KmcBatch(occ, step_capacity=n)
+    # two chunks: resume from device state must not change anything
+    eng.advance(batch, n // 2, eng.rng_struct(seed=seed))
+    eng.advance(batch, n - n // 2, eng.rng_struct(seed=seed))
+    torch.cuda.synchronize()
+    assert (batch.step.cpu().numpy() == n).all()
+    picks = rng.choice(T, size=8, replace=False)
+    for t in picks:
+        single = KmcBatch(occ[t:t + 1], step_capacity=n)
+        eng.advance(single, n, eng.rng_struct(seed=seed, traj_offset=int(t)))
+        torch.cuda.synchronize()
+        assert np.array_equal(single.step_proc[0].cpu().numpy(),
+                              batch.step_proc[t].cpu().numpy())
+        assert np.array_equal(single.step_time[0].cpu().numpy(),
+                              batch.step_time[t].cpu().numpy())
+        assert np.array_equal(single.occ[0].cpu().numpy(), batch.occ[t].cpu().numpy())
+    # oracle on a prefix of two sampled trajectories, same Philox stream
+    A = tables.A.cpu().numpy()
+    q_fixed = np.zeros(3600)
+    q_fixed[cfg["dopants"]] = cfg["dopant_charge"]
+    hop = sysm.hop_neighbor_list
+    otab = ko.Tables(hop, "Fe:Fe", np.zeros(3600, int), 12, 0, 12,
+                     sysm.material.lambda_values["Fe:Fe"], sysm.material.v_ab["Fe:Fe"])
+    m = 1500
+    for t in picks[:2]:
+        u = np.array([v for s in range(m) for v in philox.step_uniforms(seed, int(t), s)])
+        o = ko.run(A, otab, list(occ[t]), q_fixed, -1.0, np.zeros(3600),
+                   sysm.material.vn, run.temp, u, run.time_interval,
+                   tables.n_path_steps)
+        assert np.array_equal(o["proc"], batch.step_proc[t, :m].cpu().numpy())
+        assert np.abs(o["time"][1:] / batch.step_time[t, :m].cpu().numpy() - 1).max() \
+            < TIME_RTOL
+
+
+def test_device_philox_matches_host(cuda_ready):
+    import torch
+    out = torch.empty(2 * 64, dtype=torch.float64, device="cuda")
+    nat.check(nat.lib().pycd_philox_uniforms(777, 5, 1000, 64, out.data_ptr(),
+                                             nat.stream_handle()))
+    torch.cuda.synchronize()
+    ref = np.array([v for s in range(1000, 1064) for v in philox.step_uniforms(777, 5, s)])
+    assert np.array_equal(out.cpu().numpy(), ref)
+
+
+def test_zero_rates_stop_with_stalled_status(cuda_ready):
+    """vn = 0 makes every rate 0: the kernel must report STALLED, not hang
+    or index out of bounds (the reference raises IndexError here)."""
+    import torch
+    cfg, arr = gio.load("corundum324")
+    tables, run = _corundum324_engine(cfg, arr)
+    tables.vn = 0.0
+    batch = KmcBatch([[5], [17]])
+    eng = KmcEngine(tables)
+    eng.advance(batch, 100, eng.rng_struct(seed=1))
+    torch.cuda.synchronize()
+    assert batch.status.cpu().tolist() == [nat.TRAJ_STALLED] * 2
+    assert batch.step.cpu().tolist() == [0, 0]
+
+
+def test_out_of_range_neighbour_stops_with_bad_index(cuda_ready):
+    import torch
+    cfg, arr = gio.load("corundum324")
+    tables, run = _corundum324_engine(cfg, arr)
+    tables.nbr[5, 2] = 10 ** 6  # a corrupt table entry, caught before any gather
+    batch = KmcBatch([[5], [17]])
+    eng = KmcEngine(tables)
+    eng.advance(batch, 50, eng.rng_struct(seed=1))
+    torch.cuda.synchronize()
+    st = batch.status.cpu().tolist()
+    assert st[0] == nat.TRAJ_BAD_INDEX
+    assert st[1] in (nat.TRAJ_RUNNING, nat.TRAJ_BAD_INDEX)

@@ -1,0 +1,173 @@
+"""CPU: host-side set-up (lattice, neighbour lists, k-vectors, process
+tables) and the C-ABI library's exports.  No compute call needs a GPU."""
+import ctypes
+import re
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import golden_io as gio
+from oracle import ewald_oracle as eo
+from oracle import kmc_oracle as ko
+from pycd_gb300 import _native as nat
+from pycd_gb300 import ewald as ew
+from pycd_gb300.core import Run, System
+
+ROOT = Path(__file__).resolve().parent.parent
+
+
+def test_library_exports_every_declared_symbol():
+    lib = nat.lib()
+    header = (ROOT / "include" / "pycd_gb300.h").read_text()
+    declared = re.findall(r"PYCD_API\s+[\w\s\*]*?\b(pycd_\w+)\s*\(", header)
+    assert len(declared) >= 12
+    for name in declared:
+        assert hasattr(lib, name), name
+        assert name in nat.exported_symbols(), name
+    assert lib.pycd_abi_version() == 1
+
+
+def test_library_reports_missing_device_as_error():
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    with pytest.raises(nat.NativeError) as e:
+        nat.require_device()
+    assert e.value.status == nat.ERR_NO_DEVICE
+
+
+def test_neighbor_list_matches_reference_corundum324():
+    cfg, arr = gio.load("corundum324")
+    mat, nb = gio.material(cfg)
+    ours = nb.generate_neighbor_list(None, (3, 3, 3), save=False)
+    ref = gio.hop_list(cfg, arr)
+    for key in ref:
+        for ci, per_type in enumerate(ref[key]):
+            for ti, rv in enumerate(per_type):
+                mine = ours[key][ci][ti]
+                assert np.array_equal(mine.num_neighbors, rv.num_neighbors)
+                for i in range(len(rv.num_neighbors)):
+                    assert np.array_equal(mine.neighbor_system_element_indices[i],
+                                          rv.neighbor_system_element_indices[i])
+                    assert np.array_equal(mine.displacement_vector_list[i],
+                                          rv.displacement_vector_list[i])
+
+
+def test_pmiv_matches_reference_corundum324():
+    import hashlib
+    cfg, arr = gio.load("corundum324")
+    mat, nb = gio.material(cfg)
+    pmiv = nb.get_pairwise_min_image_vector_data(None)
+    assert hashlib.sha256(pmiv.tobytes()).hexdigest() == cfg["pmiv_sha256"]
+
+
+@pytest.mark.parametrize("name", ["corundum324", "hematite", "bvo"])
+def test_k_vectors_match_oracle(name):
+    cfg, arr = gio.load(name)
+    mat, nb = gio.material(cfg)
+    sysm = System(mat, nb, gio.hop_list(cfg, arr) if "hop_meta" in cfg else None,
+                  None, cfg["params"]["alpha"], cfg["params"]["r_cut"],
+                  cfg["params"]["k_cut"])
+    kmax = ew.k_max_for(sysm, sysm.k_cut)
+    ours = ew.effective_k_vectors(sysm.reciprocal_lattice_matrix, kmax, sysm.k_cut)
+    ref = []
+    for kv in eo.effective_k_vectors(kmax):
+        k = np.dot(kv, sysm.reciprocal_lattice_matrix)
+        if np.dot(k, k) < sysm.k_cut ** 2:
+            ref.append(kv)
+    assert np.array_equal(ours, np.asarray(ref, np.int32))
+    # the C++ enumerator gives the same list
+    L = nat.lib()
+    recip = (ctypes.c_double * 9)(*sysm.reciprocal_lattice_matrix.ravel())
+    km = (ctypes.c_int32 * 3)(*[int(v) for v in kmax])
+    n = ctypes.c_int64()
+    assert L.pycd_ewald_kvectors(recip, km, sysm.k_cut, None, 0, ctypes.byref(n)) == 0
+    buf = (ctypes.c_int32 * (3 * n.value))()
+    assert L.pycd_ewald_kvectors(recip, km, sysm.k_cut, buf, n.value,
+                                 ctypes.byref(n)) == 0
+    assert np.array_equal(np.frombuffer(buf, np.int32).reshape(-1, 3), ours)
+
+
+def test_corundum324_uses_feature_contraction():
+    cfg, arr = gio.load("corundum324")
+    mat, nb = gio.material(cfg)
+    pmiv = nb.get_pairwise_min_image_vector_data(None)
+    sysm = System(mat, nb, gio.hop_list(cfg, arr), pmiv, 0.25, 6.4, 1.6)
+    assert ew.choose_mode(sysm, pmiv) == "fp64"
+    assert ew.choose_mode(sysm, None) == "fp64"
+
+
+def test_shipped_hematite_pmiv_needs_direct_mode():
+    cfg, arr = gio.load("hematite")
+    mat, nb = gio.material(cfg)
+    sysm = System(mat, nb, gio.hop_list(cfg, arr), arr["pmiv"], 0.2667, 4.618, 6.998)
+    assert ew.choose_mode(sysm, arr["pmiv"]) == "fp64_direct"
+    with pytest.raises(ValueError):
+        ew.choose_mode(sysm, arr["pmiv"], "fp64")
+
+
+def _run(cfg, arr, mat, nb):
+    run = cfg["run"]
+    sysm = System(mat, nb, gio.hop_list(cfg, arr), None, cfg["params"]["alpha"],
+                  cfg["params"]["r_cut"], cfg["params"]["k_cut"])
+    return Run(sysm, arr["A"], run["temp"], run["ion_charge_type"],
+               run["species_charge_type"], 1, run["t_final"], run["time_interval"],
+               np.asarray(run["species_count"]), run["initial_occupancy"],
+               run["relative_energies"], run["external_field"], run["doping"])
+
+
+@pytest.mark.parametrize("name", ["hematite", "bvo"])
+def test_site_tables_match_oracle_process_lists(name):
+    cfg, arr = gio.load(name)
+    mat, nb = gio.material(cfg)
+    r = _run(cfg, arr, mat, nb)
+    hop = gio.hop_list(cfg, arr)
+    key = r.hop_element_type
+    et = key.split(":")[0]
+    ei = mat.element_types.index(et)
+    t = ko.Tables(hop, key, np.tile(mat.unit_cell_class_list, int(nb.num_cells)),
+                  int(mat.n_elements_per_unit_cell[ei]),
+                  int(mat.n_elements_per_unit_cell[:ei].sum()),
+                  int(mat.total_elements_per_unit_cell),
+                  mat.lambda_values[key], mat.v_ab[key])
+    n_checked = 0
+    for site in range(nb.num_system_elements):
+        if r.site_nbr[site, 0] < 0:
+            continue
+        procs = t.processes(site)
+        assert len(procs) == r.n_slots == r.n_proc
+        for s, (n, h, lam, vab, _) in enumerate(procs):
+            assert r.site_nbr[site, s] == n
+            assert np.array_equal(r.site_hop[site, s], h)
+            assert r.site_lam[site, s] == lam and r.site_vab[site, s] == vab
+        n_checked += 1
+    assert n_checked == nb.num_cells * mat.n_elements_per_unit_cell[ei]
+
+
+def test_multi_species_runs_are_rejected():
+    cfg, arr = gio.load("hematite")
+    mat, nb = gio.material(cfg)
+    cfg = dict(cfg)
+    cfg["run"] = dict(cfg["run"], species_count=[1, 1])
+    with pytest.raises(NotImplementedError):
+        _run(cfg, arr, mat, nb)
+
+
+@pytest.mark.parametrize("name,cells", [("hematite", (2, 2, 1)), ("bvo", (3, 3, 3)),
+                                        ("corundum324", (4, 3, 3))])
+def test_translated_neighbor_list_equals_full_scan(name, cells):
+    cfg, arr = gio.load(name)
+    mat, nb = gio.material(cfg, system_size=cells)
+    fast = nb.generate_neighbor_list(None, (3, 3, 3), save=False, method="auto")
+    scan = nb.generate_neighbor_list(None, (3, 3, 3), save=False, method="scan")
+    for key in scan:
+        for ci in range(len(scan[key])):
+            for ti in range(len(scan[key][ci])):
+                a, b = fast[key][ci][ti], scan[key][ci][ti]
+                assert np.array_equal(a.num_neighbors, b.num_neighbors)
+                for i in range(len(b.num_neighbors)):
+                    assert np.array_equal(a.neighbor_system_element_indices[i],
+                                          b.neighbor_system_element_indices[i])
+                    assert np.array_equal(np.asarray(a.displacement_vector_list[i]).reshape(-1, 3),
+                                          np.asarray(b.displacement_vector_list[i]).reshape(-1, 3))
