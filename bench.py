@@ -95,7 +95,7 @@ class ClockSampler(object):
                 "samples": len(self.rows)}
 
 
-def build_workload(rank=0):
+def build_workload(rank=0, n_traj=N_TRAJ):
     """System, device array, tables and initial carrier sites."""
     import torch
     from pycd_gb300 import workloads as wl
@@ -107,7 +107,7 @@ def build_workload(rank=0):
     rng = np.random.default_rng(SEED + rank)
     free = np.setdiff1d(np.arange(3600), dopants)
     occ = np.stack([rng.choice(free, size=N_CARRIERS, replace=False)
-                    for _ in range(N_TRAJ)]).astype(np.int32)
+                    for _ in range(n_traj)]).astype(np.int32)
     torch.cuda.synchronize()
     return system, A, tables, run, dopants, occ
 
@@ -264,16 +264,14 @@ def main():
     from pycd_gb300 import _native as nat
     from pycd_gb300.batch import BatchedKmc, run_batched
     nat.require_device()
-    global N_TRAJ
-    N_TRAJ = args.traj
-    system, A, tables, run, dopants, occ = build_workload(rank)
+    system, A, tables, run, dopants, occ = build_workload(rank, args.traj)
     launch = {}
     if args.lanes:
         launch["lanes_per_traj"] = args.lanes
     if args.warps:
         launch["warps_per_block"] = args.warps
     bk = BatchedKmc(tables, occ, seed=SEED, chunk_steps=args.chunk,
-                    traj_offset=rank * N_TRAJ, launch=launch)
+                    traj_offset=rank * args.traj, launch=launch)
     flush = torch.empty(256 * 2 ** 20, dtype=torch.uint8, device="cuda")
     for _ in range(args.warmup):
         bk.step_chunk()
@@ -350,7 +348,7 @@ def main():
             "config": {"workload": "batched uniform: corundum 10x10x3 = 3,600 sites, "
                                    "4 electrons + 4 fixed +1 dopants, FP64 Ewald array "
                                    "(103.7 MB), Philox streams",
-                       "trajectories_per_gpu": N_TRAJ, "steps_per_chunk": args.chunk,
+                       "trajectories_per_gpu": args.traj, "steps_per_chunk": args.chunk,
                        "chunk": "one CUDA-graph launch of the persistent kernel",
                        "l2": "256 MiB buffer written between timed chunks",
                        "parallelism": f"replicas x{world}"},

@@ -461,7 +461,8 @@ class Run(object):
                 times.append(batch.step_time[0, :n_done].cpu().numpy().copy())
                 procs.append(batch.step_proc[0, :n_done].cpu().numpy().copy())
                 status = int(batch.status.item())
-                if status == nat.TRAJ_NEED_UNIFORMS:
+                if status in (nat.TRAJ_RUNNING, nat.TRAJ_NEED_UNIFORMS):
+                    # the block of uniforms is used up: draw the next one
                     batch.status.zero_()
                     continue
                 if status == nat.TRAJ_DONE:

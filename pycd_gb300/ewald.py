@@ -51,17 +51,30 @@ def pmiv_is_lattice_consistent(system, pmiv, tol=1e-8):
     i.e. cos(k . pmiv_ij) = cos(k . r_j - k . r_i) for every kept k."""
     if not ewald_cell_matches_supercell(system):
         return False
-    coords = system.neighbors.bulk_sites.cell_coordinates
-    inv = system.neighbors.simulation_cell_matrix_inv
+    return lattice_deviation(system, pmiv) <= tol
+
+
+def lattice_deviation(system, pmiv):
+    """Largest distance (in supercell fractional units) of any
+    pmiv_ij - (r_j - r_i) from a supercell translation; inf for non-finite
+    input."""
+    coords = np.asarray(system.neighbors.bulk_sites.cell_coordinates, np.float64)
+    inv = np.asarray(system.neighbors.simulation_cell_matrix_inv, np.float64)
+    pmiv = np.asarray(pmiv, dtype=np.float64)
     n = len(coords)
+    if pmiv.shape != (n, n, 3):
+        raise ValueError("pmiv must have shape (N, N, 3), got %r" % (pmiv.shape,))
+    worst = 0.0
     chunk = max(1, 2_000_000 // max(1, n))
     for s in range(0, n, chunk):
         e = min(n, s + chunk)
         d = pmiv[s:e] - (coords[None, :, :] - coords[s:e, None, :])
-        f = np.dot(d.reshape(-1, 3), inv)
-        if np.abs(f - np.round(f)).max() > tol:
-            return False
-    return True
+        f = d.reshape(-1, 3) @ inv
+        dev = np.abs(f - np.rint(f))
+        if not np.all(np.isfinite(dev)):
+            return float("inf")
+        worst = max(worst, float(dev.max()))
+    return worst
 
 
 def ewald_cell_matches_supercell(system, rtol=1e-12):
