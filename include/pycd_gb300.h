@@ -138,6 +138,25 @@ PYCD_API int pycd_ewald_build(const PycdEwaldDesc* desc, int mode, double* d_out
                      void* d_workspace, size_t workspace_bytes, void* stream,
                      float* real_ms, float* fourier_ms);
 
+/* Allocation-free variant of pycd_ewald_build in PYCD_EWALD_FP64_GEMM mode.
+ * No counterpart in the reference: it exists for callers that must not
+ * allocate device memory, e.g. a C or Fortran host that receives only the
+ * input and output device buffers from another runtime whose allocator owns
+ * the GPU's memory.  The scratch (per-k constants and N x 2K feature rows,
+ * 8 * (5K + N * 2K) bytes rounded up) lives in a fixed 32 MiB device array
+ * inside the library, reserved on every GPU that loads it until the process
+ * exits; larger (N, K) are rejected with PYCD_ERR_WORKSPACE.  The caller
+ * still passes the descriptor's input buffers and d_out.
+ *   - The first call on a device resolves the array's device address with
+ *     that device current; make that first call before any stream capture.
+ *   - Every call uses the same array: calls whose work overlaps on the GPU
+ *     (different streams, or different host threads on one device) race and
+ *     must be serialised by the caller.  No state carries over between
+ *     calls: each call writes the scratch before it reads it.
+ *   - Makes no cudaMalloc/cudaFree or allocating library call.            */
+PYCD_API int pycd_ewald_build_noalloc(const PycdEwaldDesc* desc, double* d_out,
+                                      void* stream);
+
 /* phi = A q for a dense charge vector (lattice charges with dopants
  * overwritten): the background part of np.dot(charge, A[n]-A[o])
  * (PyCD/core.py:2004-2008).  Also returns E = q^T A q in *d_energy when

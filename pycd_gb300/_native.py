@@ -105,6 +105,7 @@ _PROTOS = {
     "pycd_ewald_build": (C.c_int, [P(EwaldDesc), C.c_int, C.c_void_p,
                                    C.c_void_p, C.c_size_t, C.c_void_p,
                                    P(C.c_float), P(C.c_float)]),
+    "pycd_ewald_build_noalloc": (C.c_int, [P(EwaldDesc), C.c_void_p, C.c_void_p]),
     "pycd_potential_gemv": (C.c_int, [C.c_void_p, C.c_int64, C.c_void_p,
                                       C.c_void_p, C.c_void_p, C.c_void_p]),
     "pycd_kmc_workspace_size": (C.c_int, [C.c_int32, P(C.c_size_t)]),

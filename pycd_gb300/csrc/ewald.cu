@@ -17,6 +17,8 @@
 #include <math.h>
 #include <stdint.h>
 
+#include <mutex>
+
 #include "common.cuh"
 
 namespace pycd {
@@ -436,6 +438,43 @@ int ewald_build(const PycdEwaldDesc* d, int mode, double* out, void* ws,
   return PYCD_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Allocation-free variant of the FP64 feature-contraction build.
+//
+// Some callers cannot allocate device memory: a host program that is handed
+// only the input and output device buffers by another runtime whose caching
+// allocator owns the GPU's memory (a C or Fortran code coupled to a larger
+// framework, for instance) must not create allocations of its own.  For them
+// the scratch (per-k constants and the N x 2K feature rows) lives in this
+// fixed file-scope array instead of a caller workspace.  Every GPU that loads
+// the library keeps these 32 MiB reserved until the process exits.
+// ---------------------------------------------------------------------------
+constexpr size_t kNoAllocScratchBytes = size_t(32) << 20;
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+// Host code cannot use &g_noalloc_scratch as a device address (it names a
+// host-side stand-in), so the address is resolved once per device with that
+// device current and cached here.
+constexpr int kMaxDevices = 64;
+static void* g_noalloc_ptr[kMaxDevices] = {nullptr};
+static std::mutex g_noalloc_mutex;
+
+static int noalloc_scratch(void** out) {
+  int dev = 0;
+  PYCD_CUDA(cudaGetDevice(&dev));
+  PYCD_REQUIRE(dev >= 0 && dev < kMaxDevices, "device ordinal %d out of range", dev);
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  if (!g_noalloc_ptr[dev]) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess)
+      return cuda_fail(e, "cudaGetSymbolAddress(g_noalloc_scratch)", __FILE__, __LINE__);
+    g_noalloc_ptr[dev] = p;
+  }
+  *out = g_noalloc_ptr[dev];
+  return PYCD_OK;
+}
+
 int potential_gemv(const double* A, int64_t n, const double* q, double* phi,
                    double* energy, cudaStream_t s) {
   PYCD_REQUIRE(A && q && phi && n > 0, "potential_gemv: bad arguments");
@@ -450,3 +489,29 @@ int potential_gemv(const double* A, int64_t n, const double* q, double* phi,
 }
 
 }  // namespace pycd
+
+extern "C" int pycd_ewald_build_noalloc(const PycdEwaldDesc* desc, double* d_out,
+                                        void* stream) {
+  using namespace pycd;
+  clear_error();
+  PYCD_REQUIRE(d_out != nullptr, "d_out is NULL");
+  int rc = ewald_validate(desc, PYCD_EWALD_FP64_GEMM);
+  if (rc) return rc;
+  const size_t need = ewald_workspace_bytes(desc, PYCD_EWALD_FP64_GEMM);
+  if (need > kNoAllocScratchBytes) {
+    set_error("pycd_ewald_build_noalloc: N=%lld with K=%lld needs %zu bytes of "
+              "scratch; the fixed scratch holds %zu bytes (use pycd_ewald_build "
+              "with a workspace)",
+              (long long)desc->n_sites, (long long)desc->n_kvec, need,
+              kNoAllocScratchBytes);
+    return PYCD_ERR_WORKSPACE;
+  }
+  void* scratch = nullptr;
+  rc = noalloc_scratch(&scratch);
+  if (rc) return rc;
+  // Nothing in the scratch needs clearing: each call writes every byte it
+  // later reads (per-k constants, then all feature rows including padding)
+  // before reading it.
+  return ewald_build(desc, PYCD_EWALD_FP64_GEMM, d_out, scratch,
+                     kNoAllocScratchBytes, (cudaStream_t)stream, nullptr, nullptr);
+}

@@ -114,6 +114,31 @@ def build_device_array(system, alpha, r_cut, k_cut, precision="auto",
         pmiv = system.pairwise_min_image_vector_data
     n = int(system.neighbors.num_system_elements)
     mode = choose_mode(system, pmiv, precision)
+    desc, keep, k_max = make_desc(system, alpha, r_cut, k_cut, pmiv)
+    dev = keep[0].device
+    L = nat.lib()
+    code = nat.EWALD_MODES[mode]
+    ws_bytes = nat.C.c_size_t()
+    nat.check(L.pycd_ewald_workspace_size(nat.C.byref(desc), code,
+                                          nat.C.byref(ws_bytes)))
+    ws = torch.empty(max(1, ws_bytes.value), dtype=torch.uint8, device=dev)
+    if out is None:
+        out = torch.empty((n, n), dtype=torch.float64, device=dev)
+    rms, fms = nat.C.c_float(), nat.C.c_float()
+    nat.check(L.pycd_ewald_build(nat.C.byref(desc), code, out.data_ptr(),
+                                 ws.data_ptr(), ws_bytes.value,
+                                 nat.stream_handle(stream), nat.C.byref(rms),
+                                 nat.C.byref(fms)))
+    info = {"mode": mode, "k_max": k_max, "n_kvec": int(desc.n_kvec),
+            "real_ms": rms.value, "fourier_ms": fms.value}
+    return out, info
+
+
+def make_desc(system, alpha, r_cut, k_cut, pmiv=None):
+    """PycdEwaldDesc for `system` on the current CUDA device.  Returns
+    (desc, tensors the descriptor points into, k_max)."""
+    import torch
+    n = int(system.neighbors.num_system_elements)
     k_max = k_max_for(system, k_cut)
     kv = effective_k_vectors(system.reciprocal_lattice_matrix, k_max, k_cut)
     dev = torch.device("cuda", torch.cuda.current_device())
@@ -140,19 +165,5 @@ def build_device_array(system, alpha, r_cut, k_cut, precision="auto",
     desc.r_cut = float(r_cut)
     desc.volume = float(system.system_volume)
     desc.dielectric = float(system.material.dielectric_constant)
-    L = nat.lib()
-    code = nat.EWALD_MODES[mode]
-    ws_bytes = nat.C.c_size_t()
-    nat.check(L.pycd_ewald_workspace_size(nat.C.byref(desc), code,
-                                          nat.C.byref(ws_bytes)))
-    ws = torch.empty(max(1, ws_bytes.value), dtype=torch.uint8, device=dev)
-    if out is None:
-        out = torch.empty((n, n), dtype=torch.float64, device=dev)
-    rms, fms = nat.C.c_float(), nat.C.c_float()
-    nat.check(L.pycd_ewald_build(nat.C.byref(desc), code, out.data_ptr(),
-                                 ws.data_ptr(), ws_bytes.value,
-                                 nat.stream_handle(stream), nat.C.byref(rms),
-                                 nat.C.byref(fms)))
-    info = {"mode": mode, "k_max": k_max, "n_kvec": int(len(kv)),
-            "real_ms": rms.value, "fourier_ms": fms.value}
-    return out, info
+    keep = [cart, d_kv] + ([d_pmiv] if d_pmiv is not None else [])
+    return desc, keep, k_max
