@@ -258,8 +258,11 @@ typedef struct PycdKmcLaunch {
  * table in d_workspace); each trajectory runs on systems[d_sys_index[t]].
  * The same device step function serves the one-trajectory (plain) form and
  * the batched form, so their event streams are identical.
- * Workspace: pycd_kmc_workspace_size(n_systems).                            */
-PYCD_API int pycd_kmc_workspace_size(int32_t n_systems, size_t* bytes);
+ * Workspace: pycd_kmc_workspace_size(systems, n_systems) bytes; it holds the
+ * device copy of the descriptors and per-slot rate coefficients derived from
+ * lam, V_ab, the field shift, kT and vn.                                    */
+PYCD_API int pycd_kmc_workspace_size(const PycdKmcSystem* systems,
+                                     int32_t n_systems, size_t* bytes);
 
 PYCD_API int pycd_kmc_advance(const PycdKmcSystem* systems, int32_t n_systems,
                      const PycdKmcState* state, const PycdKmcOutputs* out,
@@ -288,6 +291,11 @@ PYCD_API int pycd_kmc_advance_uploaded(int32_t n_systems, const PycdKmcState* st
  * `traj`.  d_out is a device pointer.                                      */
 PYCD_API int pycd_philox_uniforms(uint64_t seed, uint64_t traj, int64_t step0,
                          int64_t n_steps, double* d_out, void* stream);
+
+/* Self-check of the kernels' exp(): d_ours[i] = the KMC kernels' exp(d_x[i]),
+ * d_cuda[i] = CUDA's exp(d_x[i]).  No counterpart in the reference.        */
+PYCD_API int pycd_debug_exp(const double* d_x, int64_t n, double* d_ours,
+                            double* d_cuda, void* stream);
 
 #ifdef __cplusplus
 }

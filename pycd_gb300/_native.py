@@ -108,7 +108,7 @@ _PROTOS = {
     "pycd_ewald_build_noalloc": (C.c_int, [P(EwaldDesc), C.c_void_p, C.c_void_p]),
     "pycd_potential_gemv": (C.c_int, [C.c_void_p, C.c_int64, C.c_void_p,
                                       C.c_void_p, C.c_void_p, C.c_void_p]),
-    "pycd_kmc_workspace_size": (C.c_int, [C.c_int32, P(C.c_size_t)]),
+    "pycd_kmc_workspace_size": (C.c_int, [P(KmcSystem), C.c_int32, P(C.c_size_t)]),
     "pycd_kmc_advance": (C.c_int, [P(KmcSystem), C.c_int32, P(KmcState),
                                    P(KmcOutputs), P(KmcRng), C.c_int64,
                                    P(KmcLaunch), C.c_void_p, C.c_size_t,
@@ -123,6 +123,8 @@ _PROTOS = {
                                             C.c_void_p]),
     "pycd_philox_uniforms": (C.c_int, [C.c_uint64, C.c_uint64, C.c_int64,
                                        C.c_int64, C.c_void_p, C.c_void_p]),
+    "pycd_debug_exp": (C.c_int, [C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p,
+                                 C.c_void_p]),
 }
 
 _lib = None

@@ -8,6 +8,7 @@
 #include <vector>
 
 #include "common.cuh"
+#include "kmc_internal.cuh"
 
 namespace pycd {
 
@@ -38,26 +39,12 @@ int ewald_build(const PycdEwaldDesc* d, int mode, double* out, void* ws,
 int potential_gemv(const double* A, int64_t n, const double* q, double* phi,
                    double* energy, cudaStream_t s);
 
-struct KmcArgs {
-  const PycdKmcSystem* systems;
-  int32_t n_systems;
-  PycdKmcState st;
-  PycdKmcOutputs out;
-  PycdKmcRng rng;
-  int64_t max_steps;
-};
-int kmc_launch(const KmcArgs& a, int max_np, int max_nc,
-               const PycdKmcLaunch* launch, cudaStream_t s);
-int philox_launch(uint64_t seed, uint64_t traj, int64_t step0, int64_t n,
-                  double* out, cudaStream_t s);
-int kmc_preload();
-
 }  // namespace pycd
 
 using namespace pycd;
 
-// Header of the device-resident system table kept in the KMC workspace: the
-// shape maxima the launch heuristic needs, then the descriptor array.
+// KMC workspace layout: a 256-byte header with the shape maxima, the device
+// descriptors (KmcSysDev), then one (c1, c0) coefficient array per system.
 struct KmcTableHeader {
   int32_t n_systems;
   int32_t max_np;
@@ -66,8 +53,18 @@ struct KmcTableHeader {
 };
 static_assert(sizeof(KmcTableHeader) == 16, "header layout");
 
-static size_t kmc_ws_bytes(int32_t n_systems) {
-  return 256 + sizeof(PycdKmcSystem) * (size_t)(n_systems > 0 ? n_systems : 1);
+static size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
+
+static size_t kmc_table_bytes(int32_t n_systems) {
+  return 256 + align256(sizeof(KmcSysDev) * (size_t)(n_systems > 0 ? n_systems : 1));
+}
+
+static size_t kmc_ws_bytes(const PycdKmcSystem* systems, int32_t n_systems) {
+  size_t b = kmc_table_bytes(n_systems);
+  for (int i = 0; i < n_systems; ++i)
+    b += align256(sizeof(double2) * (size_t)systems[i].n_sites *
+                  (size_t)systems[i].n_slots);
+  return b;
 }
 
 extern "C" {
@@ -170,10 +167,11 @@ int pycd_potential_gemv(const double* d_A, int64_t n_sites, const double* d_q,
                         (cudaStream_t)stream);
 }
 
-int pycd_kmc_workspace_size(int32_t n_systems, size_t* bytes) {
+int pycd_kmc_workspace_size(const PycdKmcSystem* systems, int32_t n_systems,
+                            size_t* bytes) {
   clear_error();
-  PYCD_REQUIRE(bytes && n_systems > 0, "bad arguments");
-  *bytes = kmc_ws_bytes(n_systems);
+  PYCD_REQUIRE(bytes && systems && n_systems > 0, "bad arguments");
+  *bytes = kmc_ws_bytes(systems, n_systems);
   return PYCD_OK;
 }
 
@@ -227,18 +225,32 @@ int pycd_kmc_upload_systems(const PycdKmcSystem* systems, int32_t n_systems,
   int np = 0, nc = 0;
   int rc = validate_systems(systems, n_systems, 32, &np, &nc);
   if (rc) return rc;
-  if (!d_workspace || workspace_bytes < kmc_ws_bytes(n_systems)) {
-    set_error("KMC workspace too small (%zu < %zu)", workspace_bytes,
-              kmc_ws_bytes(n_systems));
+  const size_t need = kmc_ws_bytes(systems, n_systems);
+  if (!d_workspace || workspace_bytes < need) {
+    set_error("KMC workspace too small (%zu < %zu)", workspace_bytes, need);
     return PYCD_ERR_WORKSPACE;
   }
-  std::vector<char> host(kmc_ws_bytes(n_systems), 0);
+  const size_t table = kmc_table_bytes(n_systems);
+  std::vector<char> host(table, 0);
   KmcTableHeader h{n_systems, np, nc, 0};
   memcpy(host.data(), &h, sizeof(h));
-  memcpy(host.data() + 256, systems, sizeof(PycdKmcSystem) * n_systems);
+  KmcSysDev* dev = (KmcSysDev*)(host.data() + 256);
+  char* coef_base = (char*)d_workspace + table;
+  size_t off = 0;
+  for (int i = 0; i < n_systems; ++i) {
+    dev[i].pub = systems[i];
+    dev[i].coef = (const double2*)(coef_base + off);
+    dev[i].pad = 0;
+    off += align256(sizeof(double2) * (size_t)systems[i].n_sites *
+                    (size_t)systems[i].n_slots);
+  }
   cudaStream_t s = (cudaStream_t)stream;
   PYCD_CUDA(cudaMemcpyAsync(d_workspace, host.data(), host.size(),
                             cudaMemcpyHostToDevice, s));
+  for (int i = 0; i < n_systems; ++i) {
+    rc = kmc_coef_launch(systems[i], (double2*)dev[i].coef, s);
+    if (rc) return rc;
+  }
   PYCD_CUDA(cudaStreamSynchronize(s));
   rc = kmc_preload();
   if (rc) return rc;
@@ -258,7 +270,7 @@ int pycd_kmc_advance_uploaded(int32_t n_systems, const PycdKmcState* state,
   int rc = validate_state(state, out, rng);
   if (rc) return rc;
   PYCD_REQUIRE(max_steps >= 0, "max_steps < 0");
-  if (!d_workspace || workspace_bytes < kmc_ws_bytes(n_systems)) {
+  if (!d_workspace || workspace_bytes < kmc_table_bytes(n_systems)) {
     set_error("KMC workspace too small");
     return PYCD_ERR_WORKSPACE;
   }
@@ -267,7 +279,7 @@ int pycd_kmc_advance_uploaded(int32_t n_systems, const PycdKmcState* state,
   PYCD_REQUIRE(launch->max_carriers <= state->max_carriers,
                "carriers exceed the state stride");
   KmcArgs a;
-  a.systems = (const PycdKmcSystem*)((const char*)d_workspace + 256);
+  a.systems = (const KmcSysDev*)((const char*)d_workspace + 256);
   a.n_systems = n_systems;
   a.st = *state;
   a.out = *out;
@@ -303,6 +315,13 @@ int pycd_philox_uniforms(uint64_t seed, uint64_t traj, int64_t step0,
   clear_error();
   PYCD_REQUIRE(d_out && n_steps >= 0 && step0 >= 0, "bad arguments");
   return philox_launch(seed, traj, step0, n_steps, d_out, (cudaStream_t)stream);
+}
+
+int pycd_debug_exp(const double* d_x, int64_t n, double* d_ours, double* d_cuda,
+                   void* stream) {
+  clear_error();
+  PYCD_REQUIRE(d_x && d_ours && d_cuda && n >= 0, "bad arguments");
+  return exp_probe_launch(d_x, n, d_ours, d_cuda, (cudaStream_t)stream);
 }
 
 }  // extern "C"

@@ -3,43 +3,96 @@
 // Mapping.  A trajectory is owned by a group of G lanes of one warp
 // (G = 1..32, a power of two); a warp holds 32/G trajectories.  Process p of
 // a trajectory is (carrier c = p / S, slot s = p % S), the reference's order
-// (core.py:1946-1987).  Lane g of the group owns processes p = g + j*G,
-// j < MAXP, and carrier g (its site and its displacement accumulator).
-// Every trajectory runs the same device step, so a trajectory advanced alone
-// (the plain form) and inside a batch of thousands produce identical events.
+// (core.py:1946-1987).  Lane g owns the contiguous processes
+// p = g*MAXP + j (j < MAXP) and carrier g (its site, its displacement
+// accumulator and its path-row values); G*MAXP >= n_carriers * S.
 //
-// Arithmetic that decides events follows the reference's expression order
-// in FP64 with no contraction (__dmul_rn / __dadd_rn / __ddiv_rn):
-//   dE0   = 2 q (term01 + term02) + (E_rel[n] - E_rel[o])      core.py:2004-2026
-//   dG    = (((lam + dE0)^2 / (4 lam)) - V_ab) - shift          core.py:2045-2046
-//   k     = vn * exp(-dG / kT)                                  core.py:2047
-//   k_tot = k_0 + k_1 + ... (left to right)                     core.py:2796
-//   cum_i = sum_{j<=i} (k_j / k_tot) (left to right)            core.py:2797
-//   idx   = first i with cum_i > u1                             core.py:2800
-//   t    -= log(u2) / k_tot                                     core.py:2803
-// term01 = np.dot(q, A[n]-A[o]) is evaluated as (phi_bg[n] - phi_bg[o]) plus
-// the carriers' part sum_c' q (A[n,occ_c'] - A[o,occ_c']), phi_bg = A q_fixed.
+// Arithmetic.  GB300's FP64 pipe issues ~2 DFMA/clk/SM, and FP64 is the
+// bound of this kernel, so the step is written to spend few FP64
+// instructions while keeping every result within a few ulp of the
+// reference's expression:
+//   dE0   = 2q (term01 + term02) + (E_rel[n] - E_rel[o])      core.py:2004-2026
+//           term01 = (phi_bg[n] - phi_bg[o]) + q (sum_c' A[n,occ_c'] - sum_c' A[o,occ_c'])
+//           term02 = q (A[o,o] - A[o,n])
+//   rate  = exp(c1 (lam + dE0)^2 + c0),  c1 = -1/(4 lam kT),
+//           c0 = (V_ab + shift)/kT + ln vn   (= vn exp(-dG/kT), core.py:2045-2047)
+//   k_tot and every cumulative rate are sums over a fixed balanced binary
+//   tree over the process index (zero-padded to a power of two), so the
+//   event stream does not depend on G or MAXP: a trajectory advanced alone
+//   (the plain form) and inside a batch of thousands give identical events.
+//   The event is the first process whose cumulative rate exceeds u1 k_tot
+//   (core.py:2796-2800); t -= log(u2) / k_tot (core.py:2802-2803).
+// exp() is Tang's table-driven method (ACM TOMS 15(2), 1989): reduction by
+// ln2/32 with a 32-entry table of 2^(j/32) in two parts and a degree-6
+// polynomial on |r| <= ln2/64.
 #include <cuda_runtime.h>
 #include <math.h>
 #include <stdint.h>
 
 #include "common.cuh"
+#include "kmc_internal.cuh"
 
 namespace pycd {
-
-struct KmcArgs {
-  const PycdKmcSystem* systems;  // device table
-  int32_t n_systems;
-  PycdKmcState st;
-  PycdKmcOutputs out;
-  PycdKmcRng rng;
-  int64_t max_steps;
-};
 
 __device__ __forceinline__ double dsub(double a, double b) { return __dsub_rn(a, b); }
 __device__ __forceinline__ double dadd(double a, double b) { return __dadd_rn(a, b); }
 __device__ __forceinline__ double dmul(double a, double b) { return __dmul_rn(a, b); }
 __device__ __forceinline__ double ddiv(double a, double b) { return __ddiv_rn(a, b); }
+
+// ---------------------------------------------------------------------------
+// exp(x), Tang's method
+// ---------------------------------------------------------------------------
+__device__ const unsigned long long kExp2Hi[32] = {
+    0x3ff0000000000000ULL, 0x3ff059b0d3158574ULL, 0x3ff0b5586cf9890fULL, 0x3ff11301d0125b51ULL,
+    0x3ff172b83c7d517bULL, 0x3ff1d4873168b9aaULL, 0x3ff2387a6e756238ULL, 0x3ff29e9df51fdee1ULL,
+    0x3ff306fe0a31b715ULL, 0x3ff371a7373aa9cbULL, 0x3ff3dea64c123422ULL, 0x3ff44e086061892dULL,
+    0x3ff4bfdad5362a27ULL, 0x3ff5342b569d4f82ULL, 0x3ff5ab07dd485429ULL, 0x3ff6247eb03a5585ULL,
+    0x3ff6a09e667f3bcdULL, 0x3ff71f75e8ec5f74ULL, 0x3ff7a11473eb0187ULL, 0x3ff82589994cce13ULL,
+    0x3ff8ace5422aa0dbULL, 0x3ff93737b0cdc5e5ULL, 0x3ff9c49182a3f090ULL, 0x3ffa5503b23e255dULL,
+    0x3ffae89f995ad3adULL, 0x3ffb7f76f2fb5e47ULL, 0x3ffc199bdd85529cULL, 0x3ffcb720dcef9069ULL,
+    0x3ffd5818dcfba487ULL, 0x3ffdfc97337b9b5fULL, 0x3ffea4afa2a490daULL, 0x3fff50765b6e4540ULL};
+__device__ const unsigned long long kExp2Lo[32] = {
+    0x0000000000000000ULL, 0x3c8d73e2a475b465ULL, 0x3c98a62e4adc610bULL, 0xbc96c51039449b3aULL,
+    0xbc819041b9d78a76ULL, 0x3c9e016e00a2643cULL, 0x3c99b07eb6c70573ULL, 0x3c8612e8afad1255ULL,
+    0x3c86f46ad23182e4ULL, 0xbc963aeabf42eae2ULL, 0x3c8ada0911f09ebcULL, 0x3c489b7a04ef80d0ULL,
+    0x3c7d4397afec42e2ULL, 0xbc807abe1db13cadULL, 0x3c96324c054647adULL, 0xbc9383c17e40b497ULL,
+    0xbc9bdd3413b26456ULL, 0xbc816e4786887a99ULL, 0xbc841577ee04992fULL, 0xbc9d4c1dd41532d8ULL,
+    0x3c96e9f156864b27ULL, 0xbc675fc781b57ebcULL, 0x3c7c7c46b071f2beULL, 0xbc9d2f6edb8d41e1ULL,
+    0x3c97a1cd345dcc81ULL, 0xbc75584f7e54ac3bULL, 0x3c811065895048ddULL, 0x3c7503cbd1e949dbULL,
+    0x3c82ed02d75b3707ULL, 0xbc91a5cd4f184b5cULL, 0xbc9e9c23179c2893ULL, 0x3c99d3e12dd8a18bULL};
+
+__device__ __forceinline__ double exp_tang(double x) {
+  const double kInvL = 46.16624130844683;        // 32 / ln 2
+  const double kL1 = 0.02166084939249829;        // ln2/32, leading part
+  const double kL2 = 7.247021293269686e-19;      // ln2/32 - kL1
+  const double kShift = 6755399441055744.0;      // 1.5 * 2^52
+  if (!(x < 709.782712893384)) return (x != x) ? x : INFINITY;
+  if (x < -745.1332191019412) return 0.0;
+  // N = round(x * 32/ln2) in the low word of t
+  const double t = fma(x, kInvL, kShift);
+  const int n = __double2loint(t);
+  const double nd = dsub(t, kShift);
+  const double r = fma(-nd, kL2, fma(-nd, kL1, x));
+  const int j = n & 31;
+  const int m = (n - j) >> 5;
+  // p = expm1(r) on |r| <= ln2/64, Taylor to degree 6
+  double p = fma(r, 1.0 / 720.0, 1.0 / 120.0);
+  p = fma(p, r, 1.0 / 24.0);
+  p = fma(p, r, 1.0 / 6.0);
+  p = fma(p, r, 0.5);
+  p = fma(dmul(p, r), r, r);
+  const double shi = __longlong_as_double((long long)kExp2Hi[j]);
+  const double slo = __longlong_as_double((long long)kExp2Lo[j]);
+  // 2^(j/32) (1 + p) = shi + (slo + (shi + slo) p)
+  const double v = dadd(shi, fma(dadd(shi, slo), p, slo));
+  // scale by 2^m through the exponent field (two steps below the normal range)
+  if (m >= -1021) {
+    return __hiloint2double(__double2hiint(v) + (m << 20), __double2loint(v));
+  }
+  const double v2 = __hiloint2double(__double2hiint(v) + ((m + 64) << 20),
+                                     __double2loint(v));
+  return dmul(v2, 5.421010862427522e-20);  // 2^-64
+}
 
 template <int G>
 __device__ __forceinline__ double gshfl(unsigned mask, double v, int src) {
@@ -49,6 +102,20 @@ template <int G>
 __device__ __forceinline__ int gshfl(unsigned mask, int v, int src) {
   return __shfl_sync(mask, v, src, G);
 }
+
+// Balanced-tree sums over the MAXP register values: node sums of the
+// subtree rooted at each internal node, in heap order (1 = root).
+template <int MAXP>
+struct LocalTree {
+  double node[2 * MAXP];  // node[MAXP + j] = leaf j
+  __device__ __forceinline__ void build(const double* leaf) {
+#pragma unroll
+    for (int j = 0; j < MAXP; ++j) node[MAXP + j] = leaf[j];
+#pragma unroll
+    for (int i = MAXP - 1; i >= 1; --i) node[i] = dadd(node[2 * i], node[2 * i + 1]);
+  }
+  __device__ __forceinline__ double total() const { return node[1]; }
+};
 
 // One group of G lanes advances one trajectory by up to max_steps steps.
 template <int G, int MAXP>
@@ -62,16 +129,19 @@ __device__ void advance_trajectory(const KmcArgs& a, int64_t t, int g,
     if (g == 0) st.d_status[t] = PYCD_TRAJ_BAD_INDEX;
     return;
   }
-  const PycdKmcSystem sy = a.systems[sys_id];
+  const KmcSysDev& sd = a.systems[sys_id];
+  const PycdKmcSystem& sy = sd.pub;
   const int64_t N = sy.n_sites;
   const int S = sy.n_slots;
   const int NC = sy.n_carriers;
   const int NP = NC * S;
   const int MC = st.max_carriers;
   const double q = sy.carrier_charge;
+  const double two_q = dmul(2.0, q);
   const double* __restrict__ A = sy.d_A;
+  const double2* __restrict__ coef = sd.coef;
+  const double dt_grid = sy.time_interval;
 
-  // carrier state owned by lane g (carrier c == g)
   int occ = 0;
   double disp0 = 0.0, disp1 = 0.0, disp2 = 0.0;
   double row0 = 0.0, row1 = 0.0, row2 = 0.0;
@@ -99,134 +169,172 @@ __device__ void advance_trajectory(const KmcArgs& a, int64_t t, int g,
                                             ? a.out.unwrapped_stride
                                             : n_path * row_len)
                     : nullptr;
+  // below t_guard the quotient sim_time / dt cannot reach start_path + 1
+  double t_guard = dmul(dmul((double)(start_path + 1), dt_grid), 1.0 - 0x1p-40);
+
+  // uniforms of steps pre_base + g, prepared G at a time
+  double pre_u1 = 0.0, pre_lu2 = 0.0;
+  int64_t pre_base = -(int64_t)G - 1;
 
   for (int64_t it = 0; it < a.max_steps; ++it) {
     // ---- uniforms (core.py:2799, 2802) --------------------------------
-    double u1, u2;
-    if (ubase) {
-      if (ucur + 2 > a.rng.u_count) { status = PYCD_TRAJ_NEED_UNIFORMS; break; }
-      u1 = ubase[ucur];
-      u2 = ubase[ucur + 1];
-    } else {
-      philox_step_uniforms(a.rng.seed, a.rng.traj_offset + (uint64_t)t,
-                           (uint64_t)step, u1, u2);
+    if (ubase && ucur + 2 > a.rng.u_count) { status = PYCD_TRAJ_NEED_UNIFORMS; break; }
+    const int64_t since = step - pre_base;
+    int k = (int)since;
+    if (since < 0 || since >= G) {
+      pre_base = step;
+      k = 0;
+      double u1, u2;
+      if (ubase) {
+        const int64_t idx = ucur + 2 * (int64_t)g;
+        const bool ok = idx + 2 <= a.rng.u_count;
+        u1 = ok ? ubase[idx] : 0.5;
+        u2 = ok ? ubase[idx + 1] : 0.5;
+      } else {
+        philox_step_uniforms(a.rng.seed, a.rng.traj_offset + (uint64_t)t,
+                             (uint64_t)(step + g), u1, u2);
+      }
+      pre_u1 = u1;
+      pre_lu2 = log(u2);
     }
+    const double u1 = gshfl<G>(gmask, pre_u1, k);
+    const double lu2 = gshfl<G>(gmask, pre_lu2, k);
 
-    // ---- process attributes and rates (core.py:1946-2050) -------------
-    double kp[MAXP], dE[MAXP];
-    int newsite[MAXP], oldsite[MAXP];
+    // ---- process attributes (core.py:1946-1987) ------------------------
+    int oldsite[MAXP], newsite[MAXP];
+    bool fresh[MAXP];
     bool bad = false;
 #pragma unroll
     for (int j = 0; j < MAXP; ++j) {
-      const int p = g + j * G;
-      kp[j] = 0.0; dE[j] = 0.0; newsite[j] = 0; oldsite[j] = 0;
-      // every lane joins the shuffles; lanes past NP discard the result
+      const int p = g * MAXP + j;
       const int c = (p < NP) ? p / S : 0;
       const int o = gshfl<G>(gmask, occ, c);
+      oldsite[j] = o;
+      newsite[j] = o;
+      fresh[j] = (j == 0) || (o != oldsite[j > 0 ? j - 1 : 0]);
       if (p < NP) {
-        const int s = p - c * S;
-        const int n = sy.d_nbr[(int64_t)o * S + s];
-        oldsite[j] = o;
+        const int n = sy.d_nbr[(int64_t)o * S + (p - c * S)];
         newsite[j] = n;
         if (n < 0 || n >= N || o < 0 || o >= N) bad = true;
       }
     }
-    // all lanes of the group agree on `bad` before any gather
-    const unsigned any_bad = __ballot_sync(gmask, bad) & gmask;
-    if (any_bad) { status = PYCD_TRAJ_BAD_INDEX; break; }
+    if (__ballot_sync(gmask, bad) & gmask) { status = PYCD_TRAJ_BAD_INDEX; break; }
 
-    double t01[MAXP];
+    // ---- carriers' row sums: sum_c' A[n, occ_c'] and A[o, occ_c'] -------
+    double sn[MAXP], so[MAXP];
 #pragma unroll
-    for (int j = 0; j < MAXP; ++j) t01[j] = 0.0;
-    // carriers' part of term01, carrier order c' = 0..NC-1
+    for (int j = 0; j < MAXP; ++j) { sn[j] = 0.0; so[j] = 0.0; }
     for (int cc = 0; cc < NC; ++cc) {
       const int sc = gshfl<G>(gmask, occ, cc);
 #pragma unroll
       for (int j = 0; j < MAXP; ++j) {
-        const int p = g + j * G;
-        if (p < NP) {
-          const double an = __ldg(A + (int64_t)newsite[j] * N + sc);
-          const double ao = __ldg(A + (int64_t)oldsite[j] * N + sc);
-          t01[j] = dadd(t01[j], dmul(q, dsub(an, ao)));
+        if (g * MAXP + j < NP) {
+          sn[j] = dadd(sn[j], __ldg(A + (int64_t)newsite[j] * N + sc));
+          if (fresh[j]) so[j] = dadd(so[j], __ldg(A + (int64_t)oldsite[j] * N + sc));
         }
       }
     }
+
+    // ---- rates (core.py:1989-2050) ------------------------------------
+    double kp[MAXP], dE[MAXP];
+    double phio = 0.0, aoo = 0.0, eo = 0.0;
 #pragma unroll
     for (int j = 0; j < MAXP; ++j) {
-      const int p = g + j * G;
+      kp[j] = 0.0;
+      dE[j] = 0.0;
+      const int p = g * MAXP + j;
+      if (j > 0 && !fresh[j]) so[j] = so[j - 1];
       if (p < NP) {
         const int o = oldsite[j], n = newsite[j];
+        if (fresh[j]) {
+          phio = __ldg(sy.d_phi_bg + o);
+          aoo = __ldg(A + (int64_t)o * N + o);
+          eo = __ldg(sy.d_e_rel + o);
+        }
         const int64_t slot = (int64_t)o * S + (p % S);
-        const double term01 =
-            dadd(dsub(__ldg(sy.d_phi_bg + n), __ldg(sy.d_phi_bg + o)), t01[j]);
-        const double term02 =
-            dmul(q, dsub(__ldg(A + (int64_t)o * N + o), __ldg(A + (int64_t)o * N + n)));
-        const double ewald = dmul(dmul(2.0, q), dadd(term01, term02));
-        const double shift = dsub(__ldg(sy.d_e_rel + n), __ldg(sy.d_e_rel + o));
-        const double de0 = dadd(ewald, shift);
-        const double lam = __ldg(sy.d_lam + slot);
-        const double x = dadd(lam, de0);
-        double dg = dsub(ddiv(dmul(x, x), dmul(4.0, lam)), __ldg(sy.d_vab + slot));
-        if (sy.d_field_shift) dg = dsub(dg, __ldg(sy.d_field_shift + slot));
+        const double term01 = dadd(dsub(__ldg(sy.d_phi_bg + n), phio),
+                                   dmul(q, dsub(sn[j], so[j])));
+        const double term02 = dmul(q, dsub(aoo, __ldg(A + (int64_t)o * N + n)));
+        const double de0 = dadd(dmul(two_q, dadd(term01, term02)),
+                                dsub(__ldg(sy.d_e_rel + n), eo));
+        const double x = dadd(__ldg(sy.d_lam + slot), de0);
+        const double2 cf = __ldg(coef + slot);
         dE[j] = de0;
-        kp[j] = dmul(sy.vn, exp(ddiv(-dg, sy.kT)));
+        kp[j] = exp_tang(fma(dmul(x, x), cf.x, cf.y));
       }
     }
 
-    // ---- selection (core.py:2796-2800), left-to-right sums -------------
-    double ktot = 0.0;
+    // ---- selection (core.py:2796-2800) on the balanced tree ------------
+    LocalTree<MAXP> lt;
+    lt.build(kp);
+    // butterfly: lvl[l] = sum of the aligned block of 2^l lanes containing g
+    double lvl[6];
+    lvl[0] = lt.total();
 #pragma unroll
-    for (int j = 0; j < MAXP; ++j) {
-      if (j * G >= NP) break;
-      for (int src = 0; src < G; ++src) {
-        const double v = gshfl<G>(gmask, kp[j], src);
-        if (j * G + src < NP) ktot = dadd(ktot, v);
+    for (int l = 0; (1 << l) < G; ++l) {
+      const double other = __shfl_xor_sync(gmask, lvl[l], 1 << l, G);
+      lvl[l + 1] = dadd(lvl[l], other);
+    }
+    int lg = 0;
+    while ((1 << lg) < G) ++lg;
+    const double ktot = lvl[lg];
+    if (!(ktot > 0.0) || !(ktot < INFINITY)) { status = PYCD_TRAJ_STALLED; break; }
+    const double thr = dmul(u1, ktot);
+    // descend across lanes: block [base, base + 2^(l+1)), left half sum
+    double acc = 0.0;
+    int base = 0;
+#pragma unroll
+    for (int l = 5; l >= 0; --l) {
+      if (l < lg) {
+        const double left = gshfl<G>(gmask, lvl[l], base);
+        const double s = dadd(acc, left);
+        if (!(s > thr)) { acc = s; base += 1 << l; }
       }
     }
-    if (!(ktot > 0.0) || !isfinite(ktot)) { status = PYCD_TRAJ_STALLED; break; }
-    double frac[MAXP];
+    // descend inside lane `base` over its MAXP leaves
+    int node = 1;
 #pragma unroll
-    for (int j = 0; j < MAXP; ++j) frac[j] = ddiv(kp[j], ktot);
-    double cum = 0.0;
-    int sel = -1;
+    for (int l = 0; (MAXP >> (l + 1)) > 0; ++l) {
+      double left = 0.0;
 #pragma unroll
-    for (int j = 0; j < MAXP; ++j) {
-      if (j * G >= NP) break;
-      for (int src = 0; src < G; ++src) {
-        const double v = gshfl<G>(gmask, frac[j], src);
-        const int p = j * G + src;
-        if (p < NP) {
-          cum = dadd(cum, v);
-          if (sel < 0 && cum > u1) sel = p;
-        }
+      for (int i = 1; i < MAXP; ++i) {
+        const double v = gshfl<G>(gmask, lt.node[2 * i], base);
+        if (i == node) left = v;
       }
+      const double s = dadd(acc, left);
+      if (!(s > thr)) { acc = s; node = 2 * node + 1; } else { node = 2 * node; }
     }
-    if (sel < 0) { status = PYCD_TRAJ_NO_EVENT; break; }
+    const int jsel = node - MAXP;
+    const int sel = base * MAXP + jsel;
+    // only a u1 within rounding of 1 can walk into the zero padding
+    if (sel >= NP) { status = PYCD_TRAJ_NO_EVENT; break; }
 
     // ---- residence time (core.py:2802-2804) ---------------------------
-    sim_time = dsub(sim_time, ddiv(log(u2), ktot));
-    const double tq = ddiv(sim_time, sy.time_interval);
-    int64_t end_path = (tq < 9.0e18) ? (int64_t)tq : INT64_MAX;
+    sim_time = dsub(sim_time, ddiv(lu2, ktot));
+    int64_t end_path = start_path - 1;
+    if (sim_time >= t_guard) {
+      const double tq = ddiv(sim_time, dt_grid);
+      end_path = (tq < 9.0e18) ? (int64_t)tq : INT64_MAX;
+    }
 
     // broadcast the selected process' data from its owner lane
-    const int jsel = sel / G, lsel = sel - jsel * G;
     double de_sel = 0.0, k_sel = 0.0;
     int n_sel = 0, o_sel = 0;
 #pragma unroll
     for (int j = 0; j < MAXP; ++j) {
-      const double d = gshfl<G>(gmask, dE[j], lsel);
-      const double kk = gshfl<G>(gmask, kp[j], lsel);
-      const int ns = gshfl<G>(gmask, newsite[j], lsel);
-      const int os = gshfl<G>(gmask, oldsite[j], lsel);
+      const double d = gshfl<G>(gmask, dE[j], base);
+      const double kk = gshfl<G>(gmask, kp[j], base);
+      const int ns = gshfl<G>(gmask, newsite[j], base);
+      const int os = gshfl<G>(gmask, oldsite[j], base);
       if (j == jsel) { de_sel = d; k_sel = kk; n_sel = ns; o_sel = os; }
     }
     const int c_sel = sel / S, s_sel = sel - c_sel * S;
 
-    // delG0 grid rows [start, end) before the clamp (core.py:2807-2809)
+    // delG0 grid rows [start, end) (core.py:2807-2809)
     if (a.out.d_delg0_grid) {
       const int64_t e = end_path < n_path ? end_path : n_path;
-      double* dg = a.out.d_delg0_grid + (int64_t)t * n_path;
-      for (int64_t r = start_path + g; r < e; r += G) dg[r] = de_sel;
+      double* dgr = a.out.d_delg0_grid + (int64_t)t * n_path;
+      for (int64_t r = start_path + g; r < e; r += G) dgr[r] = de_sel;
     }
 
     // ---- state update (core.py:2810-2830) -----------------------------
@@ -275,6 +383,7 @@ __device__ void advance_trajectory(const KmcArgs& a, int64_t t, int g,
         for (int64_t r = start_path + g; r < end_path; r += G) eg[r] = energy;
       }
       start_path = end_path;
+      t_guard = dmul(dmul((double)(start_path + 1), dt_grid), 1.0 - 0x1p-40);
     }
     if (end_path >= n_path) { status = PYCD_TRAJ_DONE; break; }
   }
@@ -307,11 +416,31 @@ __global__ void __launch_bounds__(256) kmc_advance_kernel(KmcArgs a) {
   const int64_t groups_per_warp = 32 / G;
   const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int64_t n_warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  // persistent grid-stride loop over trajectories
   for (int64_t t = warp * groups_per_warp + sub; t < a.st.n_traj;
        t += n_warps * groups_per_warp) {
     advance_trajectory<G, MAXP>(a, t, g, gmask);
   }
+}
+
+// Per-slot exponent coefficients: c1 = -1/(4 lam kT), c0 = (V + shift)/kT + ln vn.
+__global__ void kmc_coef_kernel(const double* __restrict__ lam,
+                                const double* __restrict__ vab,
+                                const double* __restrict__ shift, int64_t n,
+                                double kT, double vn, double2* __restrict__ coef) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double l = lam[i];
+  const double v = vab[i] + (shift ? shift[i] : 0.0);
+  coef[i] = make_double2(-1.0 / (4.0 * l * kT), v / kT + log(vn));
+}
+
+__global__ void exp_probe_kernel(const double* __restrict__ x, int64_t n,
+                                 double* __restrict__ ours,
+                                 double* __restrict__ ref) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  ours[i] = exp_tang(x[i]);
+  ref[i] = exp(x[i]);
 }
 
 __global__ void philox_uniforms_kernel(uint64_t seed, uint64_t traj,
@@ -341,21 +470,24 @@ static cudaError_t launch_g(const KmcArgs& a, int warps_per_block, int blocks,
   return cudaGetLastError();
 }
 
+#define PYCD_KMC_SHAPES(X)                                                   \
+  X(1, 1) X(2, 1) X(4, 1) X(8, 1) X(16, 1) X(32, 1) X(2, 2) X(4, 2) X(8, 2)  \
+  X(16, 2) X(32, 2) X(4, 4) X(8, 4) X(16, 4) X(32, 4) X(4, 8) X(8, 8)        \
+  X(16, 8) X(32, 8)
+
 int kmc_launch(const KmcArgs& a, int max_np, int max_nc,
                const PycdKmcLaunch* launch, cudaStream_t s) {
   int G = launch && launch->lanes_per_traj ? launch->lanes_per_traj : 0;
-  if (G == 0) G = pow2_at_least(max_np < 32 ? max_np : 32);
+  if (G == 0) G = pow2_at_least(max_np < 16 ? max_np : 16);
   if (G < max_nc) G = pow2_at_least(max_nc);
   PYCD_REQUIRE(G >= 1 && G <= 32 && (G & (G - 1)) == 0,
                "lanes_per_traj must be a power of two in [1, 32] (got %d)", G);
   PYCD_REQUIRE(max_nc <= G, "carriers per trajectory (%d) exceed lanes (%d)",
                max_nc, G);
-  const int maxp_needed = (max_np + G - 1) / G;
-  PYCD_REQUIRE(maxp_needed <= 8,
-               "processes per trajectory (%d) exceed 8 per lane at G=%d",
-               max_np, G);
-  const int MAXP = maxp_needed <= 1 ? 1 : maxp_needed <= 2 ? 2
-                   : maxp_needed <= 4 ? 4 : 8;
+  const int need = (max_np + G - 1) / G;
+  const int MAXP = need <= 1 ? 1 : need <= 2 ? 2 : need <= 4 ? 4 : need <= 8 ? 8 : 16;
+  PYCD_REQUIRE(MAXP <= 8, "processes per trajectory (%d) exceed 8 per lane at "
+               "%d lanes", max_np, G);
   int wpb = launch && launch->warps_per_block ? launch->warps_per_block : 4;
   PYCD_REQUIRE(wpb >= 1 && wpb <= 8, "warps_per_block must be in [1, 8]");
   const int64_t tpw = 32 / G;
@@ -363,42 +495,48 @@ int kmc_launch(const KmcArgs& a, int max_np, int max_nc,
   int blocks = launch && launch->blocks ? launch->blocks
                                         : (int)((warps_needed + wpb - 1) / wpb);
   if (blocks < 1) blocks = 1;
-  cudaError_t e = cudaSuccess;
-  if (MAXP == 1) {
-    switch (G) {
-      case 1: e = launch_g<1, 1>(a, wpb, blocks, s); break;
-      case 2: e = launch_g<2, 1>(a, wpb, blocks, s); break;
-      case 4: e = launch_g<4, 1>(a, wpb, blocks, s); break;
-      case 8: e = launch_g<8, 1>(a, wpb, blocks, s); break;
-      case 16: e = launch_g<16, 1>(a, wpb, blocks, s); break;
-      case 32: e = launch_g<32, 1>(a, wpb, blocks, s); break;
-    }
-  } else {
-    PYCD_REQUIRE(G == 32, "more than one process per lane needs 32 lanes");
-    switch (MAXP) {
-      case 2: e = launch_g<32, 2>(a, wpb, blocks, s); break;
-      case 4: e = launch_g<32, 4>(a, wpb, blocks, s); break;
-      case 8: e = launch_g<32, 8>(a, wpb, blocks, s); break;
-    }
+  cudaError_t e = cudaErrorInvalidConfiguration;
+  bool found = false;
+#define PYCD_KMC_CASE(g_, m_)                                                \
+  if (!found && G == g_ && MAXP == m_) {                                     \
+    e = launch_g<g_, m_>(a, wpb, blocks, s);                                 \
+    found = true;                                                            \
   }
+  PYCD_KMC_SHAPES(PYCD_KMC_CASE)
+#undef PYCD_KMC_CASE
+  PYCD_REQUIRE(found, "no kernel instance for %d lanes x %d processes per lane",
+               G, MAXP);
   if (e != cudaSuccess) return cuda_fail(e, "kmc_advance_kernel launch", __FILE__, __LINE__);
   return PYCD_OK;
 }
 
-// Load every kernel instance now, so that a later launch inside CUDA-graph
-// capture never triggers lazy module loading.
 int kmc_preload() {
   cudaFuncAttributes fa;
-  const void* fns[] = {
-      (const void*)kmc_advance_kernel<1, 1>, (const void*)kmc_advance_kernel<2, 1>,
-      (const void*)kmc_advance_kernel<4, 1>, (const void*)kmc_advance_kernel<8, 1>,
-      (const void*)kmc_advance_kernel<16, 1>, (const void*)kmc_advance_kernel<32, 1>,
-      (const void*)kmc_advance_kernel<32, 2>, (const void*)kmc_advance_kernel<32, 4>,
-      (const void*)kmc_advance_kernel<32, 8>};
-  for (const void* f : fns) {
-    cudaError_t e = cudaFuncGetAttributes(&fa, f);
-    if (e != cudaSuccess) return cuda_fail(e, "cudaFuncGetAttributes", __FILE__, __LINE__);
-  }
+  cudaError_t e = cudaSuccess;
+#define PYCD_KMC_LOAD(g_, m_)                                                \
+  if (e == cudaSuccess)                                                      \
+    e = cudaFuncGetAttributes(&fa, (const void*)kmc_advance_kernel<g_, m_>);
+  PYCD_KMC_SHAPES(PYCD_KMC_LOAD)
+#undef PYCD_KMC_LOAD
+  if (e != cudaSuccess) return cuda_fail(e, "cudaFuncGetAttributes", __FILE__, __LINE__);
+  return PYCD_OK;
+}
+
+int kmc_coef_launch(const PycdKmcSystem& s, double2* coef, cudaStream_t st) {
+  const int64_t n = s.n_sites * (int64_t)s.n_slots;
+  kmc_coef_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(
+      s.d_lam, s.d_vab, s.d_field_shift, n, s.kT, s.vn, coef);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(e, "kmc_coef_kernel", __FILE__, __LINE__);
+  return PYCD_OK;
+}
+
+int exp_probe_launch(const double* x, int64_t n, double* ours, double* ref,
+                     cudaStream_t s) {
+  if (n <= 0) return PYCD_OK;
+  exp_probe_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(x, n, ours, ref);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(e, "exp_probe_kernel", __FILE__, __LINE__);
   return PYCD_OK;
 }
 

@@ -1,0 +1,37 @@
+// Internal KMC types shared by kmc.cu and capi.cu.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "pycd_gb300.h"
+
+namespace pycd {
+
+// Device copy of a system descriptor plus the library-derived per-slot
+// exponent coefficients (c1, c0) kept in the KMC workspace.
+struct KmcSysDev {
+  PycdKmcSystem pub;
+  const double2* coef;
+  int64_t pad;
+};
+
+struct KmcArgs {
+  const KmcSysDev* systems;  // device table
+  int32_t n_systems;
+  PycdKmcState st;
+  PycdKmcOutputs out;
+  PycdKmcRng rng;
+  int64_t max_steps;
+};
+
+int kmc_launch(const KmcArgs& a, int max_np, int max_nc,
+               const PycdKmcLaunch* launch, cudaStream_t s);
+int kmc_preload();
+int kmc_coef_launch(const PycdKmcSystem& s, double2* coef, cudaStream_t st);
+int exp_probe_launch(const double* x, int64_t n, double* ours, double* ref,
+                     cudaStream_t s);
+int philox_launch(uint64_t seed, uint64_t traj, int64_t step0, int64_t n,
+                  double* out, cudaStream_t s);
+
+}  // namespace pycd

@@ -179,7 +179,7 @@ class KmcEngine(object):
         self._descs = (nat.KmcSystem * len(self.tables))(
             *[t.descriptor() for t in self.tables])
         nbytes = C.c_size_t()
-        nat.check(nat.lib().pycd_kmc_workspace_size(len(self.tables),
+        nat.check(nat.lib().pycd_kmc_workspace_size(self._descs, len(self.tables),
                                                     C.byref(nbytes)))
         self.workspace = torch.empty(nbytes.value, dtype=torch.uint8,
                                      device=_dev())

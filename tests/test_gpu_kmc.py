@@ -193,3 +193,55 @@ def test_out_of_range_neighbour_stops_with_bad_index(cuda_ready):
     st = batch.status.cpu().tolist()
     assert st[0] == nat.TRAJ_BAD_INDEX
     assert st[1] in (nat.TRAJ_RUNNING, nat.TRAJ_BAD_INDEX)
+
+
+def _ulp_diff(a, b):
+    ia = a.view(np.int64)
+    ib = b.view(np.int64)
+    return np.abs(ia - ib)
+
+
+def test_kernel_exp_within_ulps_of_cuda_and_libm(cuda_ready):
+    """The kernels' table-driven exp against CUDA's exp and NumPy's exp on
+    the range the rates use and across the whole finite range."""
+    import torch
+    rng = np.random.default_rng(3)
+    x = np.concatenate([rng.uniform(-80.0, 40.0, 400000),
+                        rng.uniform(-745.0, 709.0, 200000),
+                        np.array([0.0, -0.0, 1e-300, -1e-300, 709.78, -708.4, -744.9,
+                                  -745.2, 709.8, 1.0, -1.0])])
+    xd = torch.as_tensor(x).cuda()
+    ours = torch.empty_like(xd)
+    ref = torch.empty_like(xd)
+    nat.check(nat.lib().pycd_debug_exp(xd.data_ptr(), len(x), ours.data_ptr(),
+                                       ref.data_ptr(), nat.stream_handle()))
+    torch.cuda.synchronize()
+    o, r, h = ours.cpu().numpy(), ref.cpu().numpy(), np.exp(x)
+    normal = np.isfinite(h) & (h > 2.3e-308)
+    assert _ulp_diff(o[normal], r[normal]).max() <= 2
+    assert _ulp_diff(o[normal], h[normal]).max() <= 2
+    sub = (h > 0) & (h <= 2.3e-308)
+    assert np.abs(o[sub] - h[sub]).max() <= 2 * 4.9e-324 or not sub.any()
+    assert np.isinf(o[x >= 709.8]).all() and (o[x <= -745.2] == 0).all()
+
+
+def test_event_stream_independent_of_launch_shape(cuda_ready):
+    """Cumulative rates are balanced-tree sums over the process index, so
+    the lanes-per-trajectory choice must not change any event or time."""
+    import torch
+    sysm, tables, run, cfg, arr = _corundum3600()
+    T, n, seed = 64, 3000, 777
+    rng = np.random.default_rng(5)
+    occ = np.stack([rng.choice(3600, size=4, replace=False) for _ in range(T)])
+    results = []
+    for lanes in (4, 8, 16, 32):
+        eng = KmcEngine(tables, launch={"lanes_per_traj": lanes})
+        b = KmcBatch(occ, step_capacity=n)
+        eng.advance(b, n, eng.rng_struct(seed=seed))
+        torch.cuda.synchronize()
+        results.append((b.step_proc.cpu().numpy(), b.step_time.cpu().numpy(),
+                        b.occ.cpu().numpy()))
+    for r in results[1:]:
+        assert np.array_equal(r[0], results[0][0])
+        assert np.array_equal(r[1], results[0][1])
+        assert np.array_equal(r[2], results[0][2])
