@@ -237,8 +237,111 @@ def cpu_baseline_1core(system, run, dopants, occ, seconds=10.0):
                       "of the reference loop"}
 
 
+# monoclinic supercells and the k_cut (1/A) that keeps K = 4,096 / 8,192 / 16,384
+# half-space k-vectors with k^2 < k_cut^2
+EWALD_SIZES = {8192: ((16, 16, 8), (0.9164, 1.1515, 1.4516)),
+               16384: ((16, 16, 16), (0.7244, 0.9156, 1.1525)),
+               32768: ((16, 16, 32), (0.5765, 0.7257, 0.9150))}
+
+
+def cpu_fourier_ns_per_entry_k(system, rows=48, n_k=24):
+    """The reference's pot_k_ewald arithmetic (oracle) on a row and k subset:
+    seconds per (array entry x k-vector), to extrapolate a full build."""
+    from oracle import ewald_oracle as eo
+    coords = system.neighbors.bulk_sites.cell_coordinates
+    n = len(coords)
+    idx = np.arange(rows)
+    d = coords[None, :, :] - coords[idx, None, :]
+    pmiv = system.neighbors.apply_minimum_image_convention_vectorized(
+        d.reshape(-1, 3)).reshape(rows, n, 3)
+    kv = eo.effective_k_vectors(eo.k_max_for(system.k_cut,
+                                             system.reciprocal_lattice_matrix))
+    kv = kv[:n_k]
+    out = np.zeros((rows, n))
+    t0 = time.perf_counter()
+    for v in kv:
+        k = np.dot(v, system.reciprocal_lattice_matrix)
+        k2 = np.dot(k, k)
+        out += ((2 * np.pi) / system.system_volume * np.exp(-k2 / (4 * system.alpha))
+                * np.cos(np.tensordot(pmiv, k, axes=([2], [0]))) / k2)
+    dt = time.perf_counter() - t0
+    return dt / (rows * n * len(kv))
+
+
+def ewald_split_bench(args):
+    """Split-precision (BF16x3 / TF32x3 tcgen05) vs FP64 GPU Ewald build on
+    the monoclinic supercells; one JSON line per (N, K)."""
+    import torch
+    from pycd_gb300 import _native as nat
+    from pycd_gb300 import constants as K
+    from pycd_gb300 import workloads as wl
+    torch.cuda.set_device(0)
+    nat.require_device()
+    peaks_file = ROOT / "MEASURED_PEAKS.json"
+    bf16_peak = json.loads(peaks_file.read_text())["bf16_tflops"] if peaks_file.exists() else 1900.0
+    sizes = [int(s) for s in args.sizes.split(",")] if args.sizes else sorted(EWALD_SIZES)
+    ks = [int(k) for k in args.kvecs.split(",")] if args.kvecs else [4096, 8192, 16384]
+    for n in sizes:
+        cells, kcuts = EWALD_SIZES[n]
+        for kk, kc in zip((4096, 8192, 16384), kcuts):
+            if kk not in ks:
+                continue
+            system = wl.monoclinic(cells, kc)
+            line = {"workload": "ewald-split", "n_sites": n, "cells": list(cells),
+                    "k_cut_per_angstrom": kc}
+            times = {}
+            arrays = {}
+            for mode in ("fp64", "bf16x3", "tf32x3"):
+                reps = 1 if mode == "fp64" else 3
+                system.get_precomputed_array_device(mode)  # warm-up / workspace
+                torch.cuda.synchronize()
+                best = None
+                for _ in range(reps):
+                    t0 = time.perf_counter()
+                    A = system.get_precomputed_array_device(mode)
+                    torch.cuda.synchronize()
+                    dt = time.perf_counter() - t0
+                    best = dt if best is None else min(best, dt)
+                info = system.last_build_info
+                times[mode] = {"build_s": best, "fourier_ms": info["fourier_ms"],
+                               "real_ms": info["real_ms"]}
+                line["n_kvec"] = info["n_kvec"]
+                if mode == "fp64":
+                    arrays["fp64"] = A
+                else:
+                    err = (A - arrays["fp64"]).abs()
+                    times[mode]["max_err_ev"] = err.max().item() / K.EV2HARTREE
+                    times[mode]["rms_err_ev"] = (err.square().mean().sqrt().item()
+                                                 / K.EV2HARTREE)
+                    del err
+                del A
+            kn = line["n_kvec"]
+            flops = 4.0 * n * n * kn  # N x 2K by 2K x N
+            for mode in ("bf16x3", "tf32x3"):
+                t = times[mode]
+                t["speedup_vs_fp64"] = times["fp64"]["build_s"] / t["build_s"]
+                t["algorithmic_tflops"] = flops / (t["fourier_ms"] / 1e3) / 1e12
+                peak = bf16_peak if mode == "bf16x3" else bf16_peak / 2
+                t["tensor_peak_tflops"] = peak
+            times["fp64"]["algorithmic_tflops"] = flops / (times["fp64"]["fourier_ms"] / 1e3) / 1e12
+            line["modes"] = times
+            del arrays["fp64"]
+            torch.cuda.empty_cache()
+            if not args.no_cpu_baseline:
+                ns = cpu_fourier_ns_per_entry_k(system)
+                line["cpu_reference_fourier"] = {
+                    "s_per_entry_k": ns, "extrapolated_build_s": ns * n * n * kn,
+                    "cores": 1, "kind": "port",
+                    "sample": "48 rows x all N columns x 24 k-vectors of pot_k_ewald"}
+            print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
+    ap.add_argument("--workload", default="batched",
+                    choices=["batched", "ewald-split"])
+    ap.add_argument("--sizes", default="")
+    ap.add_argument("--kvecs", default="")
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=3)
@@ -252,6 +355,8 @@ def main():
     args = ap.parse_args()
     if args.impl == "reference":
         return reference_arm(args)
+    if args.workload == "ewald-split":
+        return ewald_split_bench(args)
 
     import torch
     import torch.distributed as dist

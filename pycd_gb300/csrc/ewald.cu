@@ -84,6 +84,37 @@ struct EwaldGeom {
   int64_t n;
 };
 
+// Squared minimum-image distance in FP32 (screening only: pairs whose FP32
+// distance is not clearly beyond r_cut are recomputed in FP64).
+__device__ __forceinline__ float min_image_r2_f32(const EwaldGeom& g, int64_t i,
+                                                  int64_t j) {
+  float d[3], f[3];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) d[c] = (float)(g.cart[j * 3 + c] - g.cart[i * 3 + c]);
+#pragma unroll
+  for (int c = 0; c < 3; ++c)
+    f[c] = d[0] * (float)g.inv.m[c] + d[1] * (float)g.inv.m[3 + c] +
+           d[2] * (float)g.inv.m[6 + c];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) f[c] = g.pbc[c] ? f[c] - rintf(f[c]) : f[c];
+  float best = 3.0e38f;
+  for (int dx = -1; dx <= 1; ++dx)
+    for (int dy = -1; dy <= 1; ++dy)
+      for (int dz = -1; dz <= 1; ++dz) {
+        const float w0 = f[0] + (g.pbc[0] ? dx : 0), w1 = f[1] + (g.pbc[1] ? dy : 0),
+                    w2 = f[2] + (g.pbc[2] ? dz : 0);
+        float r2 = 0.f;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          const float v = w0 * (float)g.cell.m[c] + w1 * (float)g.cell.m[3 + c] +
+                          w2 * (float)g.cell.m[6 + c];
+          r2 += v * v;
+        }
+        best = fminf(best, r2);
+      }
+  return best;
+}
+
 __device__ __forceinline__ void pair_vector(const EwaldGeom& g, int64_t i,
                                             int64_t j, double d[3]) {
   if (g.pmiv) {
@@ -132,6 +163,14 @@ __global__ void __launch_bounds__(256)
   const int64_t i = blockIdx.y;
   double d[3] = {0.0, 0.0, 0.0};
   const bool valid = j < g.n;
+  if (!DIRECT && valid && !g.pmiv && i != j) {
+    // beyond r_cut by a margin far above FP32 error: no real-space term
+    const float rc = (float)r_cut * 1.0001f;
+    if (min_image_r2_f32(g, i, j) > rc * rc) {
+      out[i * g.n + j] = 0.0;
+      return;
+    }
+  }
   if (valid) pair_vector(g, i, j, d);
   double four = 0.0;
   if (DIRECT) {
@@ -197,6 +236,16 @@ __global__ void ewald_features_kernel(const double* __restrict__ cart,
   sincos(th, &s, &c);
   F[i * ld + 2 * k] = w * c;
   F[i * ld + 2 * k + 1] = w * s;
+}
+
+int ewald_features_launch(const double* cart, int64_t n, const double* kc,
+                          const double* k2, const double* ck, int64_t K,
+                          double eps, int64_t ld, double* F, cudaStream_t s) {
+  dim3 fg((unsigned)((ld / 2 + 127) / 128), (unsigned)n);
+  ewald_features_kernel<<<fg, 128, 0, s>>>(cart, n, kc, k2, ck, K, eps, ld, F);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(e, "ewald_features_kernel", __FILE__, __LINE__);
+  return PYCD_OK;
 }
 
 // out += F F^T for the upper block tiles; each off-diagonal tile is also

@@ -1,18 +1,554 @@
-// Split-precision (BF16x3 / TF32x3) tcgen05 contraction of the Ewald
-// feature rows.  Placeholder until the tensor-core kernel lands.
+// Split-precision Ewald contraction on tcgen05 tensor cores (sm_103a).
+//
+// A_fourier = F F^T with F the N x 2K FP64 feature rows
+// [sqrt(w_k) cos(k.r_i), sqrt(w_k) sin(k.r_i)].  F is split as F = Fh + Fl
+// (BF16 or TF32 parts) and
+//     A_fourier ~= Fh Fh^T + Fh Fl^T + Fl Fh^T
+// is accumulated in FP32 in tensor memory over chunks of the K dimension;
+// each finished chunk is added in FP64 to the output, which already holds
+// the real-space and self terms, so the cross-chunk sum is FP64.
+//
+// Kernel layout (one CTA per 128 x 128 upper-triangle output tile):
+//   warp 4      TMA producer: Ah, Al (tile rows) and Bh, Bl (tile columns),
+//               128-byte K slices, SWIZZLE_128B, 3-stage ring
+//   warp 5      MMA issuer: one thread issues tcgen05.mma (M=128, N=128)
+//               into one of two TMEM accumulators (double buffered)
+//   warps 0-3   epilogue: tcgen05.ld of a finished chunk (warp w reads TMEM
+//               lanes 32w..32w+31 = tile rows), FP64 add into A[i][j] and,
+//               for off-diagonal tiles, into the mirror A[j][i]
+// Every mbarrier wait is bounded; on time-out the CTA records an error,
+// stops issuing, waits (bounded) for its own copies and MMAs, frees its
+// tensor memory and returns.
+#include <cuda.h>
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
+#include <stdint.h>
 
 #include "common.cuh"
 
 namespace pycd {
 
-size_t ewald_split_workspace_bytes(const PycdEwaldDesc*, int) { return 0; }
+constexpr int kTile = 128;               // output tile rows / columns
+constexpr int kRowBytes = 128;           // one K slice per row (swizzle span)
+constexpr int kTileBytes = kTile * kRowBytes;  // 16 KB
+constexpr int kStages = 3;
+constexpr int kStageBytes = 4 * kTileBytes;    // Ah, Al, Bh, Bl
+// TMEM: two 128-column FP32 accumulators, then the hi and lo halves of the
+// cross-chunk sum (128 columns each)
+constexpr int kTmemCols = 512;
+// K columns accumulated in FP32 per chunk: the tensor core's FP32
+// accumulation truncates, so its error grows with the MMA steps per chunk
+constexpr int kChunkCols = 256;
+constexpr uint32_t kWaitLimit = 1u << 24;      // bounded try_wait iterations
 
-int ewald_build_split(const PycdEwaldDesc*, int, double*, const double*,
-                      const double*, const double*, void*, size_t,
-                      cudaStream_t) {
-  set_error("split-precision Ewald modes are not built in this library");
-  return PYCD_ERR_INVALID_ARG;
+struct SplitErr {
+  int* flag;  // device int, set non-zero on a timed-out wait
+};
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)),
+               "r"(count)
+               : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(
+                   smem_u32(bar)),
+               "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar))
+               : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Bounded wait; also gives up early once another role has aborted.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity,
+                                          volatile int* abort_flag) {
+  for (uint32_t i = 0; i < kWaitLimit; ++i) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if ((i & 1023) == 1023 && *abort_flag) return false;
+  }
+  return false;
+}
+
+// Bounded wait that ignores the abort flag (used to drain own operations).
+__device__ __forceinline__ bool mbar_wait_drain(uint64_t* bar, uint32_t parity) {
+  for (uint32_t i = 0; i < kWaitLimit; ++i)
+    if (mbar_try_wait(bar, parity)) return true;
+  return false;
+}
+
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map,
+                                            uint64_t* bar, int x, int y) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%3, %4}], [%2];" ::"r"(smem_u32(dst)),
+      "l"((uint64_t)map), "r"(smem_u32(bar)), "r"(x), "r"(y)
+      : "memory");
+}
+
+// Shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row atoms of
+// 1024 bytes (stride-dimension byte offset 1024), descriptor version 1.
+__device__ __forceinline__ uint64_t sdesc(uint32_t saddr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);
+  d |= (uint64_t)1 << 16;             // leading byte offset (unused here) = 16 B
+  d |= (uint64_t)(1024 >> 4) << 32;   // stride byte offset = 1024 B
+  d |= (uint64_t)1 << 46;             // fixed 0b001
+  d |= (uint64_t)2 << 61;             // 128-byte swizzle
+  return d;
+}
+
+// Instruction descriptor: D = F32, A/B K-major, M = 128, N = 128;
+// operand format 1 = BF16 (kind::f16) or 2 = TF32 (kind::tf32).
+__host__ __device__ constexpr uint32_t idesc(uint32_t ab_format) {
+  return (1u << 4) | (ab_format << 7) | (ab_format << 10) |
+         ((uint32_t)(kTile >> 3) << 17) | ((uint32_t)(kTile >> 4) << 24);
+}
+
+template <bool TF32>
+__device__ __forceinline__ void umma(uint32_t d_tmem, uint64_t a, uint64_t b,
+                                     uint32_t acc) {
+  if (TF32) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+        "l"(a), "l"(b), "r"(idesc(2)), "r"(acc));
+  } else {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+        "l"(a), "l"(b), "r"(idesc(1)), "r"(acc));
+  }
+}
+
+__device__ __forceinline__ void umma_commit(uint64_t* bar) {
+  asm volatile(
+      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+          smem_u32(bar))
+      : "memory");
+}
+
+// 16 consecutive TMEM columns of this thread's lane (no wait)
+__device__ __forceinline__ void tmem_ld16_nowait(uint32_t taddr, uint32_t (&r)[16]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+      "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]),
+        "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]),
+        "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+}
+
+__device__ __forceinline__ void tmem_ld_wait() {
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+__device__ __forceinline__ void tmem_st16(uint32_t taddr, const uint32_t (&r)[16]) {
+  asm volatile(
+      "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], "
+      "{%1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, %16};" ::"r"(taddr),
+      "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]),
+      "r"(r[7]), "r"(r[8]), "r"(r[9]), "r"(r[10]), "r"(r[11]), "r"(r[12]), "r"(r[13]),
+      "r"(r[14]), "r"(r[15])
+      : "memory");
+}
+
+__device__ __forceinline__ void tmem_st_wait() {
+  asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+}
+
+template <bool TF32>
+__global__ void __launch_bounds__(192, 1)
+    ewald_split_kernel(const __grid_constant__ CUtensorMap map_h,
+                       const __grid_constant__ CUtensorMap map_l, int64_t n,
+                       int k_blocks, int chunk_blocks, double* __restrict__ out,
+                       const double* __restrict__ diag_sum, SplitErr err) {
+  const double diag_value = *diag_sum;
+  const int bi = blockIdx.y, bj = blockIdx.x;
+  if (bi > bj) return;  // lower tiles are written as mirrors
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  uint64_t* full = (uint64_t*)(smem + kStages * kStageBytes);
+  uint64_t* empty = full + kStages;
+  uint64_t* acc_full = empty + kStages;
+  uint64_t* acc_empty = acc_full + 2;
+  uint64_t* drain = acc_empty + 2;
+  volatile uint32_t* tmem_slot = (volatile uint32_t*)(drain + 1);
+  volatile int* abort_flag = (volatile int*)(tmem_slot + 1);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int n_chunks = (k_blocks + chunk_blocks - 1) / chunk_blocks;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < kStages; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&acc_full[b], 1);
+      mbar_init(&acc_empty[b], 4);
+    }
+    mbar_init(drain, 1);
+    *abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 4) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32((const void*)tmem_slot)),
+                 "r"(kTmemCols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp == 4) {
+    // ---------------- TMA producer ----------------
+    if (lane == 0) {
+      int last_kb[kStages];
+      for (int s = 0; s < kStages; ++s) last_kb[s] = -1;
+      for (int kb = 0; kb < k_blocks; ++kb) {
+        const int s = kb % kStages;
+        const uint32_t ph = (uint32_t)(kb / kStages) & 1u;
+        if (!mbar_wait(&empty[s], ph ^ 1u, abort_flag)) { *abort_flag = 1; break; }
+        if (*abort_flag) break;
+        uint8_t* st = smem + s * kStageBytes;
+        mbar_arrive_expect_tx(&full[s], kStageBytes);
+        const int x = kb * (TF32 ? kRowBytes / 4 : kRowBytes / 2);
+        tma_load_2d(st, &map_h, &full[s], x, bi * kTile);
+        tma_load_2d(st + kTileBytes, &map_l, &full[s], x, bi * kTile);
+        tma_load_2d(st + 2 * kTileBytes, &map_h, &full[s], x, bj * kTile);
+        tma_load_2d(st + 3 * kTileBytes, &map_l, &full[s], x, bj * kTile);
+        last_kb[s] = kb;
+      }
+      // every copy this thread issued has landed before the CTA moves on
+      // (already true on the normal path, where the MMA issuer consumed them)
+      for (int s = 0; s < kStages; ++s)
+        if (last_kb[s] >= 0 &&
+            !mbar_wait_drain(&full[s], (uint32_t)(last_kb[s] / kStages) & 1u))
+          *abort_flag = 1;
+    }
+  } else if (warp == 5) {
+    // ---------------- MMA issuer ----------------
+    if (lane == 0) {
+      const int ksteps = TF32 ? kRowBytes / 32 : kRowBytes / 32;  // 32-byte K steps
+      int kb = 0;
+      bool ok = true;
+      for (int c = 0; c < n_chunks && ok; ++c) {
+        const int b = c & 1;
+        if (!mbar_wait(&acc_empty[b], ((uint32_t)(c >> 1) & 1u) ^ 1u, abort_flag)) {
+          *abort_flag = 1; ok = false; break;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const uint32_t d = tmem + (uint32_t)(b * kTile);
+        const int kb_end = min(k_blocks, (c + 1) * chunk_blocks);
+        for (int first = 1; kb < kb_end; ++kb, first = 0) {
+          const int s = kb % kStages;
+          const uint32_t ph = (uint32_t)(kb / kStages) & 1u;
+          if (!mbar_wait(&full[s], ph, abort_flag)) { *abort_flag = 1; ok = false; break; }
+          asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+          const uint32_t base = smem_u32(smem + s * kStageBytes);
+          const uint64_t ah = sdesc(base), al = sdesc(base + kTileBytes);
+          const uint64_t bh = sdesc(base + 2 * kTileBytes), bl = sdesc(base + 3 * kTileBytes);
+          for (int k = 0; k < ksteps; ++k) {
+            const uint64_t o = (uint64_t)(k * 2);  // +32 bytes in the >>4 field
+            const uint32_t acc0 = (first && k == 0) ? 0u : 1u;
+            umma<TF32>(d, ah + o, bh + o, acc0);
+            umma<TF32>(d, ah + o, bl + o, 1u);
+            umma<TF32>(d, al + o, bh + o, 1u);
+          }
+          umma_commit(&empty[s]);  // stage free once these MMAs complete
+        }
+        if (!ok) break;
+        umma_commit(&acc_full[b]);  // chunk finished
+      }
+      // drain: every issued MMA has completed once this commit arrives
+      umma_commit(drain);
+      if (!mbar_wait_drain(drain, 0u)) *abort_flag = 1;
+    }
+  } else {
+    // ---------------- epilogue (warps 0-3) ----------------
+    // Cross-chunk sum per output element as an unevaluated pair hi + lo of
+    // FP32 values kept in TMEM columns [256, 384) and [384, 512): each chunk
+    // is added with Knuth's error-free TwoSum, the rounding error going to
+    // lo, so the pair carries ~48 significant bits; the FP64 result
+    // (double)hi + (double)lo is written once per tile.
+    const int64_t row = (int64_t)bi * kTile + warp * 32 + lane;
+    const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
+    const uint32_t t_hi = lane_base + 2u * kTile, t_lo = lane_base + 3u * kTile;
+    bool ok = true;
+    for (int c = 0; c < n_chunks; ++c) {
+      const int b = c & 1;
+      bool got = false;
+      if (lane == 0) got = mbar_wait(&acc_full[b], (uint32_t)(c >> 1) & 1u, abort_flag);
+      got = __shfl_sync(0xffffffffu, got, 0);
+      if (!got) {
+        if (lane == 0) *abort_flag = 1;
+        ok = false;
+        break;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const uint32_t t_acc = lane_base + (uint32_t)(b * kTile);
+#pragma unroll 1
+      for (int cb = 0; cb < kTile / 16; ++cb) {
+        const uint32_t off = (uint32_t)(cb * 16);
+        uint32_t a[16], h[16], l[16];
+        tmem_ld16_nowait(t_acc + off, a);
+        if (c > 0) {
+          tmem_ld16_nowait(t_hi + off, h);
+          tmem_ld16_nowait(t_lo + off, l);
+        }
+        tmem_ld_wait();
+#pragma unroll
+        for (int q = 0; q < 16; ++q) {
+          const float x = __uint_as_float(a[q]);
+          if (c == 0) {
+            h[q] = a[q];
+            l[q] = 0u;
+          } else {
+            const float hv = __uint_as_float(h[q]);
+            const float s = __fadd_rn(hv, x);
+            const float bb = __fsub_rn(s, hv);
+            const float e = __fadd_rn(__fsub_rn(hv, __fsub_rn(s, bb)), __fsub_rn(x, bb));
+            h[q] = __float_as_uint(s);
+            l[q] = __float_as_uint(__fadd_rn(__uint_as_float(l[q]), e));
+          }
+        }
+        tmem_st16(t_hi + off, h);
+        tmem_st16(t_lo + off, l);
+      }
+      tmem_st_wait();
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&acc_empty[b]);
+    }
+    if (ok) {
+      // diagonal: F_i . F_i = sum_k w_k (cos^2 + sin^2) = sum_k w_k exactly,
+      // taken from the FP64 weight sum instead of the FP32 accumulation
+#pragma unroll 1
+      for (int cb = 0; cb < kTile / 16; ++cb) {
+        const uint32_t off = (uint32_t)(cb * 16);
+        uint32_t h[16], l[16];
+        tmem_ld16_nowait(t_hi + off, h);
+        tmem_ld16_nowait(t_lo + off, l);
+        tmem_ld_wait();
+        const int64_t col0 = (int64_t)bj * kTile + cb * 16;
+        if (row < n) {
+#pragma unroll
+          for (int q = 0; q < 16; ++q) {
+            const int64_t col = col0 + q;
+            if (col < n) {
+              double v = (double)__uint_as_float(h[q]) + (double)__uint_as_float(l[q]);
+              if (col == row) v = diag_value;
+              out[row * n + col] += v;
+              if (bi != bj) out[col * n + row] += v;
+            }
+          }
+        }
+      }
+    }
+  }
+
+  // ---------------- teardown ----------------
+  __syncthreads();
+  if (threadIdx.x == 0 && *abort_flag) atomicExch(err.flag, 1);
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  if (warp == 4) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                 "r"(kTmemCols));
+  }
+}
+
+// sum_k w_k = F_i . F_i, with w_k = 2 c_k / (k^2 eps) as in the feature rows
+__global__ void weight_sum_kernel(const double* __restrict__ k2,
+                                  const double* __restrict__ ck, int64_t K,
+                                  double eps, double* __restrict__ out) {
+  __shared__ double red[256];
+  double s = 0.0;
+  for (int64_t k = threadIdx.x; k < K; k += blockDim.x) s += 2.0 * ck[k] / (k2[k] * eps);
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int o = 128; o > 0; o >>= 1) {
+    if ((int)threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *out = red[0];
+}
+
+// Split the FP64 feature rows into hi/lo parts, zero-padded to `ld` columns.
+template <bool TF32>
+__global__ void split_features_kernel(const double* __restrict__ F, int64_t n,
+                                      int64_t ldf, int64_t kdim, int64_t ld,
+                                      void* __restrict__ hi, void* __restrict__ lo) {
+  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t r = blockIdx.y;
+  if (r >= n || c >= ld) return;
+  const double f = c < kdim ? F[r * ldf + c] : 0.0;
+  if (TF32) {
+    uint32_t hb, lb;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(hb) : "f"((float)f));
+    const float h = __uint_as_float(hb);
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(lb) : "f"((float)(f - (double)h)));
+    ((float*)hi)[r * ld + c] = h;
+    ((float*)lo)[r * ld + c] = __uint_as_float(lb);
+  } else {
+    const __nv_bfloat16 h = __double2bfloat16(f);
+    const __nv_bfloat16 l = __double2bfloat16(f - (double)__bfloat162float(h));
+    ((__nv_bfloat16*)hi)[r * ld + c] = h;
+    ((__nv_bfloat16*)lo)[r * ld + c] = l;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t,
+                                  void*, const cuuint64_t*, const cuuint64_t*,
+                                  const cuuint32_t*, const cuuint32_t*,
+                                  CUtensorMapInterleave, CUtensorMapSwizzle,
+                                  CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static int get_encode(EncodeTiledFn* fn) {
+  static EncodeTiledFn cached = nullptr;
+  if (!cached) {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p,
+                                                     12000, cudaEnableDefault, &q);
+    if (e != cudaSuccess || q != cudaDriverEntryPointSuccess || !p) {
+      set_error("cuTensorMapEncodeTiled is not available from the driver");
+      return PYCD_ERR_CUDA;
+    }
+    cached = (EncodeTiledFn)p;
+  }
+  *fn = cached;
+  return PYCD_OK;
+}
+
+static int64_t split_ld(int64_t kdim, bool tf32) {
+  const int64_t per = tf32 ? kRowBytes / 4 : kRowBytes / 2;  // elements per K block
+  return ((kdim + per - 1) / per) * per;
+}
+
+static size_t align256s(size_t b) { return (b + 255) & ~(size_t)255; }
+
+// feature matrix F (FP64) is laid out by ewald.cu; here only hi/lo + error
+size_t ewald_split_workspace_bytes(const PycdEwaldDesc* d, int mode) {
+  const bool tf32 = mode == PYCD_EWALD_TF32X3;
+  const int64_t kdim = 2 * d->n_kvec;
+  const int64_t ld = split_ld(kdim, tf32);
+  const size_t es = tf32 ? 4 : 2;
+  const int64_t ldf = ((kdim + 15) / 16) * 16;
+  return align256s(sizeof(double) * (size_t)d->n_sites * (size_t)ldf) +
+         2 * align256s(es * (size_t)d->n_sites * (size_t)ld) + 256;
+}
+
+int ewald_features_launch(const double* cart, int64_t n, const double* kc,
+                          const double* k2, const double* ck, int64_t K,
+                          double eps, int64_t ld, double* F, cudaStream_t s);
+
+int ewald_build_split(const PycdEwaldDesc* d, int mode, double* out,
+                      const double* kc, const double* k2, const double* ck,
+                      void* ws, size_t ws_bytes, cudaStream_t s) {
+  const bool tf32 = mode == PYCD_EWALD_TF32X3;
+  const int64_t n = d->n_sites, K = d->n_kvec, kdim = 2 * K;
+  const int64_t ldf = ((kdim + 15) / 16) * 16;
+  const int64_t ld = split_ld(kdim, tf32);
+  const size_t es = tf32 ? 4 : 2;
+  if (ws_bytes < ewald_split_workspace_bytes(d, mode)) {
+    set_error("split workspace too small");
+    return PYCD_ERR_WORKSPACE;
+  }
+  char* p = (char*)ws;
+  double* F = (double*)p;
+  p += align256s(sizeof(double) * (size_t)n * (size_t)ldf);
+  void* hi = p;
+  p += align256s(es * (size_t)n * (size_t)ld);
+  void* lo = p;
+  p += align256s(es * (size_t)n * (size_t)ld);
+  int* flag = (int*)p;
+  double* diag_sum = (double*)(p + 8);
+  PYCD_REQUIRE(((uintptr_t)hi & 15) == 0 && ((uintptr_t)lo & 15) == 0,
+               "split operands must be 16-byte aligned");
+  int rc = ewald_features_launch(d->d_cart, n, kc, k2, ck, K, d->dielectric, ldf, F, s);
+  if (rc) return rc;
+  weight_sum_kernel<<<1, 256, 0, s>>>(k2, ck, K, d->dielectric, diag_sum);
+  PYCD_CUDA(cudaGetLastError());
+  dim3 sg((unsigned)((ld + 255) / 256), (unsigned)n);
+  if (tf32)
+    split_features_kernel<true><<<sg, 256, 0, s>>>(F, n, ldf, kdim, ld, hi, lo);
+  else
+    split_features_kernel<false><<<sg, 256, 0, s>>>(F, n, ldf, kdim, ld, hi, lo);
+  PYCD_CUDA(cudaGetLastError());
+  PYCD_CUDA(cudaMemsetAsync(flag, 0, sizeof(int), s));
+
+  EncodeTiledFn enc;
+  rc = get_encode(&enc);
+  if (rc) return rc;
+  CUtensorMap mh, ml;
+  const cuuint64_t gdim[2] = {(cuuint64_t)ld, (cuuint64_t)n};
+  const cuuint64_t gstride[1] = {(cuuint64_t)(ld * es)};
+  const cuuint32_t box[2] = {(cuuint32_t)(kRowBytes / es), (cuuint32_t)kTile};
+  const cuuint32_t estr[2] = {1, 1};
+  const CUtensorMapDataType dt =
+      tf32 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16;
+  CUresult r1 = enc(&mh, dt, 2, hi, gdim, gstride, box, estr,
+                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                    CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  CUresult r2 = enc(&ml, dt, 2, lo, gdim, gstride, box, estr,
+                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                    CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r1 != CUDA_SUCCESS || r2 != CUDA_SUCCESS) {
+    set_error("cuTensorMapEncodeTiled failed (%d, %d)", (int)r1, (int)r2);
+    return PYCD_ERR_CUDA;
+  }
+  const int k_blocks = (int)(ld / (kRowBytes / es));
+  const int chunk_blocks = (int)(kChunkCols / (kRowBytes / es));
+  const size_t smem = (size_t)kStages * kStageBytes + 1024 + 256;
+  const unsigned nb = (unsigned)((n + kTile - 1) / kTile);
+  SplitErr err{flag};
+  if (tf32) {
+    PYCD_CUDA(cudaFuncSetAttribute(ewald_split_kernel<true>,
+                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    ewald_split_kernel<true><<<dim3(nb, nb), 192, smem, s>>>(
+        mh, ml, n, k_blocks, chunk_blocks, out, diag_sum, err);
+  } else {
+    PYCD_CUDA(cudaFuncSetAttribute(ewald_split_kernel<false>,
+                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    ewald_split_kernel<false><<<dim3(nb, nb), 192, smem, s>>>(
+        mh, ml, n, k_blocks, chunk_blocks, out, diag_sum, err);
+  }
+  PYCD_CUDA(cudaGetLastError());
+  int h_flag = 0;
+  PYCD_CUDA(cudaMemcpyAsync(&h_flag, flag, sizeof(int), cudaMemcpyDeviceToHost, s));
+  PYCD_CUDA(cudaStreamSynchronize(s));
+  if (h_flag) {
+    set_error("split-precision Ewald kernel timed out waiting on a barrier");
+    return PYCD_ERR_CUDA;
+  }
+  return PYCD_OK;
 }
 
 }  // namespace pycd

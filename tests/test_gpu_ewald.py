@@ -84,3 +84,38 @@ def test_corundum3600_build_properties_and_oracle_rows(cuda_ready):
                          (10, 10, 3), sysm.alpha, sysm.r_cut, sysm.k_cut,
                          mat.dielectric_constant, rows=rows)
     assert np.abs(An[rows] - ref).max() < TOL_HA
+
+
+SPLIT_TOL_HA = 1e-6 * K.EV2HARTREE  # split-precision target: 1e-6 eV per entry
+
+
+@pytest.mark.parametrize("precision,tol_ev", [("bf16x3", 2e-6), ("tf32x3", 1e-6)])
+def test_split_precision_small_matches_fp64(cuda_ready, precision, tol_ev):
+    """324 sites, K = 280: few, heavy k-vectors put the BF16 hi+lo split's
+    own error floor near 1e-6 eV here, hence its 2e-6 eV bound."""
+    sysm = wl.corundum((3, 3, 3), neighbor_list=False)
+    ref = sysm.get_precomputed_array_device("fp64").cpu().numpy()
+    A = sysm.get_precomputed_array_device(precision).cpu().numpy()
+    assert sysm.last_build_info["mode"] == precision
+    assert np.isfinite(A).all()
+    assert np.abs(A - ref).max() < tol_ev * K.EV2HARTREE
+    # off-diagonal tiles are written with their mirror: symmetric to rounding
+    assert np.abs(A - A.T).max() < SPLIT_TOL_HA
+
+
+@pytest.mark.parametrize("precision", ["bf16x3", "tf32x3"])
+def test_split_precision_monoclinic_8192(cuda_ready, precision):
+    """N = 8,192 monoclinic (16x16x8 cells), K = 4,095: every entry within
+    1e-6 eV of the FP64 feature build, which itself matches the oracle."""
+    sysm = wl.monoclinic((16, 16, 8), 0.9164)
+    ref = sysm.get_precomputed_array_device("fp64")
+    A = sysm.get_precomputed_array_device(precision)
+    assert sysm.last_build_info["n_kvec"] == 4095
+    err = (A - ref).abs().max().item()
+    assert err < SPLIT_TOL_HA, err / K.EV2HARTREE
+    m = sysm.material
+    rows = np.array([0, 4097, 8191])
+    orc = eo.class_array(m.cartesian_unit_cell_coords, m.lattice_matrix, (16, 16, 8),
+                         sysm.alpha, sysm.r_cut, sysm.k_cut, m.dielectric_constant,
+                         rows=rows)
+    assert np.abs(ref.cpu().numpy()[rows] - orc).max() < TOL_HA
