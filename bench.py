@@ -336,10 +336,165 @@ def ewald_split_bench(args):
             print(json.dumps(line), flush=True)
 
 
+def _lattice_tables(cache, lattice, cells, precision):
+    from pycd_gb300 import workloads as wl
+    key = (lattice, tuple(cells), precision)
+    if key not in cache:
+        system = wl.system_for(lattice, cells)
+        A = system.get_precomputed_array_device(precision)
+        base, _ = wl.batched_tables(system, A, 1, [], 1.0, T_FINAL, DT)
+        base.share_rate_coefficients()
+        cache[key] = (system, base)
+    return cache[key]
+
+
+def _job_occupancy(n_sites, n_carriers, dopants, seed, width):
+    free = np.setdiff1d(np.arange(n_sites), dopants)
+    occ = np.zeros(width, np.int32)
+    occ[:n_carriers] = np.random.default_rng(seed).choice(free, n_carriers, replace=False)
+    return occ
+
+
+def diffusivity(disp, t):
+    """D = <|dr|^2> / (6 t) per carrier (Einstein relation at the end of
+    each trajectory); returns mean and standard error over carriers."""
+    r2 = (disp ** 2).sum(-1)
+    d = (r2 / (6.0 * t[:, None])).ravel()
+    return float(d.mean()), float(d.std(ddof=1) / np.sqrt(len(d)))
+
+
+def uneven_bench(args):
+    """64 systems of both lattices (300-20,000 sites), 2,048 trajectories with
+    1-16 carriers, 0-16 dopants and 1e4-1e6 steps, split-precision arrays,
+    bucketed autotuned launches; plus FP64-vs-split diffusivity checks."""
+    import torch
+    from pycd_gb300 import _native as nat
+    from pycd_gb300 import constants as K
+    from pycd_gb300 import workloads as wl
+    from pycd_gb300.batch import BatchedKmc
+    torch.cuda.set_device(0)
+    nat.require_device()
+    specs, traj_sys, steps = wl.uneven_systems()
+    cache, tables = {}, []
+    t0 = time.perf_counter()
+    for spec in specs:
+        system, base = _lattice_tables(cache, spec["lattice"], spec["cells"], "bf16x3")
+        n = system.neighbors.num_system_elements
+        _, dop = wl.sites_for(n, spec["carriers"], spec["dopants"], spec["seed"])
+        q = np.zeros(n)
+        q[dop] = 1.0
+        tables.append(base.with_charges(q, spec["carriers"]))
+        spec["n_sites"], spec["dopant_sites"] = n, dop
+    torch.cuda.synchronize()
+    setup_s = time.perf_counter() - t0
+    occ = np.stack([_job_occupancy(specs[s]["n_sites"], specs[s]["carriers"],
+                                   specs[s]["dopant_sites"], 7000 + i, 16)
+                    for i, s in enumerate(traj_sys)])
+    bk = BatchedKmc(tables, occ, sys_index=traj_sys, seed=SEED, chunk_steps=args.chunk,
+                    step_limit=steps, autotune=True)
+    tuned = [(bkt.engine.launch.lanes_per_traj, bkt.engine.launch.warps_per_block,
+              len(bkt.idx)) for bkt in bk.buckets]
+    torch.cuda.synchronize()
+    with ClockSampler(0) as clocks:
+        t0 = time.perf_counter()
+        chunks = 0
+        while True:
+            bk.step_chunk()
+            chunks += 1
+            if chunks % 10 == 0 or chunks * args.chunk >= int(steps.max()):
+                torch.cuda.synchronize()
+                st = bk.status_counts()
+                if st.get(nat.TRAJ_RUNNING, 0) == 0:
+                    break
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+    total = bk.steps_done()
+    arrays_gb = sum(8.0 * s["n_sites"] ** 2 for s in specs) / 1e9
+    # diffusivity: FP64 vs split arrays on the six smallest lattices, no dopants
+    checks = []
+    small = sorted({(s["lattice"], tuple(s["cells"]), s["n_sites"]) for s in specs},
+                   key=lambda x: x[2])[:6]
+    for lattice, cells, n in small:
+        res = {}
+        for prec in ("fp64", "bf16x3"):
+            system, base = _lattice_tables(cache, lattice, cells, prec)
+            tab = base.with_charges(np.zeros(n), 4)
+            o = np.stack([_job_occupancy(n, 4, [], 9000 + i, 4) for i in range(256)])
+            b2 = BatchedKmc(tab, o, seed=SEED + 1, chunk_steps=20000, step_limit=100000)
+            b2.run(100000)
+            torch.cuda.synchronize()
+            disp = (b2.batch.last_row + b2.batch.disp).cpu().numpy().reshape(256, 4, 3)
+            t = b2.batch.time.cpu().numpy()
+            res[prec] = diffusivity(disp, t)
+        d64, s64 = res["fp64"]
+        ds, ss = res["bf16x3"]
+        checks.append({"lattice": lattice, "n_sites": n, "D_fp64": d64, "sem_fp64": s64,
+                       "D_split": ds, "sem_split": ss,
+                       "z": abs(d64 - ds) / max(1e-300, np.hypot(s64, ss))})
+    line = {"workload": "batched uneven", "metric": "KMC steps/s (uneven batch)",
+            "value": total / wall, "unit": "steps/s", "steps": int(total),
+            "wall_s": wall, "systems": len(specs), "trajectories": int(len(traj_sys)),
+            "site_range": [int(min(s["n_sites"] for s in specs)),
+                           int(max(s["n_sites"] for s in specs))],
+            "arrays_gb": arrays_gb, "setup_s": setup_s, "chunk_steps": args.chunk,
+            "buckets_lanes_warps_trajs": tuned, "status_counts": bk.status_counts(),
+            "diffusivity_fp64_vs_split": checks, "clocks": clocks.summary()}
+    print(json.dumps(line), flush=True)
+
+
+def serving_bench(args):
+    """Poisson arrivals (200 jobs/s) of single-trajectory KMC jobs over both
+    lattices; continuous batching; p50/p99 latency and aggregate steps/s;
+    a sample of jobs re-run alone must give identical results."""
+    import torch
+    from pycd_gb300 import _native as nat
+    from pycd_gb300.batch import BatchedKmc
+    from pycd_gb300.serving import KmcServer, poisson_jobs
+    torch.cuda.set_device(0)
+    nat.require_device()
+    jobs = poisson_jobs(args.jobs, rate=200.0, seed=11, max_steps=args.max_job_steps)
+    server = KmcServer(budget_bytes=150e9, chunk_steps=args.chunk, precision="bf16x3",
+                       seed=SEED)
+    t0 = time.perf_counter()
+    for j in jobs:  # warm the lattice cache: arrays are shared across jobs
+        server.cache.get(j["lattice"], j["cells"])
+    torch.cuda.synchronize()
+    warm_s = time.perf_counter() - t0
+    with ClockSampler(0) as clocks:
+        stats = server.run([dict(j) for j in jobs])
+    # alone vs in the mix
+    rng = np.random.default_rng(3)
+    same = []
+    for j in rng.choice(server.done, size=min(6, len(server.done)), replace=False):
+        lat = server.cache.get(j["lattice"], j["cells"])
+        n = lat["n_sites"]
+        q = np.zeros(n)
+        q[j["dopant_sites"]] = 1.0
+        tab = lat["tables"].with_charges(q, j["carriers"])
+        alone = BatchedKmc(tab, np.asarray(j["carrier_sites"])[None, :], seed=SEED,
+                           chunk_steps=j["steps"], step_limit=j["steps"],
+                           traj_offset=j["id"], use_graph=False)
+        alone.run(j["steps"])
+        torch.cuda.synchronize()
+        disp = (alone.batch.last_row + alone.batch.disp).cpu().numpy()[0, :3 * j["carriers"]]
+        same.append(bool(np.array_equal(alone.batch.occ.cpu().numpy()[0, :j["carriers"]],
+                                        j["occupancy"])
+                         and alone.batch.time.item() == j["time"]
+                         and np.array_equal(disp.reshape(-1, 3), j["displacement"])))
+    line = {"workload": "serving", "metric": "KMC job latency p50/p99 and steps/s",
+            "arrival_rate_jobs_per_s": 200.0, "jobs": len(jobs),
+            "lattice_cache_warm_s": warm_s, **stats,
+            "alone_equals_mix": same, "chunk_steps": args.chunk,
+            "clocks": clocks.summary()}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--workload", default="batched",
-                    choices=["batched", "ewald-split"])
+                    choices=["batched", "ewald-split", "uneven", "serving"])
+    ap.add_argument("--jobs", type=int, default=2000)
+    ap.add_argument("--max-job-steps", type=int, default=1_000_000)
     ap.add_argument("--sizes", default="")
     ap.add_argument("--kvecs", default="")
     ap.add_argument("--gpus", type=int, default=1)
@@ -357,6 +512,10 @@ def main():
         return reference_arm(args)
     if args.workload == "ewald-split":
         return ewald_split_bench(args)
+    if args.workload == "uneven":
+        return uneven_bench(args)
+    if args.workload == "serving":
+        return serving_bench(args)
 
     import torch
     import torch.distributed as dist
@@ -375,8 +534,12 @@ def main():
         launch["lanes_per_traj"] = args.lanes
     if args.warps:
         launch["warps_per_block"] = args.warps
+    # launch shape: autotuned (untimed) unless given; it never changes events
     bk = BatchedKmc(tables, occ, seed=SEED, chunk_steps=args.chunk,
-                    traj_offset=rank * args.traj, launch=launch)
+                    traj_offset=rank * args.traj, launch=launch,
+                    autotune=not (args.lanes or args.warps))
+    tuned = {"lanes_per_traj": bk.buckets[0].engine.launch.lanes_per_traj,
+             "warps_per_block": bk.buckets[0].engine.launch.warps_per_block}
     flush = torch.empty(256 * 2 ** 20, dtype=torch.uint8, device="cuda")
     for _ in range(args.warmup):
         bk.step_chunk()
@@ -458,6 +621,7 @@ def main():
                        "l2": "256 MiB buffer written between timed chunks",
                        "parallelism": f"replicas x{world}"},
             "plain_steps_per_s": plain, "batched_over_plain": value / world / plain,
+            "launch_shape": tuned,
             "status_counts": status,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm,
                          "unit": "GB/s", "frac": achieved / hbm, "traffic": None,

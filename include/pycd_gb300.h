@@ -62,7 +62,8 @@ typedef enum PycdTrajStatus {
   PYCD_TRAJ_NEED_UNIFORMS = 2, /* injected uniform stream exhausted; refill  */
   PYCD_TRAJ_STALLED = 3,       /* k_total == 0 or not finite (core.py:2800)  */
   PYCD_TRAJ_BAD_INDEX = 4,     /* neighbour / site index out of range        */
-  PYCD_TRAJ_NO_EVENT = 5       /* u1 at or above the last cumulative rate    */
+  PYCD_TRAJ_NO_EVENT = 5,      /* u1 at or above the last cumulative rate    */
+  PYCD_TRAJ_STEP_LIMIT = 6     /* reached its d_step_limit                   */
 } PycdTrajStatus;
 
 /* ------------------------------------------------------------------------ */
@@ -190,7 +191,18 @@ typedef struct PycdKmcSystem {
   double kT;                    /* k_B T in Hartree                          */
   double time_interval;         /* path-grid spacing (a.u. time)             */
   int64_t n_path_steps;         /* rows of the path grid: int(t_final/dt)+1  */
+  /* Optional N x S (c1, c0) rate-coefficient pairs from
+   * pycd_kmc_rate_coefficients, shared by systems on the same lattice; NULL
+   * makes the library derive them into its workspace at upload.            */
+  const double* d_rate_coef;
 } PycdKmcSystem;
+
+/* (c1, c0) per (site, slot) for `system`: c1 = -1/(4 lam kT),
+ * c0 = (V_ab + shift)/kT + ln vn, so that the hop rate is
+ * exp(c1 (lam + dE0)^2 + c0) = vn exp(-dG/kT) (PyCD/core.py:2045-2047).
+ * d_out holds 2 * n_sites * n_slots doubles.                               */
+PYCD_API int pycd_kmc_rate_coefficients(const PycdKmcSystem* system,
+                                        double* d_out, void* stream);
 
 /* Trajectory state, structure-of-arrays over T trajectories.  All device
  * arrays; the kernels read and update them in place so a run can be resumed
@@ -209,6 +221,7 @@ typedef struct PycdKmcState {
   double* d_energy;             /* T: current_state_energy (or NULL)         */
   int32_t* d_status;            /* T: PycdTrajStatus                          */
   int64_t* d_u_cursor;          /* T: uniforms consumed (injected mode)      */
+  const int64_t* d_step_limit;  /* T: stop after this many steps, or NULL    */
 } PycdKmcState;
 
 /* Optional per-trajectory outputs.  Each pointer may be NULL.               */
@@ -238,6 +251,9 @@ typedef struct PycdKmcRng {
    * key = seed and counter = (step, trajectory id + traj_offset).           */
   uint64_t seed;
   uint64_t traj_offset;
+  /* T stream ids (device), or NULL for traj_offset + t: lets a trajectory
+   * keep its stream whichever batch or bucket it is advanced in.           */
+  const uint64_t* d_traj_ids;
 } PycdKmcRng;
 
 /* Launch shape of the persistent kernel (0 fields = heuristic).  The two

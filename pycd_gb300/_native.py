@@ -26,6 +26,7 @@ TRAJ_NEED_UNIFORMS = 2
 TRAJ_STALLED = 3
 TRAJ_BAD_INDEX = 4
 TRAJ_NO_EVENT = 5
+TRAJ_STEP_LIMIT = 6
 
 # Ewald modes (PycdEwaldMode)
 EWALD_FP64_DIRECT = 0
@@ -61,7 +62,8 @@ class KmcSystem(C.Structure):
                 ("n_sites", C.c_int64), ("n_slots", C.c_int32),
                 ("n_carriers", C.c_int32), ("carrier_charge", C.c_double),
                 ("vn", C.c_double), ("kT", C.c_double),
-                ("time_interval", C.c_double), ("n_path_steps", C.c_int64)]
+                ("time_interval", C.c_double), ("n_path_steps", C.c_int64),
+                ("d_rate_coef", C.c_void_p)]
 
 
 class KmcState(C.Structure):
@@ -70,7 +72,8 @@ class KmcState(C.Structure):
                 ("d_time", C.c_void_p), ("d_step", C.c_void_p),
                 ("d_path_index", C.c_void_p), ("d_disp", C.c_void_p),
                 ("d_last_row", C.c_void_p), ("d_energy", C.c_void_p),
-                ("d_status", C.c_void_p), ("d_u_cursor", C.c_void_p)]
+                ("d_status", C.c_void_p), ("d_u_cursor", C.c_void_p),
+                ("d_step_limit", C.c_void_p)]
 
 
 class KmcOutputs(C.Structure):
@@ -84,7 +87,7 @@ class KmcOutputs(C.Structure):
 class KmcRng(C.Structure):
     _fields_ = [("d_uniforms", C.c_void_p), ("u_stride", C.c_int64),
                 ("u_count", C.c_int64), ("seed", C.c_uint64),
-                ("traj_offset", C.c_uint64)]
+                ("traj_offset", C.c_uint64), ("d_traj_ids", C.c_void_p)]
 
 
 class KmcLaunch(C.Structure):
@@ -123,6 +126,7 @@ _PROTOS = {
                                             C.c_void_p]),
     "pycd_philox_uniforms": (C.c_int, [C.c_uint64, C.c_uint64, C.c_int64,
                                        C.c_int64, C.c_void_p, C.c_void_p]),
+    "pycd_kmc_rate_coefficients": (C.c_int, [P(KmcSystem), C.c_void_p, C.c_void_p]),
     "pycd_debug_exp": (C.c_int, [C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p,
                                  C.c_void_p]),
 }

@@ -1,0 +1,65 @@
+"""Launch-shape autotuner for the KMC kernel.
+
+The kernel's event streams do not depend on its launch shape (cumulative
+rates are fixed balanced-tree sums over the process index), so the shape is
+a pure performance choice.  ``tune`` times short probes of every candidate
+(lanes per trajectory x warps per block) on the real batch, restoring the
+batch state after each probe, and keeps the fastest.  Results are cached per
+(process count, carrier count, trajectory count) in-process.
+"""
+import numpy as np
+
+_CACHE = {}
+
+
+def candidates(max_processes, max_carriers):
+    out = []
+    for lanes in (4, 8, 16, 32):
+        if lanes < max_carriers:
+            continue
+        per_lane = -(-max_processes // lanes)
+        if per_lane > 8:
+            continue
+        for warps in (2, 4, 8):
+            out.append({"lanes_per_traj": lanes, "warps_per_block": warps})
+    return out
+
+
+def tune(engine, batch, rng, probe_steps=200, reps=2, stream=None):
+    """Pick the fastest launch shape for (engine, batch); sets it on the
+    engine and returns ``{"best": shape, "table": [(shape, ms), ...]}``."""
+    import torch
+    key = (int(engine.launch.max_processes), int(engine.launch.max_carriers),
+           int(batch.n_traj))
+    if key in _CACHE:
+        best = _CACHE[key]
+        engine.launch.lanes_per_traj = best["lanes_per_traj"]
+        engine.launch.warps_per_block = best["warps_per_block"]
+        return {"best": best, "table": [], "cached": True}
+    snap = batch.snapshot()
+    limit = batch.step_limit
+    batch.step_limit = None  # probes must not stop early
+    table = []
+    s = stream or torch.cuda.current_stream()
+    for cand in candidates(engine.launch.max_processes, engine.launch.max_carriers):
+        engine.launch.lanes_per_traj = cand["lanes_per_traj"]
+        engine.launch.warps_per_block = cand["warps_per_block"]
+        times = []
+        for r in range(reps + 1):
+            batch.restore(snap)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(s)
+            engine.advance(batch, probe_steps, rng, stream=s)
+            e1.record(s)
+            e1.synchronize()
+            if r:
+                times.append(e0.elapsed_time(e1))
+        table.append((cand, float(np.median(times))))
+    batch.restore(snap)
+    batch.step_limit = limit
+    best = min(table, key=lambda x: x[1])[0]
+    engine.launch.lanes_per_traj = best["lanes_per_traj"]
+    engine.launch.warps_per_block = best["warps_per_block"]
+    _CACHE[key] = best
+    return {"best": best, "table": table, "cached": False}

@@ -254,6 +254,14 @@ class Run(object):
         per_cell = m.n_elements_per_unit_cell[eti]
         head = m.n_elements_per_unit_cell[:eti].sum()
         hl = sysm.hop_neighbor_list[key]
+        if self._site_tables_vectorised(nbr, hop, lam, vab, shift, key, hl, tpc,
+                                        per_cell, head, S):
+            self.site_nbr, self.site_hop = nbr, hop
+            self.site_lam, self.site_vab = lam, vab
+            self.site_field_shift = shift if self.electric_field_active else None
+            self.carrier_charge = float(
+                m.species_charge_list[self.species_charge_type][si])
+            return
         for cell in range(int(self.system.num_cells)):
             for e in range(per_cell):
                 site = cell * tpc + head + e
@@ -283,6 +291,42 @@ class Run(object):
         self.site_field_shift = shift if self.electric_field_active else None
         self.carrier_charge = float(
             m.species_charge_list[self.species_charge_type][si])
+
+    def _site_tables_vectorised(self, nbr, hop, lam, vab, shift, key, hl, tpc,
+                                per_cell, head, S):
+        """Fill the tables with array operations when every site of a class
+        has the same neighbour count per hop type (the common case); returns
+        False to fall back to the per-site loop."""
+        m, sysm = self.material, self.system
+        n_cells = int(self.system.num_cells)
+        eei = np.arange(n_cells * per_cell)
+        sites = (eei // per_cell) * tpc + head + (eei % per_cell)
+        cls = np.asarray(sysm.system_class_index_list)[sites]
+        for ci in np.unique(cls):
+            sel = np.nonzero(cls == ci)[0]
+            s0 = 0
+            for t, obj in enumerate(hl[ci][:len(m.neighbor_cutoff_dist[key][ci])]):
+                counts = np.asarray(obj.num_neighbors)[sel]
+                if len(counts) == 0 or np.any(counts != counts[0]):
+                    return False
+                c = int(counts[0])
+                if s0 + c > S:
+                    return False
+                idx = np.stack([np.asarray(obj.neighbor_system_element_indices[e])
+                                for e in sel]).reshape(len(sel), c)
+                vec = np.stack([np.asarray(obj.displacement_vector_list[e], np.float64)
+                                .reshape(-1, 3) for e in sel]).reshape(len(sel), c, 3)
+                nbr[sites[sel], s0:s0 + c] = idx
+                hop[sites[sel], s0:s0 + c] = vec
+                lam[sites[sel], s0:s0 + c] = m.lambda_values[key][ci][t]
+                vab[sites[sel], s0:s0 + c] = m.v_ab[key][ci][t]
+                if self.electric_field_active:
+                    shift[sites[sel], s0:s0 + c] = 0.5 * np.einsum(
+                        "k,ijk->ij", self.electric_field, vec)
+                s0 += c
+            if s0 != S:
+                return False
+        return True
 
     # -- charges (core.py:2530-2564) ----------------------------------------
     def base_charge_config(self):

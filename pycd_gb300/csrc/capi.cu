@@ -59,11 +59,14 @@ static size_t kmc_table_bytes(int32_t n_systems) {
   return 256 + align256(sizeof(KmcSysDev) * (size_t)(n_systems > 0 ? n_systems : 1));
 }
 
+static size_t kmc_coef_bytes(const PycdKmcSystem& s) {
+  return s.d_rate_coef ? 0
+                       : align256(sizeof(double2) * (size_t)s.n_sites * (size_t)s.n_slots);
+}
+
 static size_t kmc_ws_bytes(const PycdKmcSystem* systems, int32_t n_systems) {
   size_t b = kmc_table_bytes(n_systems);
-  for (int i = 0; i < n_systems; ++i)
-    b += align256(sizeof(double2) * (size_t)systems[i].n_sites *
-                  (size_t)systems[i].n_slots);
+  for (int i = 0; i < n_systems; ++i) b += kmc_coef_bytes(systems[i]);
   return b;
 }
 
@@ -239,15 +242,19 @@ int pycd_kmc_upload_systems(const PycdKmcSystem* systems, int32_t n_systems,
   size_t off = 0;
   for (int i = 0; i < n_systems; ++i) {
     dev[i].pub = systems[i];
-    dev[i].coef = (const double2*)(coef_base + off);
+    PYCD_REQUIRE(((uintptr_t)systems[i].d_rate_coef & 15) == 0,
+                 "system %d: d_rate_coef must be 16-byte aligned", i);
+    dev[i].coef = systems[i].d_rate_coef
+                      ? (const double2*)systems[i].d_rate_coef
+                      : (const double2*)(coef_base + off);
     dev[i].pad = 0;
-    off += align256(sizeof(double2) * (size_t)systems[i].n_sites *
-                    (size_t)systems[i].n_slots);
+    off += kmc_coef_bytes(systems[i]);
   }
   cudaStream_t s = (cudaStream_t)stream;
   PYCD_CUDA(cudaMemcpyAsync(d_workspace, host.data(), host.size(),
                             cudaMemcpyHostToDevice, s));
   for (int i = 0; i < n_systems; ++i) {
+    if (systems[i].d_rate_coef) continue;
     rc = kmc_coef_launch(systems[i], (double2*)dev[i].coef, s);
     if (rc) return rc;
   }
@@ -315,6 +322,16 @@ int pycd_philox_uniforms(uint64_t seed, uint64_t traj, int64_t step0,
   clear_error();
   PYCD_REQUIRE(d_out && n_steps >= 0 && step0 >= 0, "bad arguments");
   return philox_launch(seed, traj, step0, n_steps, d_out, (cudaStream_t)stream);
+}
+
+int pycd_kmc_rate_coefficients(const PycdKmcSystem* system, double* d_out,
+                               void* stream) {
+  clear_error();
+  PYCD_REQUIRE(system && d_out && system->d_lam && system->d_vab &&
+                   system->n_sites > 0 && system->n_slots > 0 && system->kT > 0.0,
+               "pycd_kmc_rate_coefficients: bad arguments");
+  PYCD_REQUIRE(((uintptr_t)d_out & 15) == 0, "d_out must be 16-byte aligned");
+  return kmc_coef_launch(*system, (double2*)d_out, (cudaStream_t)stream);
 }
 
 int pycd_debug_exp(const double* d_x, int64_t n, double* d_ours, double* d_cuda,

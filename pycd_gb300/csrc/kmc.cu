@@ -141,6 +141,10 @@ __device__ void advance_trajectory(const KmcArgs& a, int64_t t, int g,
   const double* __restrict__ A = sy.d_A;
   const double2* __restrict__ coef = sd.coef;
   const double dt_grid = sy.time_interval;
+  if (NP > G * MAXP || NC > G) {  // launch shape too small for this system
+    if (g == 0) st.d_status[t] = PYCD_TRAJ_BAD_INDEX;
+    return;
+  }
 
   int occ = 0;
   double disp0 = 0.0, disp1 = 0.0, disp2 = 0.0;
@@ -158,6 +162,7 @@ __device__ void advance_trajectory(const KmcArgs& a, int64_t t, int g,
   int64_t start_path = st.d_path_index[t];
   double energy = st.d_energy ? st.d_energy[t] : 0.0;
   int64_t ucur = st.d_u_cursor ? st.d_u_cursor[t] : 0;
+  const int64_t step_limit = st.d_step_limit ? st.d_step_limit[t] : INT64_MAX;
   const double* ubase = a.rng.d_uniforms
                             ? a.rng.d_uniforms + (int64_t)t * a.rng.u_stride
                             : nullptr;
@@ -177,6 +182,7 @@ __device__ void advance_trajectory(const KmcArgs& a, int64_t t, int g,
   int64_t pre_base = -(int64_t)G - 1;
 
   for (int64_t it = 0; it < a.max_steps; ++it) {
+    if (step >= step_limit) { status = PYCD_TRAJ_STEP_LIMIT; break; }
     // ---- uniforms (core.py:2799, 2802) --------------------------------
     if (ubase && ucur + 2 > a.rng.u_count) { status = PYCD_TRAJ_NEED_UNIFORMS; break; }
     const int64_t since = step - pre_base;
@@ -191,7 +197,9 @@ __device__ void advance_trajectory(const KmcArgs& a, int64_t t, int g,
         u1 = ok ? ubase[idx] : 0.5;
         u2 = ok ? ubase[idx + 1] : 0.5;
       } else {
-        philox_step_uniforms(a.rng.seed, a.rng.traj_offset + (uint64_t)t,
+        philox_step_uniforms(a.rng.seed,
+                             a.rng.d_traj_ids ? a.rng.d_traj_ids[t]
+                                              : a.rng.traj_offset + (uint64_t)t,
                              (uint64_t)(step + g), u1, u2);
       }
       pre_u1 = u1;

@@ -60,6 +60,20 @@ class KmcTables(object):
         self.time_interval = float(time_interval)
         self.n_path_steps = int(n_path_steps)
 
+    def with_charges(self, q_fixed, n_carriers):
+        """Tables of the same lattice with other fixed charges and carrier
+        count: every device tensor is shared except the new phi_bg."""
+        import copy
+        import torch
+        t = copy.copy(self)
+        t.q_fixed = torch.as_tensor(np.ascontiguousarray(q_fixed, np.float64)).to(self.A.device)
+        t.phi_bg = torch.empty(self.n_sites, dtype=torch.float64, device=self.A.device)
+        nat.check(nat.lib().pycd_potential_gemv(
+            self.A.data_ptr(), self.n_sites, t.q_fixed.data_ptr(),
+            t.phi_bg.data_ptr(), None, nat.stream_handle()))
+        t.n_carriers = int(n_carriers)
+        return t
+
     def descriptor(self):
         d = nat.KmcSystem()
         d.d_A = self.A.data_ptr()
@@ -79,7 +93,21 @@ class KmcTables(object):
         d.kT = self.kT
         d.time_interval = self.time_interval
         d.n_path_steps = self.n_path_steps
+        d.d_rate_coef = nat.ptr(getattr(self, "rate_coef", None))
         return d
+
+    def share_rate_coefficients(self):
+        """Compute the per-slot rate coefficients once on the device so
+        every job built from these tables (``with_charges``) reuses them."""
+        import torch
+        if getattr(self, "rate_coef", None) is None:
+            self.rate_coef = torch.empty(2 * self.n_sites * self.n_slots,
+                                         dtype=torch.float64, device=self.A.device)
+            d = self.descriptor()
+            d.d_rate_coef = None
+            nat.check(nat.lib().pycd_kmc_rate_coefficients(
+                C.byref(d), self.rate_coef.data_ptr(), nat.stream_handle()))
+        return self
 
 
 class KmcBatch(object):
@@ -87,7 +115,8 @@ class KmcBatch(object):
 
     def __init__(self, occupancy, sys_index=None, max_carriers=None,
                  energy0=None, unwrapped_rows=None, step_capacity=0,
-                 energy_grid_rows=None, delg0_grid_rows=None, drift=False):
+                 energy_grid_rows=None, delg0_grid_rows=None, drift=False,
+                 step_limit=None):
         import torch
         dev = _dev()
         occ = np.asarray(occupancy, dtype=np.int32)
@@ -127,6 +156,8 @@ class KmcBatch(object):
                           if step_capacity else None)
         self.step_offset = 0
         self.drift = z64(T, mc, 3) if drift else None
+        self.step_limit = (None if step_limit is None else torch.as_tensor(
+            np.broadcast_to(np.asarray(step_limit, np.int64), (T,)).copy()).to(dev))
 
     def state_struct(self):
         s = nat.KmcState()
@@ -142,6 +173,7 @@ class KmcBatch(object):
         s.d_energy = self.energy.data_ptr()
         s.d_status = self.status.data_ptr()
         s.d_u_cursor = self.u_cursor.data_ptr()
+        s.d_step_limit = nat.ptr(self.step_limit)
         return s
 
     def outputs_struct(self):
@@ -173,32 +205,56 @@ class KmcBatch(object):
 class KmcEngine(object):
     """Launches ``pycd_kmc_advance`` for a set of systems and a batch."""
 
-    def __init__(self, tables, launch=None):
+    def __init__(self, tables, launch=None, share=None):
+        """``share``: another engine whose uploaded system table this one
+        reuses (same systems, its own launch shape)."""
         import torch
-        self.tables = list(tables) if isinstance(tables, (list, tuple)) else [tables]
-        self._descs = (nat.KmcSystem * len(self.tables))(
-            *[t.descriptor() for t in self.tables])
-        nbytes = C.c_size_t()
-        nat.check(nat.lib().pycd_kmc_workspace_size(self._descs, len(self.tables),
-                                                    C.byref(nbytes)))
-        self.workspace = torch.empty(nbytes.value, dtype=torch.uint8,
-                                     device=_dev())
+        if share is not None:
+            if not share._uploaded:
+                share.upload()
+            self.tables, self._descs = share.tables, share._descs
+            self.workspace = share.workspace
+            self._uploaded = True
+        else:
+            self.tables = (list(tables) if isinstance(tables, (list, tuple))
+                           else [tables])
+            self._descs = (nat.KmcSystem * len(self.tables))(
+                *[t.descriptor() for t in self.tables])
+            nbytes = C.c_size_t()
+            nat.check(nat.lib().pycd_kmc_workspace_size(
+                self._descs, len(self.tables), C.byref(nbytes)))
+            self.workspace = torch.empty(nbytes.value, dtype=torch.uint8,
+                                         device=_dev())
+            self._uploaded = False
         self.launch = nat.KmcLaunch()
+        if share is not None:
+            self.launch.max_processes = share.launch.max_processes
+            self.launch.max_carriers = share.launch.max_carriers
         if launch:
             for k, v in launch.items():
                 setattr(self.launch, k, int(v))
-        self._uploaded = False
+
+    def restrict_shape(self, system_ids):
+        """Size the launch for trajectories of these systems only."""
+        t = [self.tables[i] for i in set(int(s) for s in system_ids)]
+        self.launch.max_processes = max(x.n_carriers * x.n_slots for x in t)
+        self.launch.max_carriers = max(x.n_carriers for x in t)
 
     def upload(self, stream=None):
+        keep = (self.launch.max_processes, self.launch.max_carriers)
         nat.check(nat.lib().pycd_kmc_upload_systems(
             self._descs, len(self.tables), self.workspace.data_ptr(),
             self.workspace.numel(), nat.stream_handle(stream),
             C.byref(self.launch)))
+        if keep[0] > 0:  # a restricted shape set before the upload wins
+            self.launch.max_processes, self.launch.max_carriers = keep
         self._uploaded = True
 
     @staticmethod
-    def rng_struct(uniforms=None, u_count=None, seed=0, traj_offset=0):
+    def rng_struct(uniforms=None, u_count=None, seed=0, traj_offset=0,
+                   traj_ids=None):
         r = nat.KmcRng()
+        r.d_traj_ids = nat.ptr(traj_ids)
         if uniforms is not None:
             r.d_uniforms = uniforms.data_ptr()
             r.u_stride = uniforms.shape[-1]

@@ -1,0 +1,303 @@
+"""Continuous-batching KMC job server on one GPU.
+
+Jobs (a lattice supercell, carriers, fixed dopant charges, a step budget and
+a seed) arrive over time.  The server keeps:
+
+* a cache of lattice systems: host set-up, the split-precision Ewald array
+  and the device tables, shared by every job on that supercell and evicted
+  least-recently-used when the HBM budget needs the room;
+* per-job device tables that share the lattice's array, neighbour tables and
+  rate coefficients and add only the job's background potential (dopants);
+* trajectory slots in buckets keyed by (process count, carrier count), each
+  a resident ``KmcBatch`` advanced by the persistent kernel.
+
+Each ``step()`` admits arrived jobs into free slots while the budget allows,
+advances every occupied slot by one chunk, and retires finished jobs.  A
+job's uniforms come from the Philox stream of its job id, so its result is
+the same alone and in any mix.  Latency = retirement time - arrival time.
+"""
+import time
+
+import numpy as np
+
+from . import _native as nat
+from .kmc import KmcBatch, KmcEngine
+
+
+def _pow2(v):
+    p = 1
+    while p < v:
+        p <<= 1
+    return p
+
+
+class LatticeCache(object):
+    """(lattice, cells) -> lattice system with its device array and tables."""
+
+    def __init__(self, budget_bytes, precision="bf16x3", t_final=1e30,
+                 time_interval=1e27):
+        self.budget = float(budget_bytes)
+        self.precision = precision
+        self.t_final, self.time_interval = t_final, time_interval
+        self.entries = {}
+        self.clock = 0
+        self.builds = 0
+
+    def bytes_in_use(self):
+        return sum(e["bytes"] for e in self.entries.values())
+
+    def footprint(self, n_sites, n_slots):
+        # array + neighbour/hop/lambda/V/coefficient tables + per-job potentials
+        return 8.0 * n_sites * n_sites + 8.0 * n_sites * n_slots * 9 + 64.0 * n_sites
+
+    def _evict(self, need):
+        while self.bytes_in_use() + need > self.budget:
+            idle = [(e["used"], k) for k, e in self.entries.items() if e["refs"] == 0]
+            if not idle:
+                return False
+            del self.entries[min(idle)[1]]
+        return True
+
+    def get(self, lattice, cells):
+        """Entry for (lattice, cells), building it if needed; None when the
+        budget cannot hold it now."""
+        from . import workloads as wl
+        key = (lattice, tuple(int(c) for c in cells))
+        self.clock += 1
+        e = self.entries.get(key)
+        if e is not None:
+            e["used"] = self.clock
+            return e
+        per = 12 if lattice == "corundum" else 4
+        n = per * int(np.prod(cells))
+        need = self.footprint(n, 4)
+        if not self._evict(need):
+            return None
+        system = wl.system_for(lattice, cells)
+        A = system.get_precomputed_array_device(self.precision)
+        tables, run = wl.batched_tables(system, A, 1, [], 1.0, self.t_final,
+                                        self.time_interval)
+        tables.share_rate_coefficients()
+        e = {"key": key, "system": system, "tables": tables, "run": run,
+             "n_sites": n, "bytes": self.footprint(n, tables.n_slots), "refs": 0,
+             "used": self.clock}
+        self.entries[key] = e
+        self.builds += 1
+        return e
+
+
+class _Bucket(object):
+    def __init__(self, np_bound, nc_bound, capacity, max_carriers):
+        import torch
+        self.np_bound, self.nc_bound = np_bound, nc_bound
+        self.capacity = capacity
+        self.batch = KmcBatch(np.zeros((capacity, max_carriers), np.int32),
+                              sys_index=np.zeros(capacity, np.int32),
+                              max_carriers=max_carriers,
+                              step_limit=np.zeros(capacity, np.int64))
+        self.batch.status.fill_(nat.TRAJ_DONE)  # free slots are never advanced
+        self.ids = torch.zeros(capacity, dtype=torch.int64, device="cuda")
+        self.free = list(range(capacity - 1, -1, -1))
+        self.jobs = {}  # slot -> job
+        self.engine = None
+
+
+class KmcServer(object):
+    def __init__(self, budget_bytes=150e9, chunk_steps=5000, slots_per_bucket=1024,
+                 precision="bf16x3", seed=0, max_carriers=32):
+        self.cache = LatticeCache(budget_bytes, precision)
+        self.chunk_steps = int(chunk_steps)
+        self.slots = int(slots_per_bucket)
+        self.seed = int(seed)
+        self.max_carriers = int(max_carriers)
+        self.buckets = {}
+        self.pending = []
+        self.done = []
+        self.table = []        # system-table entries (per-job KmcTables)
+        self.table_free = []
+        self.master = None
+        self.table_dirty = True
+        self.t0 = None
+
+    # -- jobs ------------------------------------------------------------
+    def submit(self, job):
+        """job: dict(id, lattice, cells, carriers, dopants, steps, seed,
+        arrival) with `arrival` in seconds since start()."""
+        self.pending.append(job)
+
+    def start(self):
+        self.t0 = time.perf_counter()
+
+    def now(self):
+        return time.perf_counter() - self.t0
+
+    def _bucket(self, n_proc, n_car):
+        key = (_pow2(n_proc), _pow2(n_car))
+        b = self.buckets.get(key)
+        if b is None:
+            b = _Bucket(key[0], key[1], self.slots, self.max_carriers)
+            self.buckets[key] = b
+        return b
+
+    def _admit(self, job):
+        lat = self.cache.get(job["lattice"], job["cells"])
+        if lat is None:
+            return False
+        n = lat["n_sites"]
+        sites = np.random.default_rng(job["seed"]).choice(
+            n, size=job["carriers"] + job["dopants"], replace=False)
+        carriers, dopants = sites[:job["carriers"]], sites[job["carriers"]:]
+        q = np.zeros(n)
+        q[dopants] = 1.0
+        tab = lat["tables"].with_charges(q, job["carriers"])
+        b = self._bucket(job["carriers"] * tab.n_slots, job["carriers"])
+        if not b.free:
+            return False
+        slot = b.free.pop()
+        if self.table_free:
+            ti = self.table_free.pop()
+            self.table[ti] = tab
+        else:
+            ti = len(self.table)
+            self.table.append(tab)
+        lat["refs"] += 1
+        job.update(table_index=ti, lattice_entry=lat, slot=slot, bucket=b,
+                   carrier_sites=carriers, dopant_sites=dopants, admitted=self.now())
+        b.jobs[slot] = job
+        self.table_dirty = True
+        return True
+
+    def _write_slots(self, b, new):
+        import torch
+        if not new:
+            return
+        idx = torch.as_tensor([j["slot"] for j in new], device="cuda")
+        occ = np.zeros((len(new), b.batch.max_carriers), np.int32)
+        for r, j in enumerate(new):
+            occ[r, :len(j["carrier_sites"])] = j["carrier_sites"]
+        bt = b.batch
+        dev = lambda a, dt: torch.as_tensor(np.asarray(a), dtype=dt, device="cuda")
+        bt.occ[idx] = dev(occ, torch.int32)
+        bt.sys_index[idx] = dev([j["table_index"] for j in new], torch.int32)
+        bt.step_limit[idx] = dev([j["steps"] for j in new], torch.int64)
+        b.ids[idx] = dev([j["id"] for j in new], torch.int64)
+        for name in ("time", "energy"):
+            getattr(bt, name)[idx] = 0.0
+        bt.step[idx] = 0
+        bt.path_index[idx] = 1
+        bt.u_cursor[idx] = 0
+        bt.disp[idx] = 0.0
+        bt.last_row[idx] = 0.0
+        bt.status[idx] = nat.TRAJ_RUNNING
+
+    def _upload(self):
+        if not self.table_dirty:
+            return
+        live = [t for t in self.table if t is not None]
+        if not live:
+            return
+        self.master = KmcEngine([t if t is not None else live[0] for t in self.table])
+        self.master.upload()
+        for b in self.buckets.values():
+            b.engine = KmcEngine(None, share=self.master)
+            b.engine.launch.max_processes = b.np_bound
+            b.engine.launch.max_carriers = b.nc_bound
+        self.table_dirty = False
+
+    def step(self):
+        """Admit, advance one chunk, retire.  Returns the jobs retired."""
+        import torch
+        now = self.now()
+        arrived = [j for j in self.pending if j["arrival"] <= now]
+        admitted = []
+        for j in arrived:
+            if self._admit(j):
+                admitted.append(j)
+        for j in admitted:
+            self.pending.remove(j)
+        for b in self.buckets.values():
+            self._write_slots(b, [j for j in admitted if j["bucket"] is b])
+        self._upload()
+        active = [b for b in self.buckets.values() if b.jobs]
+        for b in active:
+            b.engine.advance(b.batch, self.chunk_steps,
+                             b.engine.rng_struct(seed=self.seed, traj_ids=b.ids))
+        retired = []
+        if active:
+            torch.cuda.synchronize()
+            t_ret = self.now()
+            for b in active:
+                st = b.batch.status.cpu().numpy()
+                for slot, job in list(b.jobs.items()):
+                    if st[slot] != nat.TRAJ_RUNNING:
+                        self._retire(b, slot, job, int(st[slot]), t_ret)
+                        retired.append(job)
+        return retired
+
+    def _retire(self, b, slot, job, status, t_ret):
+        bt = b.batch
+        nc = job["carriers"]
+        disp = (bt.last_row[slot] + bt.disp[slot]).cpu().numpy()[:3 * nc]
+        job.update(status=status, finished=t_ret, latency=t_ret - job["arrival"],
+                   steps_done=int(bt.step[slot].item()),
+                   time=float(bt.time[slot].item()),
+                   occupancy=bt.occ[slot].cpu().numpy()[:nc].copy(),
+                   displacement=disp.reshape(nc, 3))
+        bt.status[slot] = nat.TRAJ_DONE
+        del b.jobs[slot]
+        b.free.append(slot)
+        self.table[job["table_index"]] = None
+        self.table_free.append(job["table_index"])
+        job["lattice_entry"]["refs"] -= 1
+        for k in ("bucket", "lattice_entry"):
+            job.pop(k, None)
+        self.done.append(job)
+
+    def busy(self):
+        return bool(self.pending) or any(b.jobs for b in self.buckets.values())
+
+    def run(self, jobs, max_seconds=600.0):
+        """Serve `jobs` (arrival-time ordered) to completion."""
+        for j in jobs:
+            self.submit(j)
+        self.start()
+        steps = 0
+        while self.busy() and self.now() < max_seconds:
+            if not any(b.jobs for b in self.buckets.values()):
+                nxt = min(j["arrival"] for j in self.pending)
+                wait = nxt - self.now()
+                if wait > 0:
+                    time.sleep(min(wait, 0.05))
+            for j in self.step():
+                steps += j["steps_done"]
+        wall = self.now()
+        lat = np.array([j["latency"] for j in self.done]) if self.done else np.zeros(1)
+        return {"jobs": len(self.done), "wall_s": wall, "steps": steps,
+                "steps_per_s": steps / wall if wall else 0.0,
+                "latency_p50_s": float(np.percentile(lat, 50)),
+                "latency_p99_s": float(np.percentile(lat, 99)),
+                "lattice_builds": self.cache.builds,
+                "unfinished": len(self.pending) + sum(len(b.jobs) for b in self.buckets.values())}
+
+
+def poisson_jobs(n_jobs, rate=200.0, seed=0, median_sites=2000, min_sites=300,
+                 max_sites=50000, max_carriers=32, min_steps=10_000,
+                 max_steps=1_000_000, sigma=1.0):
+    """Arrival stream of the serving workload: exponential inter-arrival
+    times at `rate` jobs/s, either lattice, log-normal site counts (clipped),
+    carriers U{1..max_carriers}, dopants U{0..16}, steps U[min, max]."""
+    from . import workloads as wl
+    rng = np.random.default_rng(seed)
+    t = np.cumsum(rng.exponential(1.0 / rate, n_jobs))
+    jobs = []
+    for i in range(n_jobs):
+        lattice = "corundum" if rng.random() < 0.5 else "monoclinic"
+        target = float(np.clip(np.exp(rng.normal(np.log(median_sites), sigma)),
+                               min_sites, max_sites))
+        jobs.append({"id": i, "lattice": lattice,
+                     "cells": wl.supercell_for(lattice, target),
+                     "carriers": int(rng.integers(1, max_carriers + 1)),
+                     "dopants": int(rng.integers(0, 17)),
+                     "steps": int(rng.integers(min_steps, max_steps + 1)),
+                     "seed": int(rng.integers(1 << 31)), "arrival": float(t[i])})
+    return jobs

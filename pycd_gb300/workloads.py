@@ -59,18 +59,68 @@ MONOCLINIC_FRAC = [[0.0, 0.125, 0.5], [0.0, 0.875, 0.5], [0.5, 0.625, 0.5],
 
 
 def monoclinic_params(k_cut):
-    # hop shells: the first two distinct V-V distances of this cell
+    # hop shells: the first three distinct V-V distances of this cell
+    # (one neighbour each at 2.9253, 3.8991 and 3.9249 A), with the corundum
+    # lambda and V_ab
     return dict(
         name="monoclinic", species_types=["electron"],
         species_charge_list={"full": [-1]},
         species_to_element_type_map={"electron": ["V"]},
         charge_types={"full": {"V": 0.0}},
-        neighbor_cutoff_dist={"V:V": [[3.7315, 3.8470]]},
-        neighbor_cutoff_dist_tol={"V:V": [[0.01, 0.01]]},
-        vn=1.85e13, lambda_values={"V:V": [[0.9, 0.9]]},
-        v_ab={"V:V": [[0.2, 0.2]]}, class_list={"V": [1] * 4},
+        neighbor_cutoff_dist={"V:V": [[2.9253, 3.8991, 3.9249]]},
+        neighbor_cutoff_dist_tol={"V:V": [[0.005, 0.005, 0.005]]},
+        vn=1.85e13, lambda_values={"V:V": [[0.9, 0.9, 0.9]]},
+        v_ab={"V:V": [[0.2, 0.2, 0.2]]}, class_list={"V": [1] * 4},
         element_type_delimiter=":", dielectric_constant=12.0,
         alpha=0.2, r_cut=6.4, k_cut=k_cut)
+
+
+def supercell_for(lattice, target_sites):
+    """(s, s, t) supercell nearest to `target_sites` whose inscribed sphere
+    holds the 6.4 A real-space cutoff (s_a = s_b keeps the Ewald cell equal to
+    the supercell)."""
+    per, s_min, t_min = (12, 3, 1) if lattice == "corundum" else (4, 3, 3)
+    best = None
+    for s in range(s_min, 200):
+        if per * s * s * t_min > 4 * target_sites:
+            break
+        t = max(t_min, int(round(target_sites / (per * s * s))))
+        n = per * s * s * t
+        cand = (abs(np.log(n / target_sites)), (s, s, t))
+        if best is None or cand < best:
+            best = cand
+    return best[1]
+
+
+def system_for(lattice, cells):
+    if lattice == "corundum":
+        return corundum(cells)
+    return monoclinic(cells, 0.9164, neighbor_list=True)
+
+
+def uneven_systems(seed=2025, n_systems=64, n_traj=2048, min_sites=300,
+                   max_sites=20000):
+    """The uneven batch: seeded lattices, supercells with log-uniform site
+    counts, carriers U{1..16}, dopants U{0..16}, and trajectories spread over
+    the systems with step budgets U[1e4, 1e6]."""
+    rng = np.random.default_rng(seed)
+    specs = []
+    for i in range(n_systems):
+        lattice = "corundum" if rng.random() < 0.5 else "monoclinic"
+        target = float(np.exp(rng.uniform(np.log(min_sites), np.log(max_sites))))
+        specs.append({"lattice": lattice, "cells": supercell_for(lattice, target),
+                      "carriers": int(rng.integers(1, 17)),
+                      "dopants": int(rng.integers(0, 17)), "seed": int(seed + i)})
+    traj_sys = np.sort(rng.integers(0, n_systems, n_traj))
+    steps = rng.integers(10_000, 1_000_001, n_traj)
+    return specs, traj_sys, steps
+
+
+def sites_for(n_sites, n_carriers, n_dopants, seed):
+    """Distinct carrier and dopant sites from `seed`."""
+    s = np.random.default_rng(seed).choice(n_sites, size=n_carriers + n_dopants,
+                                           replace=False)
+    return s[:n_carriers].tolist(), s[n_carriers:].tolist()
 
 
 def _material(params, lattice, types_, counts, frac):

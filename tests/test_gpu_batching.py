@@ -1,0 +1,84 @@
+"""GPU: uneven multi-system batches (buckets, autotuned shapes) and the
+continuous-batching server: every trajectory's result equals the same
+trajectory advanced alone."""
+import numpy as np
+import pytest
+
+from pycd_gb300 import _native as nat
+from pycd_gb300 import workloads as wl
+from pycd_gb300.batch import BatchedKmc
+
+pytestmark = pytest.mark.gpu
+
+
+def _tables(lattice, cells, n_carriers, dopants, precision="fp64"):
+    system = wl.system_for(lattice, cells)
+    A = system.get_precomputed_array_device(precision)
+    base, _ = wl.batched_tables(system, A, 1, [], 1.0, 1e30, 1e27)
+    base.share_rate_coefficients()
+    n = system.neighbors.num_system_elements
+    q = np.zeros(n)
+    q[dopants] = 1.0
+    return base.with_charges(q, n_carriers), n
+
+
+def test_uneven_buckets_equal_alone_runs(cuda_ready):
+    import torch
+    specs = [("corundum", (3, 3, 1), 1, [5]), ("monoclinic", (3, 3, 3), 3, []),
+             ("corundum", (3, 3, 2), 6, [1, 2, 3]), ("monoclinic", (4, 4, 3), 12, [7])]
+    tables = [_tables(*s)[0] for s in specs]
+    rng = np.random.default_rng(0)
+    occ, sys_index, limits = [], [], []
+    for t in range(40):
+        s = t % len(specs)
+        n = tables[s].n_sites
+        row = np.zeros(16, np.int32)
+        row[:tables[s].n_carriers] = rng.choice(n, tables[s].n_carriers, replace=False)
+        occ.append(row)
+        sys_index.append(s)
+        limits.append(int(rng.integers(500, 3000)))
+    bk = BatchedKmc(tables, np.stack(occ), sys_index=sys_index, seed=77,
+                    chunk_steps=1000, step_limit=limits, autotune=True)
+    assert len(bk.buckets) >= 3
+    bk.run(3000)
+    torch.cuda.synchronize()
+    assert (bk.gather("status").cpu().numpy() == nat.TRAJ_STEP_LIMIT).all()
+    assert (bk.gather("step").cpu().numpy() == np.array(limits)).all()
+    for t in (0, 1, 2, 3, 17, 38):
+        s = sys_index[t]
+        alone = BatchedKmc(tables[s], occ[t][None, :tables[s].n_carriers], seed=77,
+                           chunk_steps=limits[t], step_limit=limits[t],
+                           traj_offset=t, use_graph=False)
+        alone.run(limits[t])
+        torch.cuda.synchronize()
+        nc = tables[s].n_carriers
+        assert np.array_equal(alone.batch.occ.cpu().numpy()[0, :nc],
+                              bk.gather("occ").cpu().numpy()[t, :nc])
+        assert alone.batch.time.item() == bk.gather("time")[t].item()
+
+
+def test_server_results_equal_alone_runs(cuda_ready):
+    import torch
+    from pycd_gb300.serving import KmcServer, poisson_jobs
+    jobs = poisson_jobs(24, rate=400.0, seed=5, median_sites=400, max_sites=2000,
+                        max_carriers=8, min_steps=2000, max_steps=20000)
+    server = KmcServer(budget_bytes=20e9, chunk_steps=1500, slots_per_bucket=8, seed=9)
+    stats = server.run([dict(j) for j in jobs], max_seconds=300)
+    assert stats["jobs"] == 24 and stats["unfinished"] == 0
+    assert stats["latency_p99_s"] >= stats["latency_p50_s"] > 0
+    for j in server.done[:6]:
+        assert j["status"] == nat.TRAJ_STEP_LIMIT and j["steps_done"] == j["steps"]
+        lat = server.cache.get(j["lattice"], j["cells"])
+        q = np.zeros(lat["n_sites"])
+        q[j["dopant_sites"]] = 1.0
+        tab = lat["tables"].with_charges(q, j["carriers"])
+        alone = BatchedKmc(tab, np.asarray(j["carrier_sites"])[None, :], seed=9,
+                           chunk_steps=j["steps"], step_limit=j["steps"],
+                           traj_offset=j["id"], use_graph=False)
+        alone.run(j["steps"])
+        torch.cuda.synchronize()
+        nc = j["carriers"]
+        assert np.array_equal(alone.batch.occ.cpu().numpy()[0, :nc], j["occupancy"])
+        assert alone.batch.time.item() == j["time"]
+        disp = (alone.batch.last_row + alone.batch.disp).cpu().numpy()[0, :3 * nc]
+        assert np.array_equal(disp.reshape(nc, 3), j["displacement"])
