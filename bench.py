@@ -456,12 +456,20 @@ def serving_bench(args):
     server = KmcServer(budget_bytes=150e9, chunk_steps=args.chunk, precision="bf16x3",
                        seed=SEED)
     t0 = time.perf_counter()
-    for j in jobs:  # warm the lattice cache: arrays are shared across jobs
-        server.cache.get(j["lattice"], j["cells"])
+    keys = sorted({(j["lattice"], tuple(j["cells"])) for j in jobs},
+                  key=lambda k: np.prod(k[1]))
+    for i, k in enumerate(keys):  # warm the lattice cache (arrays are shared)
+        server.cache.get(*k)
+        if i % 8 == 0:
+            print(f"[serving] lattice {i + 1}/{len(keys)} {k} "
+                  f"{time.perf_counter() - t0:.1f}s", file=sys.stderr, flush=True)
     torch.cuda.synchronize()
+    torch.cuda.empty_cache()
     warm_s = time.perf_counter() - t0
+    print(f"[serving] cache warm in {warm_s:.1f}s, {server.cache.bytes_in_use() / 1e9:.1f} GB",
+          file=sys.stderr, flush=True)
     with ClockSampler(0) as clocks:
-        stats = server.run([dict(j) for j in jobs])
+        stats = server.run([dict(j) for j in jobs], max_seconds=420.0, log=sys.stderr)
     # alone vs in the mix
     rng = np.random.default_rng(3)
     same = []
@@ -527,6 +535,7 @@ def main():
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     from pycd_gb300 import _native as nat
     from pycd_gb300.batch import BatchedKmc, run_batched
+    from pycd_gb300.replicas import stream_offset
     nat.require_device()
     system, A, tables, run, dopants, occ = build_workload(rank, args.traj)
     launch = {}
@@ -536,8 +545,8 @@ def main():
         launch["warps_per_block"] = args.warps
     # launch shape: autotuned (untimed) unless given; it never changes events
     bk = BatchedKmc(tables, occ, seed=SEED, chunk_steps=args.chunk,
-                    traj_offset=rank * args.traj, launch=launch,
-                    autotune=not (args.lanes or args.warps))
+                    traj_offset=stream_offset(rank, args.traj), launch=launch,
+                    autotune=0 if (args.lanes or args.warps) else 2000)
     tuned = {"lanes_per_traj": bk.buckets[0].engine.launch.lanes_per_traj,
              "warps_per_block": bk.buckets[0].engine.launch.warps_per_block}
     flush = torch.empty(256 * 2 ** 20, dtype=torch.uint8, device="cuda")
@@ -564,14 +573,8 @@ def main():
     kernel_ms = [a.elapsed_time(b) for a, b in ev]
     steps_done = bk.batch.step.sum().item() - steps0
     status = bk.status_counts()
-    elapsed = torch.tensor([wall, steps_done], dtype=torch.float64, device="cuda")
-    if world > 1:
-        gathered = [torch.zeros_like(elapsed) for _ in range(world)]
-        dist.all_gather(gathered, elapsed)
-        wall_max = max(float(g[0]) for g in gathered)
-        total_steps = sum(float(g[1]) for g in gathered)
-    else:
-        wall_max, total_steps = wall, float(steps_done)
+    from pycd_gb300 import replicas
+    wall_max, total_steps = replicas.aggregate(wall, steps_done, device="cuda")
     value = total_steps / wall_max
 
     # plain one-trajectory form (same kernel, same events)

@@ -166,6 +166,14 @@ PYCD_API int pycd_potential_gemv(const double* d_A, int64_t n_sites,
                         const double* d_q, double* d_phi, double* d_energy,
                         void* stream);
 
+/* phi[i] = sum_j q[j] A[idx[j]][i] for m charged sites (dopants on an
+ * otherwise neutral lattice): the same background potential as
+ * pycd_potential_gemv when q is zero elsewhere, reading m rows of the
+ * symmetric array instead of all N^2 entries.                              */
+PYCD_API int pycd_potential_sparse(const double* d_A, int64_t n_sites,
+                                   const int32_t* d_idx, const double* d_q,
+                                   int32_t m, double* d_phi, void* stream);
+
 /* ------------------------------------------------------------------------ */
 /* KMC                                                                       */
 /* ------------------------------------------------------------------------ */

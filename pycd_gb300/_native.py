@@ -127,6 +127,8 @@ _PROTOS = {
     "pycd_philox_uniforms": (C.c_int, [C.c_uint64, C.c_uint64, C.c_int64,
                                        C.c_int64, C.c_void_p, C.c_void_p]),
     "pycd_kmc_rate_coefficients": (C.c_int, [P(KmcSystem), C.c_void_p, C.c_void_p]),
+    "pycd_potential_sparse": (C.c_int, [C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p,
+                                        C.c_int32, C.c_void_p, C.c_void_p]),
     "pycd_debug_exp": (C.c_int, [C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p,
                                  C.c_void_p]),
 }

@@ -84,8 +84,8 @@ class BatchedKmc(object):
             pos += len(idx)
         self.graph = None
         self.stream = torch.cuda.Stream()
-        if autotune:
-            self.autotune()
+        if autotune:  # True, or the probe length in steps
+            self.autotune(probe_steps=int(autotune) if int(autotune) > 1 else 200)
 
     def _rng(self, bk):
         return bk.engine.rng_struct(seed=self.seed, traj_ids=bk.ids)

@@ -38,6 +38,8 @@ int ewald_build(const PycdEwaldDesc* d, int mode, double* out, void* ws,
                 float* fourier_ms);
 int potential_gemv(const double* A, int64_t n, const double* q, double* phi,
                    double* energy, cudaStream_t s);
+int potential_sparse(const double* A, int64_t n, const int32_t* idx,
+                     const double* q, int32_t m, double* phi, cudaStream_t s);
 
 }  // namespace pycd
 
@@ -322,6 +324,13 @@ int pycd_philox_uniforms(uint64_t seed, uint64_t traj, int64_t step0,
   clear_error();
   PYCD_REQUIRE(d_out && n_steps >= 0 && step0 >= 0, "bad arguments");
   return philox_launch(seed, traj, step0, n_steps, d_out, (cudaStream_t)stream);
+}
+
+int pycd_potential_sparse(const double* d_A, int64_t n_sites,
+                          const int32_t* d_idx, const double* d_q, int32_t m,
+                          double* d_phi, void* stream) {
+  clear_error();
+  return potential_sparse(d_A, n_sites, d_idx, d_q, m, d_phi, (cudaStream_t)stream);
 }
 
 int pycd_kmc_rate_coefficients(const PycdKmcSystem* system, double* d_out,

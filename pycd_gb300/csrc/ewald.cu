@@ -313,6 +313,29 @@ __global__ void gemv_rows_kernel(const double* __restrict__ A, int64_t n,
   if (lane == 0) phi[row] = s;
 }
 
+// phi[i] = sum_j q_j A[idx_j][i] for a few charged sites idx_j: the array is
+// symmetric, so the columns A[:, idx_j] are read as rows (coalesced);
+// charges are added in the given order.
+__global__ void sparse_potential_kernel(const double* __restrict__ A, int64_t n,
+                                        const int32_t* __restrict__ idx,
+                                        const double* __restrict__ q, int32_t m,
+                                        double* __restrict__ phi) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double s = 0.0;
+  for (int32_t j = 0; j < m; ++j) s = fma(q[j], A[(int64_t)idx[j] * n + i], s);
+  phi[i] = s;
+}
+
+int potential_sparse(const double* A, int64_t n, const int32_t* idx,
+                     const double* q, int32_t m, double* phi, cudaStream_t s) {
+  PYCD_REQUIRE(A && phi && n > 0 && m >= 0 && (m == 0 || (idx && q)),
+               "potential_sparse: bad arguments");
+  sparse_potential_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(A, n, idx, q, m, phi);
+  PYCD_CUDA(cudaGetLastError());
+  return PYCD_OK;
+}
+
 __global__ void dot_kernel(const double* __restrict__ a,
                            const double* __restrict__ b, int64_t n,
                            double* __restrict__ out) {

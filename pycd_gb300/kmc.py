@@ -66,11 +66,21 @@ class KmcTables(object):
         import copy
         import torch
         t = copy.copy(self)
-        t.q_fixed = torch.as_tensor(np.ascontiguousarray(q_fixed, np.float64)).to(self.A.device)
-        t.phi_bg = torch.empty(self.n_sites, dtype=torch.float64, device=self.A.device)
-        nat.check(nat.lib().pycd_potential_gemv(
-            self.A.data_ptr(), self.n_sites, t.q_fixed.data_ptr(),
-            t.phi_bg.data_ptr(), None, nat.stream_handle()))
+        q = np.ascontiguousarray(q_fixed, np.float64)
+        dev = self.A.device
+        t.q_fixed = torch.as_tensor(q).to(dev)
+        t.phi_bg = torch.empty(self.n_sites, dtype=torch.float64, device=dev)
+        nz = np.nonzero(q)[0]
+        if len(nz) <= 64:  # a few charged sites: gather their rows
+            d_idx = torch.as_tensor(nz.astype(np.int32)).to(dev)
+            d_q = torch.as_tensor(q[nz]).to(dev)
+            nat.check(nat.lib().pycd_potential_sparse(
+                self.A.data_ptr(), self.n_sites, nat.ptr(d_idx), nat.ptr(d_q),
+                len(nz), t.phi_bg.data_ptr(), nat.stream_handle()))
+        else:
+            nat.check(nat.lib().pycd_potential_gemv(
+                self.A.data_ptr(), self.n_sites, t.q_fixed.data_ptr(),
+                t.phi_bg.data_ptr(), None, nat.stream_handle()))
         t.n_carriers = int(n_carriers)
         return t
 

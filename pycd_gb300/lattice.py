@@ -208,7 +208,8 @@ class Neighbors(object):
         return self.apply_minimum_image_convention_vectorized(
             np.asarray(displacement_vector, dtype=np.float64)[None, :])[0]
 
-    def apply_minimum_image_convention_vectorized(self, displacement_vectors):
+    def apply_minimum_image_convention_vectorized(self, displacement_vectors,
+                                                  tie_check_below=None):
         """Minimum-image vectors for an (n, 3) array.
 
         Candidates are the rounded fractional image and its 26 neighbours in
@@ -216,6 +217,8 @@ class Neighbors(object):
         wins.  Distances are compared vectorised, then every row whose
         decision is within rounding of a tie is redone with the per-vector
         norm the reference uses, so the chosen image is the reference's.
+        ``tie_check_below``: only rows shorter than this are redone (callers
+        that only keep short vectors, such as the hop-neighbour windows).
         """
         M = self.simulation_cell_matrix
         D = np.asarray(displacement_vectors, dtype=np.float64)
@@ -234,6 +237,8 @@ class Neighbors(object):
             best = np.where(better[:, None], cand, best)
             best_d = np.where(better, cd, best_d)
         close = second_gap <= self._TIE_RTOL * np.maximum(best_d, 1e-300)
+        if tie_check_below is not None:
+            close &= best_d <= tie_check_below
         for i in np.nonzero(close)[0]:
             best[i] = self._min_image_exact(D[i])
         return best
@@ -251,6 +256,14 @@ class Neighbors(object):
             if cd < best_d:
                 best_d, best = cd, cand
         return best
+
+    def _max_hop(self):
+        """Longest hop-window edge over all element pairs (bohr), with slack."""
+        m = self.material
+        edges = [d + t for key, cls in m.neighbor_cutoff_dist.items()
+                 for ci, ds in enumerate(cls) for d, t in
+                 zip(ds, m.neighbor_cutoff_dist_tol[key][ci]) if d is not None]
+        return (max(edges) if edges else 0.0) * (1 + 1e-6)
 
     # -- index maps (PyCD/core.py:363-466) ---------------------------------
     def get_system_element_index(self, system_size, quantum_indices):
@@ -313,7 +326,8 @@ class Neighbors(object):
             else:
                 D = (nb_coords[None, :, :] - c_coords[s:e, None, :])
                 mi = self.apply_minimum_image_convention_vectorized(
-                    D.reshape(-1, 3)).reshape(e - s, len(nb_coords), 3)
+                    D.reshape(-1, 3), tie_check_below=self._max_hop()
+                ).reshape(e - s, len(nb_coords), 3)
                 dist = np.sqrt(np.einsum("ijk,ijk->ij", mi, mi))
                 if _cache is not None:
                     _cache[(s, e)] = (mi, dist)
@@ -369,7 +383,8 @@ class Neighbors(object):
         uc_idx = idx[:per_cell]
         D = coords[idx][None, :, :] - coords[uc_idx][:, None, :]
         mi = self.apply_minimum_image_convention_vectorized(
-            D.reshape(-1, 3)).reshape(per_cell, n_idx, 3)
+            D.reshape(-1, 3), tie_check_below=hi * (1 + 1e-6)
+        ).reshape(per_cell, n_idx, 3)
         dist = np.sqrt(np.einsum("ijk,ijk->ij", mi, mi))
         tol = 1e-9 * hi
         if np.any((np.abs(dist - lo) <= tol) | (np.abs(dist - hi) <= tol)):
@@ -399,7 +414,8 @@ class Neighbors(object):
             ci = idx[centres]
             D = coords[flat] - coords[ci][:, None, :]
             v = self.apply_minimum_image_convention_vectorized(
-                D.reshape(-1, 3)).reshape(flat.shape + (3,))
+                D.reshape(-1, 3), tie_check_below=hi * (1 + 1e-6)
+            ).reshape(flat.shape + (3,))
             dd = np.sqrt(np.einsum("ijk,ijk->ij", v, v))
             if not np.all((lo < dd) & (dd <= hi)):
                 return None

@@ -256,13 +256,20 @@ class KmcServer(object):
     def busy(self):
         return bool(self.pending) or any(b.jobs for b in self.buckets.values())
 
-    def run(self, jobs, max_seconds=600.0):
-        """Serve `jobs` (arrival-time ordered) to completion."""
+    def run(self, jobs, max_seconds=600.0, log=None):
+        """Serve `jobs` (arrival-time ordered) to completion; `log` is an
+        optional file for a progress line every ~2 s."""
         for j in jobs:
             self.submit(j)
         self.start()
         steps = 0
+        next_log = 2.0
         while self.busy() and self.now() < max_seconds:
+            if log is not None and self.now() >= next_log:
+                next_log += 2.0
+                active = sum(len(b.jobs) for b in self.buckets.values())
+                print(f"[serving] t={self.now():.1f}s done={len(self.done)} "
+                      f"active={active} pending={len(self.pending)}", file=log, flush=True)
             if not any(b.jobs for b in self.buckets.values()):
                 nxt = min(j["arrival"] for j in self.pending)
                 wait = nxt - self.now()
@@ -282,18 +289,25 @@ class KmcServer(object):
 
 def poisson_jobs(n_jobs, rate=200.0, seed=0, median_sites=2000, min_sites=300,
                  max_sites=50000, max_carriers=32, min_steps=10_000,
-                 max_steps=1_000_000, sigma=1.0):
+                 max_steps=1_000_000, sigma=1.0, size_grid=24):
     """Arrival stream of the serving workload: exponential inter-arrival
     times at `rate` jobs/s, either lattice, log-normal site counts (clipped),
-    carriers U{1..max_carriers}, dopants U{0..16}, steps U[min, max]."""
+    carriers U{1..max_carriers}, dopants U{0..16}, steps U[min, max].
+    With ``size_grid`` the drawn site count is snapped to the nearest of that
+    many log-spaced sizes, so that jobs share a catalogue of lattices whose
+    arrays stay cached (otherwise nearly every job needs its own array)."""
     from . import workloads as wl
     rng = np.random.default_rng(seed)
     t = np.cumsum(rng.exponential(1.0 / rate, n_jobs))
+    grid = (np.exp(np.linspace(np.log(min_sites), np.log(max_sites), size_grid))
+            if size_grid else None)
     jobs = []
     for i in range(n_jobs):
         lattice = "corundum" if rng.random() < 0.5 else "monoclinic"
         target = float(np.clip(np.exp(rng.normal(np.log(median_sites), sigma)),
                                min_sites, max_sites))
+        if grid is not None:
+            target = float(grid[np.argmin(np.abs(np.log(grid / target)))])
         jobs.append({"id": i, "lattice": lattice,
                      "cells": wl.supercell_for(lattice, target),
                      "carriers": int(rng.integers(1, max_carriers + 1)),
