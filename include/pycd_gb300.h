@@ -230,6 +230,16 @@ typedef struct PycdKmcState {
   int32_t* d_status;            /* T: PycdTrajStatus                          */
   int64_t* d_u_cursor;          /* T: uniforms consumed (injected mode)      */
   const int64_t* d_step_limit;  /* T: stop after this many steps, or NULL    */
+  /* Carrier-potential sums per process p: sum_c' A[n_p, occ_c'] and
+   * sum_c' A[o_p, occ_c'] (T x csum_stride doubles, first half / second
+   * half).  After each event only the moving carrier's delta is added
+   * (2 gathers per process instead of n_carriers); every csum_refresh steps
+   * (global step index) all sums are recomputed exactly.  csum_stride must
+   * be >= 2 * max processes.  Results are the same for any launch shape or
+   * chunking at a given csum_refresh (a power of two).                     */
+  double* d_csum;
+  int32_t csum_stride;
+  int32_t csum_refresh;
 } PycdKmcState;
 
 /* Optional per-trajectory outputs.  Each pointer may be NULL.               */

@@ -73,7 +73,8 @@ class KmcState(C.Structure):
                 ("d_path_index", C.c_void_p), ("d_disp", C.c_void_p),
                 ("d_last_row", C.c_void_p), ("d_energy", C.c_void_p),
                 ("d_status", C.c_void_p), ("d_u_cursor", C.c_void_p),
-                ("d_step_limit", C.c_void_p)]
+                ("d_step_limit", C.c_void_p), ("d_csum", C.c_void_p),
+                ("csum_stride", C.c_int32), ("csum_refresh", C.c_int32)]
 
 
 class KmcOutputs(C.Structure):

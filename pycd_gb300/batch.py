@@ -71,6 +71,7 @@ class BatchedKmc(object):
             sub_occ = np.zeros((len(idx), mc), np.int32)
             sub_occ[:, :occ.shape[1]] = occ[idx]
             b = KmcBatch(sub_occ, sys_index=sys_index[idx], max_carriers=mc,
+                         max_processes=int(n_proc.max()),
                          unwrapped_rows=rows, step_capacity=step_capacity,
                          step_limit=None if limits is None else limits[idx])
             eng = KmcEngine(None, launch, share=self.master)

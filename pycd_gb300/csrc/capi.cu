@@ -220,6 +220,9 @@ static int validate_state(const PycdKmcState* st, const PycdKmcOutputs* out,
                "u_stride < u_count");
   PYCD_REQUIRE(!out->d_step_time == !out->d_step_proc,
                "d_step_time and d_step_proc go together");
+  PYCD_REQUIRE(!st->d_csum || (st->csum_refresh > 0 &&
+                               (st->csum_refresh & (st->csum_refresh - 1)) == 0),
+               "csum_refresh must be a positive power of two");
   return PYCD_OK;
 }
 
@@ -287,6 +290,9 @@ int pycd_kmc_advance_uploaded(int32_t n_systems, const PycdKmcState* state,
                "launch shape maxima missing (call pycd_kmc_upload_systems)");
   PYCD_REQUIRE(launch->max_carriers <= state->max_carriers,
                "carriers exceed the state stride");
+  PYCD_REQUIRE(!state->d_csum || state->csum_stride >= 2 * launch->max_processes,
+               "csum_stride %d below 2 x %d processes", state->csum_stride,
+               launch->max_processes);
   KmcArgs a;
   a.systems = (const KmcSysDev*)((const char*)d_workspace + 256);
   a.n_systems = n_systems;

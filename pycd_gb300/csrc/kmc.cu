@@ -117,6 +117,129 @@ struct LocalTree {
   __device__ __forceinline__ double total() const { return node[1]; }
 };
 
+// Per-process cache of one lane: geometry, constants that change only when
+// the process' own carrier moves, and the two carrier-potential sums.
+template <int MAXP>
+struct ProcCache {
+  int oldsite[MAXP], newsite[MAXP], carrier[MAXP];
+  double dphi[MAXP], t02[MAXP], de[MAXP], lam[MAXP], c1[MAXP], c0[MAXP];
+  double P[MAXP], Q[MAXP];
+  bool valid[MAXP];
+};
+
+// (Re)build geometry and constants of this lane's processes that belong to
+// carrier `only` (all when only < 0).  Every lane runs the shuffles.
+// Returns true when an index is out of range (no gather was issued with it).
+template <int G, int MAXP>
+__device__ __forceinline__ bool setup_processes(const PycdKmcSystem& sy,
+                                                const double2* __restrict__ coef,
+                                                int g, unsigned gmask, int occ,
+                                                int only, ProcCache<MAXP>& pc) {
+  const int64_t N = sy.n_sites;
+  const int S = sy.n_slots;
+  const int NP = sy.n_carriers * S;
+  const double* __restrict__ A = sy.d_A;
+  bool bad = false;
+#pragma unroll
+  for (int j = 0; j < MAXP; ++j) {
+    const int p = g * MAXP + j;
+    const bool v = p < NP;
+    const int c = v ? p / S : 0;
+    const int o = gshfl<G>(gmask, occ, c);
+    pc.valid[j] = v;
+    if (v && (only < 0 || c == only)) {
+      pc.carrier[j] = c;
+      const int s = p - c * S;
+      const int n = sy.d_nbr[(int64_t)o * S + s];
+      pc.oldsite[j] = o;
+      pc.newsite[j] = n;
+      if (n < 0 || n >= N || o < 0 || o >= N) {
+        bad = true;
+        continue;
+      }
+      const int64_t slot = (int64_t)o * S + s;
+      pc.dphi[j] = dsub(__ldg(sy.d_phi_bg + n), __ldg(sy.d_phi_bg + o));
+      pc.t02[j] = dsub(__ldg(A + (int64_t)o * N + o), __ldg(A + (int64_t)o * N + n));
+      pc.de[j] = dsub(__ldg(sy.d_e_rel + n), __ldg(sy.d_e_rel + o));
+      pc.lam[j] = __ldg(sy.d_lam + slot);
+      const double2 cf = __ldg(coef + slot);
+      pc.c1[j] = cf.x;
+      pc.c0[j] = cf.y;
+    } else if (!v) {
+      pc.carrier[j] = -1;
+      pc.oldsite[j] = 0;
+      pc.newsite[j] = 0;
+    }
+  }
+  return bad;
+}
+
+// Carriers in blocks of U: all loads of a block are issued before any of
+// their sums, so a step waits for a few memory round trips instead of one
+// per carrier; the additions keep carrier order (identical results for any U).
+template <int G, int MAXP, int U>
+__device__ __forceinline__ void fresh_sums_block(const double* __restrict__ A,
+                                                 int64_t N, int NC, unsigned gmask,
+                                                 int occ, const bool (&doit)[MAXP],
+                                                 const bool (&ownq)[MAXP],
+                                                 ProcCache<MAXP>& pc) {
+  for (int c0 = 0; c0 < NC; c0 += U) {
+    int sc[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) sc[u] = gshfl<G>(gmask, occ, min(c0 + u, NC - 1));
+#pragma unroll
+    for (int j = 0; j < MAXP; ++j) {
+      if (doit[j]) {
+        const double* rn = A + (int64_t)pc.newsite[j] * N;
+        const double* ro = A + (int64_t)pc.oldsite[j] * N;
+        double vn[U], vo[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          vn[u] = (c0 + u < NC) ? __ldg(rn + sc[u]) : 0.0;
+          vo[u] = (ownq[j] && c0 + u < NC) ? __ldg(ro + sc[u]) : 0.0;
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          if (c0 + u < NC) {
+            pc.P[j] = dadd(pc.P[j], vn[u]);
+            if (ownq[j]) pc.Q[j] = dadd(pc.Q[j], vo[u]);
+          }
+        }
+      }
+    }
+  }
+}
+
+// Exact carrier sums for this lane's processes of carrier `only` (all when
+// only < 0): P = sum_c' A[n, occ_c'], Q = sum_c' A[o, occ_c'] in carrier
+// order; Q is evaluated once per carrier and shared by its processes.
+template <int G, int MAXP>
+__device__ __forceinline__ void fresh_sums(const PycdKmcSystem& sy, int g,
+                                           unsigned gmask, int occ, int only,
+                                           ProcCache<MAXP>& pc) {
+  const int64_t N = sy.n_sites;
+  const int NC = sy.n_carriers;
+  const double* __restrict__ A = sy.d_A;
+  bool doit[MAXP], ownq[MAXP];
+#pragma unroll
+  for (int j = 0; j < MAXP; ++j) {
+    doit[j] = pc.valid[j] && (only < 0 || pc.carrier[j] == only);
+    ownq[j] = doit[j] && (j == 0 || pc.carrier[j] != pc.carrier[j > 0 ? j - 1 : 0] ||
+                          !doit[j > 0 ? j - 1 : 0]);
+    if (doit[j]) {
+      pc.P[j] = 0.0;
+      if (ownq[j]) pc.Q[j] = 0.0;
+    }
+  }
+  if (NC <= 4)
+    fresh_sums_block<G, MAXP, 4>(A, N, NC, gmask, occ, doit, ownq, pc);
+  else
+    fresh_sums_block<G, MAXP, 8>(A, N, NC, gmask, occ, doit, ownq, pc);
+#pragma unroll
+  for (int j = 1; j < MAXP; ++j)
+    if (doit[j] && !ownq[j]) pc.Q[j] = pc.Q[j - 1];
+}
+
 // One group of G lanes advances one trajectory by up to max_steps steps.
 template <int G, int MAXP>
 __device__ void advance_trajectory(const KmcArgs& a, int64_t t, int g,
@@ -141,10 +264,15 @@ __device__ void advance_trajectory(const KmcArgs& a, int64_t t, int g,
   const double* __restrict__ A = sy.d_A;
   const double2* __restrict__ coef = sd.coef;
   const double dt_grid = sy.time_interval;
-  if (NP > G * MAXP || NC > G) {  // launch shape too small for this system
+  if (NP > G * MAXP || NC > G || (st.d_csum && 2 * NP > st.csum_stride)) {
+    // launch shape or carrier-sum storage too small for this system
     if (g == 0) st.d_status[t] = PYCD_TRAJ_BAD_INDEX;
     return;
   }
+  // refresh period of the carrier sums (every step without storage)
+  const int64_t R = (st.d_csum && st.csum_refresh > 0) ? st.csum_refresh : 1;
+  double* csum = st.d_csum ? st.d_csum + t * (int64_t)st.csum_stride : nullptr;
+  const int half = st.csum_stride / 2;
 
   int occ = 0;
   double disp0 = 0.0, disp1 = 0.0, disp2 = 0.0;
@@ -166,6 +294,8 @@ __device__ void advance_trajectory(const KmcArgs& a, int64_t t, int g,
   const double* ubase = a.rng.d_uniforms
                             ? a.rng.d_uniforms + (int64_t)t * a.rng.u_stride
                             : nullptr;
+  const uint64_t stream_id = a.rng.d_traj_ids ? a.rng.d_traj_ids[t]
+                                              : a.rng.traj_offset + (uint64_t)t;
   const int64_t n_path = sy.n_path_steps;
   const int64_t row_len = 3 * (int64_t)MC;
   double* unw = a.out.d_unwrapped
@@ -180,6 +310,23 @@ __device__ void advance_trajectory(const KmcArgs& a, int64_t t, int g,
   // uniforms of steps pre_base + g, prepared G at a time
   double pre_u1 = 0.0, pre_lu2 = 0.0;
   int64_t pre_base = -(int64_t)G - 1;
+
+  // ---- process cache: geometry, constants, carrier sums ----------------
+  ProcCache<MAXP> pc;
+  bool bad = setup_processes<G, MAXP>(sy, coef, g, gmask, occ, -1, pc);
+  if (__ballot_sync(gmask, bad) & gmask) {
+    if (g == 0) st.d_status[t] = PYCD_TRAJ_BAD_INDEX;
+    return;
+  }
+  if (csum && (step & (R - 1)) != 0) {
+#pragma unroll
+    for (int j = 0; j < MAXP; ++j) {
+      const int p = g * MAXP + j;
+      if (pc.valid[j]) { pc.P[j] = csum[p]; pc.Q[j] = csum[half + p]; }
+    }
+  } else {
+    fresh_sums<G, MAXP>(sy, g, gmask, occ, -1, pc);
+  }
 
   for (int64_t it = 0; it < a.max_steps; ++it) {
     if (step >= step_limit) { status = PYCD_TRAJ_STEP_LIMIT; break; }
@@ -197,10 +344,7 @@ __device__ void advance_trajectory(const KmcArgs& a, int64_t t, int g,
         u1 = ok ? ubase[idx] : 0.5;
         u2 = ok ? ubase[idx + 1] : 0.5;
       } else {
-        philox_step_uniforms(a.rng.seed,
-                             a.rng.d_traj_ids ? a.rng.d_traj_ids[t]
-                                              : a.rng.traj_offset + (uint64_t)t,
-                             (uint64_t)(step + g), u1, u2);
+        philox_step_uniforms(a.rng.seed, stream_id, (uint64_t)(step + g), u1, u2);
       }
       pre_u1 = u1;
       pre_lu2 = log(u2);
@@ -208,74 +352,28 @@ __device__ void advance_trajectory(const KmcArgs& a, int64_t t, int g,
     const double u1 = gshfl<G>(gmask, pre_u1, k);
     const double lu2 = gshfl<G>(gmask, pre_lu2, k);
 
-    // ---- process attributes (core.py:1946-1987) ------------------------
-    int oldsite[MAXP], newsite[MAXP];
-    bool fresh[MAXP];
-    bool bad = false;
-#pragma unroll
-    for (int j = 0; j < MAXP; ++j) {
-      const int p = g * MAXP + j;
-      const int c = (p < NP) ? p / S : 0;
-      const int o = gshfl<G>(gmask, occ, c);
-      oldsite[j] = o;
-      newsite[j] = o;
-      fresh[j] = (j == 0) || (o != oldsite[j > 0 ? j - 1 : 0]);
-      if (p < NP) {
-        const int n = sy.d_nbr[(int64_t)o * S + (p - c * S)];
-        newsite[j] = n;
-        if (n < 0 || n >= N || o < 0 || o >= N) bad = true;
-      }
-    }
-    if (__ballot_sync(gmask, bad) & gmask) { status = PYCD_TRAJ_BAD_INDEX; break; }
-
-    // ---- carriers' row sums: sum_c' A[n, occ_c'] and A[o, occ_c'] -------
-    double sn[MAXP], so[MAXP];
-#pragma unroll
-    for (int j = 0; j < MAXP; ++j) { sn[j] = 0.0; so[j] = 0.0; }
-    for (int cc = 0; cc < NC; ++cc) {
-      const int sc = gshfl<G>(gmask, occ, cc);
-#pragma unroll
-      for (int j = 0; j < MAXP; ++j) {
-        if (g * MAXP + j < NP) {
-          sn[j] = dadd(sn[j], __ldg(A + (int64_t)newsite[j] * N + sc));
-          if (fresh[j]) so[j] = dadd(so[j], __ldg(A + (int64_t)oldsite[j] * N + sc));
-        }
-      }
-    }
+    // periodic exact refresh of every carrier sum (global step index)
+    if (it > 0 && (step & (R - 1)) == 0) fresh_sums<G, MAXP>(sy, g, gmask, occ, -1, pc);
 
     // ---- rates (core.py:1989-2050) ------------------------------------
     double kp[MAXP], dE[MAXP];
-    double phio = 0.0, aoo = 0.0, eo = 0.0;
 #pragma unroll
     for (int j = 0; j < MAXP; ++j) {
       kp[j] = 0.0;
       dE[j] = 0.0;
-      const int p = g * MAXP + j;
-      if (j > 0 && !fresh[j]) so[j] = so[j - 1];
-      if (p < NP) {
-        const int o = oldsite[j], n = newsite[j];
-        if (fresh[j]) {
-          phio = __ldg(sy.d_phi_bg + o);
-          aoo = __ldg(A + (int64_t)o * N + o);
-          eo = __ldg(sy.d_e_rel + o);
-        }
-        const int64_t slot = (int64_t)o * S + (p % S);
-        const double term01 = dadd(dsub(__ldg(sy.d_phi_bg + n), phio),
-                                   dmul(q, dsub(sn[j], so[j])));
-        const double term02 = dmul(q, dsub(aoo, __ldg(A + (int64_t)o * N + n)));
-        const double de0 = dadd(dmul(two_q, dadd(term01, term02)),
-                                dsub(__ldg(sy.d_e_rel + n), eo));
-        const double x = dadd(__ldg(sy.d_lam + slot), de0);
-        const double2 cf = __ldg(coef + slot);
+      if (pc.valid[j]) {
+        const double term01 = dadd(pc.dphi[j], dmul(q, dsub(pc.P[j], pc.Q[j])));
+        const double term02 = dmul(q, pc.t02[j]);
+        const double de0 = dadd(dmul(two_q, dadd(term01, term02)), pc.de[j]);
+        const double x = dadd(pc.lam[j], de0);
         dE[j] = de0;
-        kp[j] = exp_tang(fma(dmul(x, x), cf.x, cf.y));
+        kp[j] = exp_tang(fma(dmul(x, x), pc.c1[j], pc.c0[j]));
       }
     }
 
     // ---- selection (core.py:2796-2800) on the balanced tree ------------
     LocalTree<MAXP> lt;
     lt.build(kp);
-    // butterfly: lvl[l] = sum of the aligned block of 2^l lanes containing g
     double lvl[6];
     lvl[0] = lt.total();
 #pragma unroll
@@ -288,7 +386,6 @@ __device__ void advance_trajectory(const KmcArgs& a, int64_t t, int g,
     const double ktot = lvl[lg];
     if (!(ktot > 0.0) || !(ktot < INFINITY)) { status = PYCD_TRAJ_STALLED; break; }
     const double thr = dmul(u1, ktot);
-    // descend across lanes: block [base, base + 2^(l+1)), left half sum
     double acc = 0.0;
     int base = 0;
 #pragma unroll
@@ -299,7 +396,6 @@ __device__ void advance_trajectory(const KmcArgs& a, int64_t t, int g,
         if (!(s > thr)) { acc = s; base += 1 << l; }
       }
     }
-    // descend inside lane `base` over its MAXP leaves
     int node = 1;
 #pragma unroll
     for (int l = 0; (MAXP >> (l + 1)) > 0; ++l) {
@@ -332,8 +428,8 @@ __device__ void advance_trajectory(const KmcArgs& a, int64_t t, int g,
     for (int j = 0; j < MAXP; ++j) {
       const double d = gshfl<G>(gmask, dE[j], base);
       const double kk = gshfl<G>(gmask, kp[j], base);
-      const int ns = gshfl<G>(gmask, newsite[j], base);
-      const int os = gshfl<G>(gmask, oldsite[j], base);
+      const int ns = gshfl<G>(gmask, pc.newsite[j], base);
+      const int os = gshfl<G>(gmask, pc.oldsite[j], base);
       if (j == jsel) { de_sel = d; k_sel = kk; n_sel = ns; o_sel = os; }
     }
     const int c_sel = sel / S, s_sel = sel - c_sel * S;
@@ -371,6 +467,21 @@ __device__ void advance_trajectory(const KmcArgs& a, int64_t t, int g,
     ++step;
     if (ubase) ucur += 2;
 
+    // ---- carrier sums after the move o_sel -> n_sel --------------------
+    // other carriers' processes: add the moving charge's change; the moved
+    // carrier's processes: new geometry and exact sums
+#pragma unroll
+    for (int j = 0; j < MAXP; ++j) {
+      if (pc.valid[j] && pc.carrier[j] != c_sel) {
+        const int64_t rn = (int64_t)pc.newsite[j] * N, ro = (int64_t)pc.oldsite[j] * N;
+        pc.P[j] = dadd(pc.P[j], dsub(__ldg(A + rn + n_sel), __ldg(A + rn + o_sel)));
+        pc.Q[j] = dadd(pc.Q[j], dsub(__ldg(A + ro + n_sel), __ldg(A + ro + o_sel)));
+      }
+    }
+    bad = setup_processes<G, MAXP>(sy, coef, g, gmask, occ, c_sel, pc);
+    if (__ballot_sync(gmask, bad) & gmask) { status = PYCD_TRAJ_BAD_INDEX; break; }
+    fresh_sums<G, MAXP>(sy, g, gmask, occ, c_sel, pc);
+
     // ---- path-grid rows (core.py:2847-2861) ---------------------------
     if (end_path >= start_path + 1) {
       if (end_path >= n_path) end_path = n_path;
@@ -397,6 +508,13 @@ __device__ void advance_trajectory(const KmcArgs& a, int64_t t, int g,
   }
 
   // ---- write the state back ---------------------------------------------
+  if (csum) {
+#pragma unroll
+    for (int j = 0; j < MAXP; ++j) {
+      const int p = g * MAXP + j;
+      if (pc.valid[j]) { csum[p] = pc.P[j]; csum[half + p] = pc.Q[j]; }
+    }
+  }
   if (owns_carrier) {
     st.d_occ[t * MC + g] = occ;
     double* dp = st.d_disp + (t * MC + g) * 3;

@@ -123,10 +123,13 @@ class KmcTables(object):
 class KmcBatch(object):
     """State of T trajectories (device SoA) plus optional outputs."""
 
+    # exact refresh period of the carrier-potential sums (steps)
+    CSUM_REFRESH = 64
+
     def __init__(self, occupancy, sys_index=None, max_carriers=None,
                  energy0=None, unwrapped_rows=None, step_capacity=0,
                  energy_grid_rows=None, delg0_grid_rows=None, drift=False,
-                 step_limit=None):
+                 step_limit=None, max_processes=256):
         import torch
         dev = _dev()
         occ = np.asarray(occupancy, dtype=np.int32)
@@ -168,6 +171,9 @@ class KmcBatch(object):
         self.drift = z64(T, mc, 3) if drift else None
         self.step_limit = (None if step_limit is None else torch.as_tensor(
             np.broadcast_to(np.asarray(step_limit, np.int64), (T,)).copy()).to(dev))
+        self.csum_stride = 2 * int(max_processes)
+        self.csum = z64(T, self.csum_stride)
+        self.csum_refresh = self.CSUM_REFRESH
 
     def state_struct(self):
         s = nat.KmcState()
@@ -184,6 +190,9 @@ class KmcBatch(object):
         s.d_status = self.status.data_ptr()
         s.d_u_cursor = self.u_cursor.data_ptr()
         s.d_step_limit = nat.ptr(self.step_limit)
+        s.d_csum = self.csum.data_ptr()
+        s.csum_stride = self.csum_stride
+        s.csum_refresh = self.csum_refresh
         return s
 
     def outputs_struct(self):
@@ -203,7 +212,7 @@ class KmcBatch(object):
     def snapshot(self):
         """Host copy of the resumable state (checkpoint between chunks)."""
         keys = ("occ", "time", "step", "path_index", "disp", "last_row",
-                "energy", "status", "u_cursor")
+                "energy", "status", "u_cursor", "csum")
         return {k: getattr(self, k).cpu().numpy().copy() for k in keys}
 
     def restore(self, snap):

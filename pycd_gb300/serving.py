@@ -100,6 +100,7 @@ class _Bucket(object):
         self.free = list(range(capacity - 1, -1, -1))
         self.jobs = {}  # slot -> job
         self.engine = None
+        self.stream = None
 
 
 class KmcServer(object):
@@ -219,9 +220,17 @@ class KmcServer(object):
             self._write_slots(b, [j for j in admitted if j["bucket"] is b])
         self._upload()
         active = [b for b in self.buckets.values() if b.jobs]
+        # buckets run concurrently, each on its own stream
+        cur = torch.cuda.current_stream()
+        ready = torch.cuda.Event()
+        ready.record(cur)
         for b in active:
-            b.engine.advance(b.batch, self.chunk_steps,
-                             b.engine.rng_struct(seed=self.seed, traj_ids=b.ids))
+            if b.stream is None:
+                b.stream = torch.cuda.Stream()
+            b.stream.wait_event(ready)
+            b.engine.advance(b.batch, self.chunk_for(b),
+                             b.engine.rng_struct(seed=self.seed, traj_ids=b.ids),
+                             stream=b.stream)
         retired = []
         if active:
             torch.cuda.synchronize()
@@ -252,6 +261,12 @@ class KmcServer(object):
         for k in ("bucket", "lattice_entry"):
             job.pop(k, None)
         self.done.append(job)
+
+    def chunk_for(self, b):
+        """Steps per chunk for bucket b: a step costs roughly in proportion
+        to the carriers it sums over, so lighter buckets take longer chunks
+        and every bucket's chunk lasts about as long."""
+        return max(500, int(self.chunk_steps * 8 / max(8, b.nc_bound)))
 
     def busy(self):
         return bool(self.pending) or any(b.jobs for b in self.buckets.values())
