@@ -393,7 +393,7 @@ def uneven_bench(args):
     bk = BatchedKmc(tables, occ, sys_index=traj_sys, seed=SEED, chunk_steps=args.chunk,
                     step_limit=steps, autotune=True)
     tuned = [(bkt.engine.launch.lanes_per_traj, bkt.engine.launch.warps_per_block,
-              len(bkt.idx)) for bkt in bk.buckets]
+              bkt.engine.launch.min_blocks_per_sm, len(bkt.idx)) for bkt in bk.buckets]
     torch.cuda.synchronize()
     with ClockSampler(0) as clocks:
         t0 = time.perf_counter()
@@ -437,7 +437,7 @@ def uneven_bench(args):
             "site_range": [int(min(s["n_sites"] for s in specs)),
                            int(max(s["n_sites"] for s in specs))],
             "arrays_gb": arrays_gb, "setup_s": setup_s, "chunk_steps": args.chunk,
-            "buckets_lanes_warps_trajs": tuned, "status_counts": bk.status_counts(),
+            "buckets_lanes_warps_minblocks_trajs": tuned, "status_counts": bk.status_counts(),
             "diffusivity_fp64_vs_split": checks, "clocks": clocks.summary()}
     print(json.dumps(line), flush=True)
 
@@ -515,6 +515,8 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--lanes", type=int, default=0)
     ap.add_argument("--warps", type=int, default=0)
+    ap.add_argument("--min-blocks", type=int, default=0,
+                    help="2 = the 128-register kernel variant")
     args = ap.parse_args()
     if args.impl == "reference":
         return reference_arm(args)
@@ -543,12 +545,15 @@ def main():
         launch["lanes_per_traj"] = args.lanes
     if args.warps:
         launch["warps_per_block"] = args.warps
+    if args.min_blocks:
+        launch["min_blocks_per_sm"] = args.min_blocks
     # launch shape: autotuned (untimed) unless given; it never changes events
     bk = BatchedKmc(tables, occ, seed=SEED, chunk_steps=args.chunk,
                     traj_offset=stream_offset(rank, args.traj), launch=launch,
                     autotune=0 if (args.lanes or args.warps) else 2000)
     tuned = {"lanes_per_traj": bk.buckets[0].engine.launch.lanes_per_traj,
-             "warps_per_block": bk.buckets[0].engine.launch.warps_per_block}
+             "warps_per_block": bk.buckets[0].engine.launch.warps_per_block,
+             "min_blocks_per_sm": bk.buckets[0].engine.launch.min_blocks_per_sm}
     flush = torch.empty(256 * 2 ** 20, dtype=torch.uint8, device="cuda")
     for _ in range(args.warmup):
         bk.step_chunk()

@@ -283,7 +283,11 @@ typedef struct PycdKmcLaunch {
   int32_t blocks;               /* grid size; 0 = cover all trajectories     */
   int32_t max_processes;        /* max n_carriers * n_slots over the systems */
   int32_t max_carriers;         /* max n_carriers over the systems           */
-  int32_t reserved;
+  /* 0 or 1: kernel as compiled; 2: a variant limited to 128 registers per
+   * thread (two 256-thread blocks per SM, more warps to hide load latency,
+   * some spills); only for at most 2 processes per lane.  Results do not
+   * depend on it.                                                          */
+  int32_t min_blocks_per_sm;
 } PycdKmcLaunch;
 
 /* Advance every trajectory by up to max_steps KMC steps, or until its path

@@ -94,7 +94,7 @@ class KmcRng(C.Structure):
 class KmcLaunch(C.Structure):
     _fields_ = [("lanes_per_traj", C.c_int32), ("warps_per_block", C.c_int32),
                 ("blocks", C.c_int32), ("max_processes", C.c_int32),
-                ("max_carriers", C.c_int32), ("reserved", C.c_int32)]
+                ("max_carriers", C.c_int32), ("min_blocks_per_sm", C.c_int32)]
 
 
 P = C.POINTER

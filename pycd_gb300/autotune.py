@@ -3,7 +3,8 @@
 The kernel's event streams do not depend on its launch shape (cumulative
 rates are fixed balanced-tree sums over the process index), so the shape is
 a pure performance choice.  ``tune`` times short probes of every candidate
-(lanes per trajectory x warps per block) on the real batch, restoring the
+(lanes per trajectory x warps per block x register variant) on the real
+batch, restoring the
 batch state after each probe, and keeps the fastest.  Results are cached per
 (process count, carrier count, trajectory count) in-process.
 """
@@ -20,9 +21,17 @@ def candidates(max_processes, max_carriers):
         per_lane = -(-max_processes // lanes)
         if per_lane > 8:
             continue
-        for warps in (2, 4, 8):
-            out.append({"lanes_per_traj": lanes, "warps_per_block": warps})
+        for warps in (1, 2, 4, 8):
+            for minb in ((1, 2) if per_lane <= 2 else (1,)):
+                out.append({"lanes_per_traj": lanes, "warps_per_block": warps,
+                            "min_blocks_per_sm": minb})
     return out
+
+
+def _apply(engine, shape):
+    engine.launch.lanes_per_traj = shape["lanes_per_traj"]
+    engine.launch.warps_per_block = shape["warps_per_block"]
+    engine.launch.min_blocks_per_sm = shape.get("min_blocks_per_sm", 1)
 
 
 def tune(engine, batch, rng, probe_steps=200, reps=2, stream=None):
@@ -33,8 +42,7 @@ def tune(engine, batch, rng, probe_steps=200, reps=2, stream=None):
            int(batch.n_traj))
     if key in _CACHE:
         best = _CACHE[key]
-        engine.launch.lanes_per_traj = best["lanes_per_traj"]
-        engine.launch.warps_per_block = best["warps_per_block"]
+        _apply(engine, best)
         return {"best": best, "table": [], "cached": True}
     snap = batch.snapshot()
     limit = batch.step_limit
@@ -42,8 +50,7 @@ def tune(engine, batch, rng, probe_steps=200, reps=2, stream=None):
     table = []
     s = stream or torch.cuda.current_stream()
     for cand in candidates(engine.launch.max_processes, engine.launch.max_carriers):
-        engine.launch.lanes_per_traj = cand["lanes_per_traj"]
-        engine.launch.warps_per_block = cand["warps_per_block"]
+        _apply(engine, cand)
         times = []
         for r in range(reps + 1):
             batch.restore(snap)
@@ -59,7 +66,6 @@ def tune(engine, batch, rng, probe_steps=200, reps=2, stream=None):
     batch.restore(snap)
     batch.step_limit = limit
     best = min(table, key=lambda x: x[1])[0]
-    engine.launch.lanes_per_traj = best["lanes_per_traj"]
-    engine.launch.warps_per_block = best["warps_per_block"]
+    _apply(engine, best)
     _CACHE[key] = best
     return {"best": best, "table": table, "cached": False}

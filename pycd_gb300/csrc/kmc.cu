@@ -1,552 +1,12 @@
-// Lattice KMC on sm_103a: the Run.do_kmc_steps loop (PyCD/core.py:2787-2861).
-//
-// Mapping.  A trajectory is owned by a group of G lanes of one warp
-// (G = 1..32, a power of two); a warp holds 32/G trajectories.  Process p of
-// a trajectory is (carrier c = p / S, slot s = p % S), the reference's order
-// (core.py:1946-1987).  Lane g owns the contiguous processes
-// p = g*MAXP + j (j < MAXP) and carrier g (its site, its displacement
-// accumulator and its path-row values); G*MAXP >= n_carriers * S.
-//
-// Arithmetic.  GB300's FP64 pipe issues ~2 DFMA/clk/SM, and FP64 is the
-// bound of this kernel, so the step is written to spend few FP64
-// instructions while keeping every result within a few ulp of the
-// reference's expression:
-//   dE0   = 2q (term01 + term02) + (E_rel[n] - E_rel[o])      core.py:2004-2026
-//           term01 = (phi_bg[n] - phi_bg[o]) + q (sum_c' A[n,occ_c'] - sum_c' A[o,occ_c'])
-//           term02 = q (A[o,o] - A[o,n])
-//   rate  = exp(c1 (lam + dE0)^2 + c0),  c1 = -1/(4 lam kT),
-//           c0 = (V_ab + shift)/kT + ln vn   (= vn exp(-dG/kT), core.py:2045-2047)
-//   k_tot and every cumulative rate are sums over a fixed balanced binary
-//   tree over the process index (zero-padded to a power of two), so the
-//   event stream does not depend on G or MAXP: a trajectory advanced alone
-//   (the plain form) and inside a batch of thousands give identical events.
-//   The event is the first process whose cumulative rate exceeds u1 k_tot
-//   (core.py:2796-2800); t -= log(u2) / k_tot (core.py:2802-2803).
-// exp() is Tang's table-driven method (ACM TOMS 15(2), 1989): reduction by
-// ln2/32 with a 32-entry table of 2^(j/32) in two parts and a degree-6
-// polynomial on |r| <= ln2/64.
+// Lattice KMC on sm_103a: launch dispatch of the persistent kernel
+// (kmc_device.cuh) and the small helper kernels.
 #include <cuda_runtime.h>
 #include <math.h>
 #include <stdint.h>
 
-#include "common.cuh"
-#include "kmc_internal.cuh"
+#include "kmc_device.cuh"
 
 namespace pycd {
-
-__device__ __forceinline__ double dsub(double a, double b) { return __dsub_rn(a, b); }
-__device__ __forceinline__ double dadd(double a, double b) { return __dadd_rn(a, b); }
-__device__ __forceinline__ double dmul(double a, double b) { return __dmul_rn(a, b); }
-__device__ __forceinline__ double ddiv(double a, double b) { return __ddiv_rn(a, b); }
-
-// ---------------------------------------------------------------------------
-// exp(x), Tang's method
-// ---------------------------------------------------------------------------
-__device__ const unsigned long long kExp2Hi[32] = {
-    0x3ff0000000000000ULL, 0x3ff059b0d3158574ULL, 0x3ff0b5586cf9890fULL, 0x3ff11301d0125b51ULL,
-    0x3ff172b83c7d517bULL, 0x3ff1d4873168b9aaULL, 0x3ff2387a6e756238ULL, 0x3ff29e9df51fdee1ULL,
-    0x3ff306fe0a31b715ULL, 0x3ff371a7373aa9cbULL, 0x3ff3dea64c123422ULL, 0x3ff44e086061892dULL,
-    0x3ff4bfdad5362a27ULL, 0x3ff5342b569d4f82ULL, 0x3ff5ab07dd485429ULL, 0x3ff6247eb03a5585ULL,
-    0x3ff6a09e667f3bcdULL, 0x3ff71f75e8ec5f74ULL, 0x3ff7a11473eb0187ULL, 0x3ff82589994cce13ULL,
-    0x3ff8ace5422aa0dbULL, 0x3ff93737b0cdc5e5ULL, 0x3ff9c49182a3f090ULL, 0x3ffa5503b23e255dULL,
-    0x3ffae89f995ad3adULL, 0x3ffb7f76f2fb5e47ULL, 0x3ffc199bdd85529cULL, 0x3ffcb720dcef9069ULL,
-    0x3ffd5818dcfba487ULL, 0x3ffdfc97337b9b5fULL, 0x3ffea4afa2a490daULL, 0x3fff50765b6e4540ULL};
-__device__ const unsigned long long kExp2Lo[32] = {
-    0x0000000000000000ULL, 0x3c8d73e2a475b465ULL, 0x3c98a62e4adc610bULL, 0xbc96c51039449b3aULL,
-    0xbc819041b9d78a76ULL, 0x3c9e016e00a2643cULL, 0x3c99b07eb6c70573ULL, 0x3c8612e8afad1255ULL,
-    0x3c86f46ad23182e4ULL, 0xbc963aeabf42eae2ULL, 0x3c8ada0911f09ebcULL, 0x3c489b7a04ef80d0ULL,
-    0x3c7d4397afec42e2ULL, 0xbc807abe1db13cadULL, 0x3c96324c054647adULL, 0xbc9383c17e40b497ULL,
-    0xbc9bdd3413b26456ULL, 0xbc816e4786887a99ULL, 0xbc841577ee04992fULL, 0xbc9d4c1dd41532d8ULL,
-    0x3c96e9f156864b27ULL, 0xbc675fc781b57ebcULL, 0x3c7c7c46b071f2beULL, 0xbc9d2f6edb8d41e1ULL,
-    0x3c97a1cd345dcc81ULL, 0xbc75584f7e54ac3bULL, 0x3c811065895048ddULL, 0x3c7503cbd1e949dbULL,
-    0x3c82ed02d75b3707ULL, 0xbc91a5cd4f184b5cULL, 0xbc9e9c23179c2893ULL, 0x3c99d3e12dd8a18bULL};
-
-__device__ __forceinline__ double exp_tang(double x) {
-  const double kInvL = 46.16624130844683;        // 32 / ln 2
-  const double kL1 = 0.02166084939249829;        // ln2/32, leading part
-  const double kL2 = 7.247021293269686e-19;      // ln2/32 - kL1
-  const double kShift = 6755399441055744.0;      // 1.5 * 2^52
-  if (!(x < 709.782712893384)) return (x != x) ? x : INFINITY;
-  if (x < -745.1332191019412) return 0.0;
-  // N = round(x * 32/ln2) in the low word of t
-  const double t = fma(x, kInvL, kShift);
-  const int n = __double2loint(t);
-  const double nd = dsub(t, kShift);
-  const double r = fma(-nd, kL2, fma(-nd, kL1, x));
-  const int j = n & 31;
-  const int m = (n - j) >> 5;
-  // p = expm1(r) on |r| <= ln2/64, Taylor to degree 6
-  double p = fma(r, 1.0 / 720.0, 1.0 / 120.0);
-  p = fma(p, r, 1.0 / 24.0);
-  p = fma(p, r, 1.0 / 6.0);
-  p = fma(p, r, 0.5);
-  p = fma(dmul(p, r), r, r);
-  const double shi = __longlong_as_double((long long)kExp2Hi[j]);
-  const double slo = __longlong_as_double((long long)kExp2Lo[j]);
-  // 2^(j/32) (1 + p) = shi + (slo + (shi + slo) p)
-  const double v = dadd(shi, fma(dadd(shi, slo), p, slo));
-  // scale by 2^m through the exponent field (two steps below the normal range)
-  if (m >= -1021) {
-    return __hiloint2double(__double2hiint(v) + (m << 20), __double2loint(v));
-  }
-  const double v2 = __hiloint2double(__double2hiint(v) + ((m + 64) << 20),
-                                     __double2loint(v));
-  return dmul(v2, 5.421010862427522e-20);  // 2^-64
-}
-
-template <int G>
-__device__ __forceinline__ double gshfl(unsigned mask, double v, int src) {
-  return __shfl_sync(mask, v, src, G);
-}
-template <int G>
-__device__ __forceinline__ int gshfl(unsigned mask, int v, int src) {
-  return __shfl_sync(mask, v, src, G);
-}
-
-// Balanced-tree sums over the MAXP register values: node sums of the
-// subtree rooted at each internal node, in heap order (1 = root).
-template <int MAXP>
-struct LocalTree {
-  double node[2 * MAXP];  // node[MAXP + j] = leaf j
-  __device__ __forceinline__ void build(const double* leaf) {
-#pragma unroll
-    for (int j = 0; j < MAXP; ++j) node[MAXP + j] = leaf[j];
-#pragma unroll
-    for (int i = MAXP - 1; i >= 1; --i) node[i] = dadd(node[2 * i], node[2 * i + 1]);
-  }
-  __device__ __forceinline__ double total() const { return node[1]; }
-};
-
-// Per-process cache of one lane: geometry, constants that change only when
-// the process' own carrier moves, and the two carrier-potential sums.
-template <int MAXP>
-struct ProcCache {
-  int oldsite[MAXP], newsite[MAXP], carrier[MAXP];
-  double dphi[MAXP], t02[MAXP], de[MAXP], lam[MAXP], c1[MAXP], c0[MAXP];
-  double P[MAXP], Q[MAXP];
-  bool valid[MAXP];
-};
-
-// (Re)build geometry and constants of this lane's processes that belong to
-// carrier `only` (all when only < 0).  Every lane runs the shuffles.
-// Returns true when an index is out of range (no gather was issued with it).
-template <int G, int MAXP>
-__device__ __forceinline__ bool setup_processes(const PycdKmcSystem& sy,
-                                                const double2* __restrict__ coef,
-                                                int g, unsigned gmask, int occ,
-                                                int only, ProcCache<MAXP>& pc) {
-  const int64_t N = sy.n_sites;
-  const int S = sy.n_slots;
-  const int NP = sy.n_carriers * S;
-  const double* __restrict__ A = sy.d_A;
-  bool bad = false;
-#pragma unroll
-  for (int j = 0; j < MAXP; ++j) {
-    const int p = g * MAXP + j;
-    const bool v = p < NP;
-    const int c = v ? p / S : 0;
-    const int o = gshfl<G>(gmask, occ, c);
-    pc.valid[j] = v;
-    if (v && (only < 0 || c == only)) {
-      pc.carrier[j] = c;
-      const int s = p - c * S;
-      const int n = sy.d_nbr[(int64_t)o * S + s];
-      pc.oldsite[j] = o;
-      pc.newsite[j] = n;
-      if (n < 0 || n >= N || o < 0 || o >= N) {
-        bad = true;
-        continue;
-      }
-      const int64_t slot = (int64_t)o * S + s;
-      pc.dphi[j] = dsub(__ldg(sy.d_phi_bg + n), __ldg(sy.d_phi_bg + o));
-      pc.t02[j] = dsub(__ldg(A + (int64_t)o * N + o), __ldg(A + (int64_t)o * N + n));
-      pc.de[j] = dsub(__ldg(sy.d_e_rel + n), __ldg(sy.d_e_rel + o));
-      pc.lam[j] = __ldg(sy.d_lam + slot);
-      const double2 cf = __ldg(coef + slot);
-      pc.c1[j] = cf.x;
-      pc.c0[j] = cf.y;
-    } else if (!v) {
-      pc.carrier[j] = -1;
-      pc.oldsite[j] = 0;
-      pc.newsite[j] = 0;
-    }
-  }
-  return bad;
-}
-
-// Carriers in blocks of U: all loads of a block are issued before any of
-// their sums, so a step waits for a few memory round trips instead of one
-// per carrier; the additions keep carrier order (identical results for any U).
-template <int G, int MAXP, int U>
-__device__ __forceinline__ void fresh_sums_block(const double* __restrict__ A,
-                                                 int64_t N, int NC, unsigned gmask,
-                                                 int occ, const bool (&doit)[MAXP],
-                                                 const bool (&ownq)[MAXP],
-                                                 ProcCache<MAXP>& pc) {
-  for (int c0 = 0; c0 < NC; c0 += U) {
-    int sc[U];
-#pragma unroll
-    for (int u = 0; u < U; ++u) sc[u] = gshfl<G>(gmask, occ, min(c0 + u, NC - 1));
-#pragma unroll
-    for (int j = 0; j < MAXP; ++j) {
-      if (doit[j]) {
-        const double* rn = A + (int64_t)pc.newsite[j] * N;
-        const double* ro = A + (int64_t)pc.oldsite[j] * N;
-        double vn[U], vo[U];
-#pragma unroll
-        for (int u = 0; u < U; ++u) {
-          vn[u] = (c0 + u < NC) ? __ldg(rn + sc[u]) : 0.0;
-          vo[u] = (ownq[j] && c0 + u < NC) ? __ldg(ro + sc[u]) : 0.0;
-        }
-#pragma unroll
-        for (int u = 0; u < U; ++u) {
-          if (c0 + u < NC) {
-            pc.P[j] = dadd(pc.P[j], vn[u]);
-            if (ownq[j]) pc.Q[j] = dadd(pc.Q[j], vo[u]);
-          }
-        }
-      }
-    }
-  }
-}
-
-// Exact carrier sums for this lane's processes of carrier `only` (all when
-// only < 0): P = sum_c' A[n, occ_c'], Q = sum_c' A[o, occ_c'] in carrier
-// order; Q is evaluated once per carrier and shared by its processes.
-template <int G, int MAXP>
-__device__ __forceinline__ void fresh_sums(const PycdKmcSystem& sy, int g,
-                                           unsigned gmask, int occ, int only,
-                                           ProcCache<MAXP>& pc) {
-  const int64_t N = sy.n_sites;
-  const int NC = sy.n_carriers;
-  const double* __restrict__ A = sy.d_A;
-  bool doit[MAXP], ownq[MAXP];
-#pragma unroll
-  for (int j = 0; j < MAXP; ++j) {
-    doit[j] = pc.valid[j] && (only < 0 || pc.carrier[j] == only);
-    ownq[j] = doit[j] && (j == 0 || pc.carrier[j] != pc.carrier[j > 0 ? j - 1 : 0] ||
-                          !doit[j > 0 ? j - 1 : 0]);
-    if (doit[j]) {
-      pc.P[j] = 0.0;
-      if (ownq[j]) pc.Q[j] = 0.0;
-    }
-  }
-  if (NC <= 4)
-    fresh_sums_block<G, MAXP, 4>(A, N, NC, gmask, occ, doit, ownq, pc);
-  else
-    fresh_sums_block<G, MAXP, 8>(A, N, NC, gmask, occ, doit, ownq, pc);
-#pragma unroll
-  for (int j = 1; j < MAXP; ++j)
-    if (doit[j] && !ownq[j]) pc.Q[j] = pc.Q[j - 1];
-}
-
-// One group of G lanes advances one trajectory by up to max_steps steps.
-template <int G, int MAXP>
-__device__ void advance_trajectory(const KmcArgs& a, int64_t t, int g,
-                                   unsigned gmask) {
-  const PycdKmcState& st = a.st;
-  int32_t status = st.d_status[t];
-  if (status != PYCD_TRAJ_RUNNING) return;
-  const int sys_id = st.d_sys_index ? st.d_sys_index[t] : 0;
-  if (sys_id < 0 || sys_id >= a.n_systems) {
-    if (g == 0) st.d_status[t] = PYCD_TRAJ_BAD_INDEX;
-    return;
-  }
-  const KmcSysDev& sd = a.systems[sys_id];
-  const PycdKmcSystem& sy = sd.pub;
-  const int64_t N = sy.n_sites;
-  const int S = sy.n_slots;
-  const int NC = sy.n_carriers;
-  const int NP = NC * S;
-  const int MC = st.max_carriers;
-  const double q = sy.carrier_charge;
-  const double two_q = dmul(2.0, q);
-  const double* __restrict__ A = sy.d_A;
-  const double2* __restrict__ coef = sd.coef;
-  const double dt_grid = sy.time_interval;
-  if (NP > G * MAXP || NC > G || (st.d_csum && 2 * NP > st.csum_stride)) {
-    // launch shape or carrier-sum storage too small for this system
-    if (g == 0) st.d_status[t] = PYCD_TRAJ_BAD_INDEX;
-    return;
-  }
-  // refresh period of the carrier sums (every step without storage)
-  const int64_t R = (st.d_csum && st.csum_refresh > 0) ? st.csum_refresh : 1;
-  double* csum = st.d_csum ? st.d_csum + t * (int64_t)st.csum_stride : nullptr;
-  const int half = st.csum_stride / 2;
-
-  int occ = 0;
-  double disp0 = 0.0, disp1 = 0.0, disp2 = 0.0;
-  double row0 = 0.0, row1 = 0.0, row2 = 0.0;
-  const bool owns_carrier = g < NC;
-  if (owns_carrier) {
-    occ = st.d_occ[t * MC + g];
-    const double* dp = st.d_disp + (t * MC + g) * 3;
-    disp0 = dp[0]; disp1 = dp[1]; disp2 = dp[2];
-    const double* lr = st.d_last_row + (t * MC + g) * 3;
-    row0 = lr[0]; row1 = lr[1]; row2 = lr[2];
-  }
-  double sim_time = st.d_time[t];
-  int64_t step = st.d_step[t];
-  int64_t start_path = st.d_path_index[t];
-  double energy = st.d_energy ? st.d_energy[t] : 0.0;
-  int64_t ucur = st.d_u_cursor ? st.d_u_cursor[t] : 0;
-  const int64_t step_limit = st.d_step_limit ? st.d_step_limit[t] : INT64_MAX;
-  const double* ubase = a.rng.d_uniforms
-                            ? a.rng.d_uniforms + (int64_t)t * a.rng.u_stride
-                            : nullptr;
-  const uint64_t stream_id = a.rng.d_traj_ids ? a.rng.d_traj_ids[t]
-                                              : a.rng.traj_offset + (uint64_t)t;
-  const int64_t n_path = sy.n_path_steps;
-  const int64_t row_len = 3 * (int64_t)MC;
-  double* unw = a.out.d_unwrapped
-                    ? a.out.d_unwrapped +
-                          (int64_t)t * (a.out.unwrapped_stride
-                                            ? a.out.unwrapped_stride
-                                            : n_path * row_len)
-                    : nullptr;
-  // below t_guard the quotient sim_time / dt cannot reach start_path + 1
-  double t_guard = dmul(dmul((double)(start_path + 1), dt_grid), 1.0 - 0x1p-40);
-
-  // uniforms of steps pre_base + g, prepared G at a time
-  double pre_u1 = 0.0, pre_lu2 = 0.0;
-  int64_t pre_base = -(int64_t)G - 1;
-
-  // ---- process cache: geometry, constants, carrier sums ----------------
-  ProcCache<MAXP> pc;
-  bool bad = setup_processes<G, MAXP>(sy, coef, g, gmask, occ, -1, pc);
-  if (__ballot_sync(gmask, bad) & gmask) {
-    if (g == 0) st.d_status[t] = PYCD_TRAJ_BAD_INDEX;
-    return;
-  }
-  if (csum && (step & (R - 1)) != 0) {
-#pragma unroll
-    for (int j = 0; j < MAXP; ++j) {
-      const int p = g * MAXP + j;
-      if (pc.valid[j]) { pc.P[j] = csum[p]; pc.Q[j] = csum[half + p]; }
-    }
-  } else {
-    fresh_sums<G, MAXP>(sy, g, gmask, occ, -1, pc);
-  }
-
-  for (int64_t it = 0; it < a.max_steps; ++it) {
-    if (step >= step_limit) { status = PYCD_TRAJ_STEP_LIMIT; break; }
-    // ---- uniforms (core.py:2799, 2802) --------------------------------
-    if (ubase && ucur + 2 > a.rng.u_count) { status = PYCD_TRAJ_NEED_UNIFORMS; break; }
-    const int64_t since = step - pre_base;
-    int k = (int)since;
-    if (since < 0 || since >= G) {
-      pre_base = step;
-      k = 0;
-      double u1, u2;
-      if (ubase) {
-        const int64_t idx = ucur + 2 * (int64_t)g;
-        const bool ok = idx + 2 <= a.rng.u_count;
-        u1 = ok ? ubase[idx] : 0.5;
-        u2 = ok ? ubase[idx + 1] : 0.5;
-      } else {
-        philox_step_uniforms(a.rng.seed, stream_id, (uint64_t)(step + g), u1, u2);
-      }
-      pre_u1 = u1;
-      pre_lu2 = log(u2);
-    }
-    const double u1 = gshfl<G>(gmask, pre_u1, k);
-    const double lu2 = gshfl<G>(gmask, pre_lu2, k);
-
-    // periodic exact refresh of every carrier sum (global step index)
-    if (it > 0 && (step & (R - 1)) == 0) fresh_sums<G, MAXP>(sy, g, gmask, occ, -1, pc);
-
-    // ---- rates (core.py:1989-2050) ------------------------------------
-    double kp[MAXP], dE[MAXP];
-#pragma unroll
-    for (int j = 0; j < MAXP; ++j) {
-      kp[j] = 0.0;
-      dE[j] = 0.0;
-      if (pc.valid[j]) {
-        const double term01 = dadd(pc.dphi[j], dmul(q, dsub(pc.P[j], pc.Q[j])));
-        const double term02 = dmul(q, pc.t02[j]);
-        const double de0 = dadd(dmul(two_q, dadd(term01, term02)), pc.de[j]);
-        const double x = dadd(pc.lam[j], de0);
-        dE[j] = de0;
-        kp[j] = exp_tang(fma(dmul(x, x), pc.c1[j], pc.c0[j]));
-      }
-    }
-
-    // ---- selection (core.py:2796-2800) on the balanced tree ------------
-    LocalTree<MAXP> lt;
-    lt.build(kp);
-    double lvl[6];
-    lvl[0] = lt.total();
-#pragma unroll
-    for (int l = 0; (1 << l) < G; ++l) {
-      const double other = __shfl_xor_sync(gmask, lvl[l], 1 << l, G);
-      lvl[l + 1] = dadd(lvl[l], other);
-    }
-    int lg = 0;
-    while ((1 << lg) < G) ++lg;
-    const double ktot = lvl[lg];
-    if (!(ktot > 0.0) || !(ktot < INFINITY)) { status = PYCD_TRAJ_STALLED; break; }
-    const double thr = dmul(u1, ktot);
-    double acc = 0.0;
-    int base = 0;
-#pragma unroll
-    for (int l = 5; l >= 0; --l) {
-      if (l < lg) {
-        const double left = gshfl<G>(gmask, lvl[l], base);
-        const double s = dadd(acc, left);
-        if (!(s > thr)) { acc = s; base += 1 << l; }
-      }
-    }
-    int node = 1;
-#pragma unroll
-    for (int l = 0; (MAXP >> (l + 1)) > 0; ++l) {
-      double left = 0.0;
-#pragma unroll
-      for (int i = 1; i < MAXP; ++i) {
-        const double v = gshfl<G>(gmask, lt.node[2 * i], base);
-        if (i == node) left = v;
-      }
-      const double s = dadd(acc, left);
-      if (!(s > thr)) { acc = s; node = 2 * node + 1; } else { node = 2 * node; }
-    }
-    const int jsel = node - MAXP;
-    const int sel = base * MAXP + jsel;
-    // only a u1 within rounding of 1 can walk into the zero padding
-    if (sel >= NP) { status = PYCD_TRAJ_NO_EVENT; break; }
-
-    // ---- residence time (core.py:2802-2804) ---------------------------
-    sim_time = dsub(sim_time, ddiv(lu2, ktot));
-    int64_t end_path = start_path - 1;
-    if (sim_time >= t_guard) {
-      const double tq = ddiv(sim_time, dt_grid);
-      end_path = (tq < 9.0e18) ? (int64_t)tq : INT64_MAX;
-    }
-
-    // broadcast the selected process' data from its owner lane
-    double de_sel = 0.0, k_sel = 0.0;
-    int n_sel = 0, o_sel = 0;
-#pragma unroll
-    for (int j = 0; j < MAXP; ++j) {
-      const double d = gshfl<G>(gmask, dE[j], base);
-      const double kk = gshfl<G>(gmask, kp[j], base);
-      const int ns = gshfl<G>(gmask, pc.newsite[j], base);
-      const int os = gshfl<G>(gmask, pc.oldsite[j], base);
-      if (j == jsel) { de_sel = d; k_sel = kk; n_sel = ns; o_sel = os; }
-    }
-    const int c_sel = sel / S, s_sel = sel - c_sel * S;
-
-    // delG0 grid rows [start, end) (core.py:2807-2809)
-    if (a.out.d_delg0_grid) {
-      const int64_t e = end_path < n_path ? end_path : n_path;
-      double* dgr = a.out.d_delg0_grid + (int64_t)t * n_path;
-      for (int64_t r = start_path + g; r < e; r += G) dgr[r] = de_sel;
-    }
-
-    // ---- state update (core.py:2810-2830) -----------------------------
-    if (g == c_sel) {
-      occ = n_sel;
-      const double* hv = sy.d_hop + ((int64_t)o_sel * S + s_sel) * 3;
-      const double h0 = __ldg(hv), h1 = __ldg(hv + 1), h2 = __ldg(hv + 2);
-      disp0 = dadd(disp0, h0);
-      disp1 = dadd(disp1, h1);
-      disp2 = dadd(disp2, h2);
-      if (a.out.d_drift) {
-        double* dr = a.out.d_drift + ((int64_t)t * MC + g) * 3;
-        dr[0] = dadd(dr[0], dmul(h0, k_sel));
-        dr[1] = dadd(dr[1], dmul(h1, k_sel));
-        dr[2] = dadd(dr[2], dmul(h2, k_sel));
-      }
-    }
-    energy = dadd(energy, de_sel);
-    if (g == 0 && a.out.d_step_time) {
-      const int64_t col = step - a.out.step_offset;
-      if (col >= 0 && col < a.out.step_capacity) {
-        a.out.d_step_time[(int64_t)t * a.out.step_capacity + col] = sim_time;
-        a.out.d_step_proc[(int64_t)t * a.out.step_capacity + col] = sel;
-      }
-    }
-    ++step;
-    if (ubase) ucur += 2;
-
-    // ---- carrier sums after the move o_sel -> n_sel --------------------
-    // other carriers' processes: add the moving charge's change; the moved
-    // carrier's processes: new geometry and exact sums
-#pragma unroll
-    for (int j = 0; j < MAXP; ++j) {
-      if (pc.valid[j] && pc.carrier[j] != c_sel) {
-        const int64_t rn = (int64_t)pc.newsite[j] * N, ro = (int64_t)pc.oldsite[j] * N;
-        pc.P[j] = dadd(pc.P[j], dsub(__ldg(A + rn + n_sel), __ldg(A + rn + o_sel)));
-        pc.Q[j] = dadd(pc.Q[j], dsub(__ldg(A + ro + n_sel), __ldg(A + ro + o_sel)));
-      }
-    }
-    bad = setup_processes<G, MAXP>(sy, coef, g, gmask, occ, c_sel, pc);
-    if (__ballot_sync(gmask, bad) & gmask) { status = PYCD_TRAJ_BAD_INDEX; break; }
-    fresh_sums<G, MAXP>(sy, g, gmask, occ, c_sel, pc);
-
-    // ---- path-grid rows (core.py:2847-2861) ---------------------------
-    if (end_path >= start_path + 1) {
-      if (end_path >= n_path) end_path = n_path;
-      if (owns_carrier) {
-        row0 = dadd(row0, disp0);
-        row1 = dadd(row1, disp1);
-        row2 = dadd(row2, disp2);
-        if (unw) {
-          for (int64_t r = start_path; r < end_path; ++r) {
-            double* rp = unw + r * row_len + 3 * g;
-            rp[0] = row0; rp[1] = row1; rp[2] = row2;
-          }
-        }
-        disp0 = disp1 = disp2 = 0.0;
-      }
-      if (a.out.d_energy_grid) {
-        double* eg = a.out.d_energy_grid + (int64_t)t * n_path;
-        for (int64_t r = start_path + g; r < end_path; r += G) eg[r] = energy;
-      }
-      start_path = end_path;
-      t_guard = dmul(dmul((double)(start_path + 1), dt_grid), 1.0 - 0x1p-40);
-    }
-    if (end_path >= n_path) { status = PYCD_TRAJ_DONE; break; }
-  }
-
-  // ---- write the state back ---------------------------------------------
-  if (csum) {
-#pragma unroll
-    for (int j = 0; j < MAXP; ++j) {
-      const int p = g * MAXP + j;
-      if (pc.valid[j]) { csum[p] = pc.P[j]; csum[half + p] = pc.Q[j]; }
-    }
-  }
-  if (owns_carrier) {
-    st.d_occ[t * MC + g] = occ;
-    double* dp = st.d_disp + (t * MC + g) * 3;
-    dp[0] = disp0; dp[1] = disp1; dp[2] = disp2;
-    double* lr = st.d_last_row + (t * MC + g) * 3;
-    lr[0] = row0; lr[1] = row1; lr[2] = row2;
-  }
-  if (g == 0) {
-    st.d_time[t] = sim_time;
-    st.d_step[t] = step;
-    st.d_path_index[t] = start_path;
-    if (st.d_energy) st.d_energy[t] = energy;
-    if (st.d_u_cursor) st.d_u_cursor[t] = ucur;
-    st.d_status[t] = status;
-  }
-}
-
-template <int G, int MAXP>
-__global__ void __launch_bounds__(256) kmc_advance_kernel(KmcArgs a) {
-  const int lane = threadIdx.x & 31;
-  const int sub = lane / G;
-  const int g = lane - sub * G;
-  const unsigned gmask =
-      (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << (sub * G));
-  const int64_t groups_per_warp = 32 / G;
-  const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int64_t n_warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  for (int64_t t = warp * groups_per_warp + sub; t < a.st.n_traj;
-       t += n_warps * groups_per_warp) {
-    advance_trajectory<G, MAXP>(a, t, g, gmask);
-  }
-}
 
 // Per-slot exponent coefficients: c1 = -1/(4 lam kT), c0 = (V + shift)/kT + ln vn.
 __global__ void kmc_coef_kernel(const double* __restrict__ lam,
@@ -589,18 +49,6 @@ static int pow2_at_least(int v) {
   return p;
 }
 
-template <int G, int MAXP>
-static cudaError_t launch_g(const KmcArgs& a, int warps_per_block, int blocks,
-                            cudaStream_t s) {
-  kmc_advance_kernel<G, MAXP><<<blocks, warps_per_block * 32, 0, s>>>(a);
-  return cudaGetLastError();
-}
-
-#define PYCD_KMC_SHAPES(X)                                                   \
-  X(1, 1) X(2, 1) X(4, 1) X(8, 1) X(16, 1) X(32, 1) X(2, 2) X(4, 2) X(8, 2)  \
-  X(16, 2) X(32, 2) X(4, 4) X(8, 4) X(16, 4) X(32, 4) X(4, 8) X(8, 8)        \
-  X(16, 8) X(32, 8)
-
 int kmc_launch(const KmcArgs& a, int max_np, int max_nc,
                const PycdKmcLaunch* launch, cudaStream_t s) {
   int G = launch && launch->lanes_per_traj ? launch->lanes_per_traj : 0;
@@ -616,6 +64,10 @@ int kmc_launch(const KmcArgs& a, int max_np, int max_nc,
                "%d lanes", max_np, G);
   int wpb = launch && launch->warps_per_block ? launch->warps_per_block : 4;
   PYCD_REQUIRE(wpb >= 1 && wpb <= 8, "warps_per_block must be in [1, 8]");
+  const int minb = launch && launch->min_blocks_per_sm ? launch->min_blocks_per_sm : 1;
+  PYCD_REQUIRE(minb == 1 || (minb == 2 && MAXP <= 2),
+               "min_blocks_per_sm must be 0, 1, or 2 with at most 2 processes "
+               "per lane (got %d with %d)", minb, MAXP);
   const int64_t tpw = 32 / G;
   const int64_t warps_needed = (a.st.n_traj + tpw - 1) / tpw;
   int blocks = launch && launch->blocks ? launch->blocks
@@ -623,13 +75,17 @@ int kmc_launch(const KmcArgs& a, int max_np, int max_nc,
   if (blocks < 1) blocks = 1;
   cudaError_t e = cudaErrorInvalidConfiguration;
   bool found = false;
+  if (minb == 2) {
+    e = kmc_launch_capped(a, G, MAXP, wpb, blocks, s, &found);
+  } else {
 #define PYCD_KMC_CASE(g_, m_)                                                \
   if (!found && G == g_ && MAXP == m_) {                                     \
-    e = launch_g<g_, m_>(a, wpb, blocks, s);                                 \
+    e = launch_g<g_, m_, 1>(a, wpb, blocks, s);                              \
     found = true;                                                            \
   }
-  PYCD_KMC_SHAPES(PYCD_KMC_CASE)
+    PYCD_KMC_SHAPES(PYCD_KMC_CASE)
 #undef PYCD_KMC_CASE
+  }
   PYCD_REQUIRE(found, "no kernel instance for %d lanes x %d processes per lane",
                G, MAXP);
   if (e != cudaSuccess) return cuda_fail(e, "kmc_advance_kernel launch", __FILE__, __LINE__);
@@ -641,9 +97,10 @@ int kmc_preload() {
   cudaError_t e = cudaSuccess;
 #define PYCD_KMC_LOAD(g_, m_)                                                \
   if (e == cudaSuccess)                                                      \
-    e = cudaFuncGetAttributes(&fa, (const void*)kmc_advance_kernel<g_, m_>);
+    e = cudaFuncGetAttributes(&fa, (const void*)kmc_advance_kernel<g_, m_, 1>);
   PYCD_KMC_SHAPES(PYCD_KMC_LOAD)
 #undef PYCD_KMC_LOAD
+  if (e == cudaSuccess) e = kmc_preload_capped();
   if (e != cudaSuccess) return cuda_fail(e, "cudaFuncGetAttributes", __FILE__, __LINE__);
   return PYCD_OK;
 }

@@ -28,6 +28,11 @@ struct KmcArgs {
 int kmc_launch(const KmcArgs& a, int max_np, int max_nc,
                const PycdKmcLaunch* launch, cudaStream_t s);
 int kmc_preload();
+// the register-capped instances (kmc_capped.cu); *found = false when
+// there is no instance for (G, MAXP)
+cudaError_t kmc_launch_capped(const KmcArgs& a, int G, int MAXP, int warps_per_block,
+                              int blocks, cudaStream_t s, bool* found);
+cudaError_t kmc_preload_capped();
 int kmc_coef_launch(const PycdKmcSystem& s, double2* coef, cudaStream_t st);
 int exp_probe_launch(const double* x, int64_t n, double* ours, double* ref,
                      cudaStream_t s);

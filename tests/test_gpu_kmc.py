@@ -234,8 +234,10 @@ def test_event_stream_independent_of_launch_shape(cuda_ready):
     rng = np.random.default_rng(5)
     occ = np.stack([rng.choice(3600, size=4, replace=False) for _ in range(T)])
     results = []
-    for lanes in (4, 8, 16, 32):
-        eng = KmcEngine(tables, launch={"lanes_per_traj": lanes})
+    shapes = [(4, 1), (8, 1), (8, 2), (16, 1), (16, 2), (32, 1), (32, 2)]
+    for lanes, minb in shapes:  # minb 2: the 128-register variant
+        eng = KmcEngine(tables, launch={"lanes_per_traj": lanes,
+                                        "min_blocks_per_sm": minb})
         b = KmcBatch(occ, step_capacity=n)
         eng.advance(b, n, eng.rng_struct(seed=seed))
         torch.cuda.synchronize()

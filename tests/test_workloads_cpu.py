@@ -41,6 +41,8 @@ def test_autotune_candidates_respect_kernel_limits():
         for c in candidates(npr, nc):
             lanes = c["lanes_per_traj"]
             assert lanes >= nc and -(-npr // lanes) <= 8
+            # the register-capped instances exist for <= 2 processes per lane
+            assert c["min_blocks_per_sm"] == 1 or -(-npr // lanes) <= 2
 
 
 def test_monoclinic_hop_shells_have_three_neighbours():
