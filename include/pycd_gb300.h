@@ -335,6 +335,52 @@ PYCD_API int pycd_philox_uniforms(uint64_t seed, uint64_t traj, int64_t step0,
 PYCD_API int pycd_debug_exp(const double* d_x, int64_t n, double* d_ours,
                             double* d_cuda, void* stream);
 
+/* ---------------------------------------------------------------------------
+ * Mean squared displacement: Analysis.compute_msd (PyCD/core.py:2974-3081)
+ * on unwrapped trajectory rows already in device memory.
+ * ------------------------------------------------------------------------- */
+#define PYCD_MSD_MAX_SPECIES 64
+#define PYCD_MSD_MAX_TYPES 32
+
+typedef struct PycdMsdDesc {
+  const double* d_rows;     /* row r of trajectory t at d_rows + t*traj_stride
+                             * + r*row_stride: 3 coordinates per carrier, in
+                             * bohr, carriers grouped by species type        */
+  int64_t n_traj;
+  int64_t n_rows;           /* rows used per trajectory (core.py:2947-2948)  */
+  int64_t traj_stride;      /* doubles                                       */
+  int64_t row_stride;       /* doubles, >= 3 * n_species                     */
+  int32_t n_species;        /* carriers per row, 1..PYCD_MSD_MAX_SPECIES     */
+  int32_t n_types;          /* species types present, 1..PYCD_MSD_MAX_TYPES  */
+  int32_t type_count[PYCD_MSD_MAX_TYPES]; /* carriers per present type, > 0,
+                             * summing to n_species (core.py:3009-3024)      */
+  int64_t n_lags;           /* lags 0..n_lags-1 (core.py:2971-2972)          */
+  int64_t trim_length;      /* slope fit on lags [trim, n_lags - trim)       */
+  double dist_conversion;   /* bohr -> output length unit                    */
+  double time_interval;     /* atomic units                                  */
+  double time_conversion;   /* atomic time -> output time unit               */
+} PycdMsdDesc;
+
+/* Squared displacements and their averages, replacing the NumPy loops of
+ * Analysis.compute_msd (core.py:2983-3034, 3053-3060).  Outputs (device,
+ * float64, C order):
+ *   d_sd          n_traj x n_lags x n_species: mean over every pair of rows
+ *                 `lag` apart of the squared displacement (lag 0 = 0; NaN
+ *                 when lag >= n_rows, as the reference's empty mean)
+ *   d_species_avg n_traj x n_lags x n_types   (core.py:3006-3024)
+ *   d_msd_data    n_lags x (n_types + 1): time column, then the mean over
+ *                 trajectories                (core.py:3026-3033)
+ *   d_sem_data    n_lags x n_types: population std / sqrt(n_traj) (3034)
+ *   d_slopes      n_traj x n_types: least-squares slope of species_avg on
+ *                 the time column over the trimmed lags (core.py:3053-3060)
+ *   d_slope_stats 2 x n_types: mean and std / sqrt(n_traj) of d_slopes
+ * Any output but d_sd may be NULL only if every later one is NULL too
+ * (each is computed from the previous).  Asynchronous on `stream`.         */
+PYCD_API int pycd_msd_compute(const PycdMsdDesc* desc, double* d_sd,
+                              double* d_species_avg, double* d_msd_data,
+                              double* d_sem_data, double* d_slopes,
+                              double* d_slope_stats, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

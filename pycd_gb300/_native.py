@@ -97,6 +97,19 @@ class KmcLaunch(C.Structure):
                 ("max_carriers", C.c_int32), ("min_blocks_per_sm", C.c_int32)]
 
 
+MSD_MAX_SPECIES = 64
+MSD_MAX_TYPES = 32
+
+
+class MsdDesc(C.Structure):
+    _fields_ = [("d_rows", C.c_void_p), ("n_traj", C.c_int64), ("n_rows", C.c_int64),
+                ("traj_stride", C.c_int64), ("row_stride", C.c_int64),
+                ("n_species", C.c_int32), ("n_types", C.c_int32),
+                ("type_count", C.c_int32 * MSD_MAX_TYPES), ("n_lags", C.c_int64),
+                ("trim_length", C.c_int64), ("dist_conversion", C.c_double),
+                ("time_interval", C.c_double), ("time_conversion", C.c_double)]
+
+
 P = C.POINTER
 _PROTOS = {
     "pycd_last_error": (C.c_char_p, []),
@@ -132,6 +145,8 @@ _PROTOS = {
                                         C.c_int32, C.c_void_p, C.c_void_p]),
     "pycd_debug_exp": (C.c_int, [C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p,
                                  C.c_void_p]),
+    "pycd_msd_compute": (C.c_int, [P(MsdDesc), C.c_void_p, C.c_void_p, C.c_void_p,
+                                   C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
 }
 
 _lib = None

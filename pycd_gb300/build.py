@@ -21,7 +21,8 @@ LIB = OUT_DIR / "libpycd_gb300.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC",
               "-Xcompiler", "-fvisibility=hidden", "--expt-relaxed-constexpr"]
-SOURCES = ["capi.cu", "ewald.cu", "ewald_split.cu", "kmc.cu", "kmc_capped.cu"]
+SOURCES = ["capi.cu", "ewald.cu", "ewald_split.cu", "kmc.cu", "kmc_capped.cu",
+           "msd.cu"]
 
 
 def _nvcc():

@@ -38,6 +38,8 @@ int ewald_build(const PycdEwaldDesc* d, int mode, double* out, void* ws,
                 float* fourier_ms);
 int potential_gemv(const double* A, int64_t n, const double* q, double* phi,
                    double* energy, cudaStream_t s);
+int msd_compute(const PycdMsdDesc& d, double* sd, double* avg, double* msd, double* sem,
+                double* slopes, double* stats, cudaStream_t s);
 int potential_sparse(const double* A, int64_t n, const int32_t* idx,
                      const double* q, int32_t m, double* phi, cudaStream_t s);
 
@@ -347,6 +349,41 @@ int pycd_kmc_rate_coefficients(const PycdKmcSystem* system, double* d_out,
                "pycd_kmc_rate_coefficients: bad arguments");
   PYCD_REQUIRE(((uintptr_t)d_out & 15) == 0, "d_out must be 16-byte aligned");
   return kmc_coef_launch(*system, (double2*)d_out, (cudaStream_t)stream);
+}
+
+int pycd_msd_compute(const PycdMsdDesc* desc, double* d_sd, double* d_species_avg,
+                     double* d_msd_data, double* d_sem_data, double* d_slopes,
+                     double* d_slope_stats, void* stream) {
+  clear_error();
+  PYCD_REQUIRE(desc && desc->d_rows && d_sd, "pycd_msd_compute: NULL descriptor or output");
+  const PycdMsdDesc& d = *desc;
+  PYCD_REQUIRE(d.n_traj >= 1 && d.n_rows >= 1 && d.n_lags >= 1,
+               "n_traj, n_rows and n_lags must be >= 1");
+  PYCD_REQUIRE(d.n_species >= 1 && d.n_species <= PYCD_MSD_MAX_SPECIES,
+               "n_species must be in [1, %d] (got %d)", PYCD_MSD_MAX_SPECIES, d.n_species);
+  PYCD_REQUIRE(d.row_stride >= 3 * (int64_t)d.n_species,
+               "row_stride (%lld) must hold 3 * n_species doubles", (long long)d.row_stride);
+  PYCD_REQUIRE(d.n_traj == 1 || d.traj_stride >= d.n_rows * d.row_stride,
+               "traj_stride must hold n_rows rows");
+  PYCD_REQUIRE(d.n_types >= 1 && d.n_types <= PYCD_MSD_MAX_TYPES,
+               "n_types must be in [1, %d]", PYCD_MSD_MAX_TYPES);
+  int total = 0;
+  for (int k = 0; k < d.n_types; ++k) {
+    PYCD_REQUIRE(d.type_count[k] > 0, "type_count[%d] must be > 0", k);
+    total += d.type_count[k];
+  }
+  PYCD_REQUIRE(total == d.n_species, "type counts sum to %d, not n_species %d", total,
+               d.n_species);
+  PYCD_REQUIRE(!(d_slopes || d_slope_stats) ||
+                   (d.trim_length >= 0 && d.n_lags - 2 * d.trim_length >= 2),
+               "the slope fit needs at least 2 lags in [trim, n_lags - trim)");
+  PYCD_REQUIRE(d_species_avg || !(d_msd_data || d_sem_data || d_slopes || d_slope_stats),
+               "later MSD outputs need d_species_avg");
+  PYCD_REQUIRE(d_msd_data || !(d_sem_data || d_slopes || d_slope_stats),
+               "later MSD outputs need d_msd_data");
+  PYCD_REQUIRE(d_slopes || !d_slope_stats, "d_slope_stats needs d_slopes");
+  return msd_compute(d, d_sd, d_species_avg, d_msd_data, d_sem_data, d_slopes,
+                     d_slope_stats, (cudaStream_t)stream);
 }
 
 int pycd_debug_exp(const double* d_x, int64_t n, double* d_ours, double* d_cuda,

@@ -25,6 +25,11 @@ produced by the reference's code or ships with it:
       the 3,600-site lattice with 4 electrons and 4 fixed +1 dopants: the
       reference's event stream for a 2,000-step prefix of two trajectories,
       run on the oracle's array and our hop list (both pinned above).
+  msd.json/.npz
+      Analysis.compute_msd of the reference on the shipped Hematite
+      trajectory (examples/Hematite/traj1, with the example's MSD parameters)
+      and on three synthetic random-walk trajectories with three species
+      types, one of them empty: MSD table, SEM table and report lines.
 """
 import hashlib
 import json
@@ -468,8 +473,70 @@ def corundum3600(core):
     (HERE / "corundum3600.json").write_text(json.dumps(cfg, indent=1))
 
 
+def _ref_msd(core, rows_per_traj, species_types, species_count, params):
+    """Run the reference's Analysis.compute_msd on trajectory files written
+    the way do_kmc_steps writes them (traj{i}/unwrapped_traj.npy)."""
+    mat = types.SimpleNamespace(num_species_types=len(species_types),
+                                species_types=list(species_types))
+    with tempfile.TemporaryDirectory() as d:
+        d = Path(d)
+        for i, rows in enumerate(rows_per_traj):
+            (d / f"traj{i + 1}").mkdir()
+            np.save(d / f"traj{i + 1}" / "unwrapped_traj.npy", rows)
+        an = core.Analysis(mat, params["n_dim"], np.asarray(species_count),
+                           len(rows_per_traj), params["t_final"], params["time_interval"],
+                           params["msd_t_final"], params["trim_length"], params["temp"],
+                           params["repr_time"], params["repr_dist"])
+        out = an.compute_msd(d, {"unwrapped_traj": {"file_name": "unwrapped_traj.npy"}})
+        msd_file = d / ("MSD_Data_" + out.file_name + ".npy")
+        saved = np.load(msd_file)
+        report = (d / ("MSD_Analysis_" + out.file_name + ".log")).read_text()
+    assert np.array_equal(saved, out.msd_data)
+    prefix = report[:report.index("Time elapsed")]
+    return out, prefix
+
+
+def msd(core):
+    """MSD fixtures: the shipped Hematite trajectory with the example's own
+    MSD parameters (examples/Hematite/simulation_parameters.yml), and a
+    synthetic 3-trajectory case with three species types, one of them empty."""
+    hem_params = {"n_dim": 3, "t_final": 1e-4, "time_interval": 1e-8,
+                  "msd_t_final": 5000.0, "trim_length": 50, "temp": 300,
+                  "repr_time": "ns", "repr_dist": "angstrom"}
+    hem_rows = np.load(REF / "examples" / "Hematite" / "traj1" / "unwrapped_traj.npy")
+    hem, hem_prefix = _ref_msd(core, [hem_rows], ["electron", "hole"], [1, 0], hem_params)
+    # synthetic: 2 electrons + 0 holes + 1 "ion" per trajectory, random walks
+    # of bohr-sized hops, 301 rows per trajectory
+    syn_params = {"n_dim": 3, "t_final": 3e-6, "time_interval": 1e-8,
+                  "msd_t_final": 1000.0, "trim_length": 10, "temp": 450,
+                  "repr_time": "ns", "repr_dist": "angstrom"}
+    rng = np.random.default_rng(11)
+    syn_rows = []
+    for t in range(3):
+        steps = rng.normal(0.0, 5.5, size=(301, 9))
+        steps[0] = 0.0
+        syn_rows.append(np.cumsum(steps, axis=0))
+    syn, syn_prefix = _ref_msd(core, syn_rows, ["electron", "hole", "ion"], [2, 0, 1],
+                               syn_params)
+    np.savez_compressed(HERE / "msd.npz", hem_rows=hem_rows, hem_msd=hem.msd_data,
+                        hem_sem=hem.sem_data, syn_rows=np.stack(syn_rows),
+                        syn_msd=syn.msd_data, syn_sem=syn.sem_data)
+    cfg = {"hematite": dict(hem_params, species_types=["electron", "hole"],
+                            species_count=[1, 0], n_traj=1, file_name=hem.file_name,
+                            out_species=hem.species_types, report_prefix=hem_prefix),
+           "synthetic": dict(syn_params, species_types=["electron", "hole", "ion"],
+                             species_count=[2, 0, 1], n_traj=3, file_name=syn.file_name,
+                             out_species=syn.species_types, report_prefix=syn_prefix,
+                             rows_seed=11)}
+    (HERE / "msd.json").write_text(json.dumps(cfg, indent=1))
+    print("msd:", hem.file_name, hem_prefix.strip().replace("\n", " | "))
+    print("msd:", syn.file_name, syn_prefix.strip().replace("\n", " | "))
+
+
 def main(parts):
     core = install_shims()
+    if "msd" in parts:
+        msd(core)
     if "hematite" in parts:
         example(core, "Hematite", HEMATITE, 1e-4)
     if "bvo" in parts:
@@ -481,4 +548,4 @@ def main(parts):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1:] or ["hematite", "bvo", "corundum324", "corundum3600"])
+    main(sys.argv[1:] or ["hematite", "bvo", "corundum324", "corundum3600", "msd"])
