@@ -394,6 +394,76 @@ __device__ __forceinline__ void process_rates(const ProcCache<MAXP>& pc, double 
   }
 }
 
+// ---------------------------------------------------------------------------
+// Residence times t -= log(u2) / k_tot (core.py:2802-2803), deferred.
+//
+// The exact FP64 chain is what the reference computes; only its timing
+// changes.  Lane j keeps step j of a window of up to G steps; an upper bound
+// of the elapsed time is accumulated in FP32 with upward rounding (integer
+// bit operations and the FP32 pipe only).  While the bound stays below
+// `slack` (the gap to t_guard minus the rounding of G chained subtractions),
+// no grid boundary can have been reached and the exact time is not needed.
+// A flush divides the pending steps in parallel, one per lane, and applies
+// the G subtractions in step order: the same doubles as one division and one
+// subtraction per step, at about a G-th of the FP64 divisions.
+// ---------------------------------------------------------------------------
+// float >= x for a double x >= 0 (integer operations only)
+__device__ __forceinline__ float f32_above(double x) {
+  const unsigned hi = (unsigned)__double2hiint(x) & 0x7fffffffu;
+  const int e = (int)(hi >> 20) - 1023 + 127;
+  if (e >= 255) return INFINITY;
+  if (e <= 0) return (hi == 0 && __double2loint(x) == 0) ? 0.0f : 0x1p-126f;
+  return __uint_as_float((((unsigned)e << 23) | ((hi & 0xfffffu) << 3)) + 1u);
+}
+// float <= x for a double x >= 0 (integer operations only)
+__device__ __forceinline__ float f32_below(double x) {
+  const unsigned hi = (unsigned)__double2hiint(x) & 0x7fffffffu;
+  const int e = (int)(hi >> 20) - 1023 + 127;
+  if (e >= 255) return 3.4028234663852886e38f;
+  if (e <= 0) return 0.0f;
+  return __uint_as_float(((unsigned)e << 23) | ((hi & 0xfffffu) << 3));
+}
+
+template <int G>
+struct TimeChain {
+  double kt = 1.0, nlu2 = 0.0;  // this lane's pending step: k_tot, log(u2)
+  int npend = 0;
+  float bound = 0.0f, slack = -1.0f;
+
+  // slack = (t_guard - t) - 2^(e(t_guard) - 46) >= the rounding of up to 32
+  // chained subtractions below t_guard, as a float rounded down
+  // (a t_guard below 2^-975 keeps the chain exact at every step)
+  __device__ __forceinline__ void reset(double t_guard, double t) {
+    bound = 0.0f;
+    slack = -1.0f;
+    const int ef = (__double2hiint(t_guard) >> 20) & 0x7ff;
+    if (ef <= 47 || ef == 0x7ff) return;
+    const double m = __hiloint2double((ef - 46) << 20, 0);  // 64 ulp(t_guard)
+    const double gap = dsub(dsub(t_guard, t), m);
+    if (__double_as_longlong(gap) > 0) slack = f32_below(gap);
+  }
+  // record this step; true when the exact time is needed now
+  __device__ __forceinline__ bool push(int g, double ktot, double lu2, bool force) {
+    if (g == npend) { kt = ktot; nlu2 = lu2; }
+    ++npend;
+    // -lu2 / ktot <= above(-lu2) / below(ktot), rounded up, with room for
+    // the rounding of the double quotient
+    const float inc = __fmul_ru(__fdiv_ru(f32_above(-lu2), f32_below(ktot)),
+                                1.0f + 0x1p-20f);
+    bound = __fadd_ru(bound, inc);
+    return force || npend == G || !(bound < slack);
+  }
+  __device__ __forceinline__ void flush(int g, unsigned gmask, double& t) {
+    const double q = (g < npend) ? ddiv(nlu2, kt) : 0.0;
+#pragma unroll
+    for (int j = 0; j < G; ++j) {
+      const double qj = gshfl<G>(gmask, q, j);
+      if (j < npend) t = dsub(t, qj);
+    }
+    npend = 0;
+  }
+};
+
 // One group of G lanes advances one trajectory by up to max_steps steps.
 template <int G, int MAXP>
 __device__ void advance_trajectory(const KmcArgs& a, int64_t t, int g,
@@ -465,6 +535,10 @@ __device__ void advance_trajectory(const KmcArgs& a, int64_t t, int g,
                     : nullptr;
   // below t_guard the quotient sim_time / dt cannot reach start_path + 1
   double t_guard = dmul(dmul((double)(start_path + 1), dt_grid), 1.0 - 0x1p-40);
+  TimeChain<G> tc;
+  tc.reset(t_guard, sim_time);
+  // per-step times are an output: keep the chain exact every step
+  const bool exact_each_step = a.out.d_step_time != nullptr;
 
   // uniforms of steps pre_base + g, prepared G at a time
   double pre_u1 = 0.0, pre_lu2 = 0.0;
@@ -568,9 +642,11 @@ __device__ void advance_trajectory(const KmcArgs& a, int64_t t, int g,
     if (sel >= NP) { status = PYCD_TRAJ_NO_EVENT; break; }
 
     // ---- residence time (core.py:2802-2804) ---------------------------
-    sim_time = dsub(sim_time, ddiv(lu2, ktot));
+    const bool exact = tc.push(g, ktot, lu2, exact_each_step);
+    if (exact) tc.flush(g, gmask, sim_time);
     int64_t end_path = start_path - 1;
-    if (!nonneg_gt(t_guard, sim_time)) {  // sim_time >= t_guard, both >= +0
+    // without a flush sim_time < t_guard is guaranteed by the bound
+    if (exact && !nonneg_gt(t_guard, sim_time)) {  // sim_time >= t_guard, both >= +0
       const double tq = ddiv(sim_time, dt_grid);
       end_path = (tq < 9.0e18) ? (int64_t)tq : INT64_MAX;
     }
@@ -662,7 +738,9 @@ __device__ void advance_trajectory(const KmcArgs& a, int64_t t, int g,
       t_guard = dmul(dmul((double)(start_path + 1), dt_grid), 1.0 - 0x1p-40);
     }
     if (end_path >= n_path) { status = PYCD_TRAJ_DONE; break; }
+    if (exact) tc.reset(t_guard, sim_time);
   }
+  if (tc.npend > 0) tc.flush(g, gmask, sim_time);
 
   // ---- write the state back ---------------------------------------------
   if (csum) {

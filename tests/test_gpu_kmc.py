@@ -247,3 +247,41 @@ def test_event_stream_independent_of_launch_shape(cuda_ready):
         assert np.array_equal(r[0], results[0][0])
         assert np.array_equal(r[1], results[0][1])
         assert np.array_equal(r[2], results[0][2])
+
+
+def test_deferred_times_equal_exact_chain_across_shapes(cuda_ready):
+    """Without per-step time output the kernel defers the residence-time
+    divisions (bounded in FP32, exact FP64 chain at grid crossings and every
+    G steps).  On a fine time grid (a crossing every ~50 steps) the rows,
+    energies, final times and sites must equal the every-step exact chain
+    bit for bit, for every launch shape."""
+    import torch
+    cfg, arr = gio.load("corundum324")
+    mat, nb = gio.material(cfg)
+    sysm = System(mat, nb, gio.hop_list(cfg, arr), None, cfg["params"]["alpha"],
+                  cfg["params"]["r_cut"], cfg["params"]["k_cut"])
+    A = sysm.get_precomputed_array_device("fp64")
+    tables, run = wl.batched_tables(sysm, A, 2, [], t_final=1e-9, time_interval=2e-12)
+    rows = tables.n_path_steps
+    rng = np.random.default_rng(3)
+    occ = np.stack([rng.choice(324, size=2, replace=False) for _ in range(48)])
+
+    def run_until_done(lanes, exact):
+        eng = KmcEngine(tables, launch={"lanes_per_traj": lanes})
+        b = KmcBatch(occ, unwrapped_rows=rows, energy_grid_rows=rows,
+                     step_capacity=1 if exact else 0)
+        for _ in range(100):
+            eng.advance(b, 20000, eng.rng_struct(seed=31))
+            if (b.status.cpu().numpy() == nat.TRAJ_DONE).all():
+                break
+        torch.cuda.synchronize()
+        assert (b.status.cpu().numpy() == nat.TRAJ_DONE).all()
+        return {k: getattr(b, k).cpu().numpy() for k in
+                ("unwrapped", "energy_grid", "time", "occ", "step")}
+
+    ref = run_until_done(8, exact=True)
+    assert ref["step"].min() > 10 * rows  # many crossings per trajectory
+    for lanes in (4, 8, 16, 32):  # 2 and 1 or 4 processes per lane
+        got = run_until_done(lanes, exact=False)
+        for k in ref:
+            assert np.array_equal(got[k], ref[k]), (lanes, k)
