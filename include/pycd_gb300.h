@@ -37,7 +37,7 @@
 extern "C" {
 #endif
 
-#define PYCD_ABI_VERSION 1
+#define PYCD_ABI_VERSION 2
 
 #if defined(__GNUC__)
 #define PYCD_API __attribute__((visibility("default")))
@@ -116,7 +116,17 @@ typedef struct PycdEwaldDesc {
   double r_cut;                 /* real-space cutoff (bohr), strict <        */
   double volume;                /* cell volume used by the Fourier prefactor */
   double dielectric;            /* relative permittivity                     */
+  int32_t parts;                /* PYCD_EWALD_PART_* mask of the terms to
+                                 * build; 0 = all.  The real part alone is
+                                 * get_precomputed_array_real (core.py:1594-
+                                 * 1596), the Fourier part alone
+                                 * get_precomputed_array_fourier (1598-1602)  */
 } PycdEwaldDesc;
+
+#define PYCD_EWALD_PART_REAL 1     /* erfc(sqrt(alpha) r)/(2 r eps), r < r_cut */
+#define PYCD_EWALD_PART_FOURIER 2  /* the k-space sum / eps                  */
+#define PYCD_EWALD_PART_SELF 4     /* -sqrt(alpha/pi)/eps on the diagonal    */
+#define PYCD_EWALD_PART_ALL 7
 
 /* Enumerate the half-space k-vector list of PyCD/core.py:816-838 filtered by
  * k^2 < k_cut^2 (PyCD/core.py:868), in the reference's order, on the host.
@@ -278,8 +288,9 @@ typedef struct PycdKmcRng {
  * shape maxima are filled by pycd_kmc_upload_systems and are required by
  * pycd_kmc_advance_uploaded (pycd_kmc_advance computes them itself).       */
 typedef struct PycdKmcLaunch {
-  int32_t lanes_per_traj;       /* 1..32 (power of two); 0 = from processes  */
-  int32_t warps_per_block;      /* 1..8; 0 = 4                               */
+  int32_t lanes_per_traj;       /* 1..32 (power of two); 0 = about 2 processes
+                                 * per lane, at least one lane per carrier   */
+  int32_t warps_per_block;      /* 1..8; 0 = 1                               */
   int32_t blocks;               /* grid size; 0 = cover all trajectories     */
   int32_t max_processes;        /* max n_carriers * n_slots over the systems */
   int32_t max_carriers;         /* max n_carriers over the systems           */

@@ -17,12 +17,18 @@ import numpy as np
 
 from . import constants
 from . import _native as nat
+from .ewald_params import EwaldParameterSearch
 from .io import generate_report
 from .lattice import Material, Neighbors, ReturnValues  # noqa: F401
 
 
-class System(object):
-    """Ewald geometry and parameters (PyCD/core.py:671-797)."""
+def _numeric(v):
+    return not isinstance(v, str) and bool(np.isreal(v))
+
+
+class System(EwaldParameterSearch):
+    """Ewald geometry and parameters (PyCD/core.py:671-797); the automatic
+    parameter choices of PyCD/core.py:913-1592 come from EwaldParameterSearch."""
 
     def __init__(self, material_info, material_neighbors, hop_neighbor_list,
                  pairwise_min_image_vector_data, alpha, r_cut, k_cut,
@@ -74,25 +80,30 @@ class System(object):
         else:
             self.k_cut = k_cut
         self.precision_parameters = precision_parameters
+        if precision_parameters is not None:
+            self._load_precision_parameters(precision_parameters)
         self.last_build_info = None
 
+    def _user_specified(self):
+        return (_numeric(self.alpha) and _numeric(self.r_cut)
+                and (isinstance(self.k_cut, list) or _numeric(self.k_cut)))
+
     def _ewald_parameters(self):
-        """Numeric alpha / r_cut / k_cut (user-specified, or a k_max list as
-        core.py:1377-1382).  The automatic choices ('optimal', 'converge',
-        'simulation_cell') are parameter searches outside this hot path."""
-        if not (np.isreal(self.alpha) and np.isreal(self.r_cut)):
-            raise NotImplementedError(
-                "automatic Ewald parameter selection is not part of this "
-                "package; give numeric alpha and r_cut")
+        """Numeric alpha / r_cut / k_cut: user-specified, or a k_max list as
+        core.py:1377-1382, or the result of the automatic selection
+        (get_ewald_parameters, run once and kept)."""
+        if not self._user_specified():
+            chosen = getattr(self, "_chosen_parameters", None)
+            if chosen is None:
+                raise ValueError("automatic Ewald parameters are chosen by "
+                                 "get_precomputed_array(dst_path, ...) first")
+            return chosen
         if isinstance(self.k_cut, list):
             k_cut = 1.10 * max(np.asarray(self.k_cut)
                                * self.reciprocal_lattice_vector_length)
             choice = "user-specified (k_max)"
-        elif np.isreal(self.k_cut):
-            k_cut, choice = self.k_cut, "user-specified"
         else:
-            raise NotImplementedError("automatic k_cut selection is not part "
-                                      "of this package")
+            k_cut, choice = self.k_cut, "user-specified"
         return float(self.alpha), float(self.r_cut), float(k_cut), choice
 
     def get_precomputed_array_device(self, precision="auto", pmiv="system",
@@ -107,39 +118,68 @@ class System(object):
 
     def get_precomputed_array(self, dst_path, compute_energy_contributions=0,
                               return_k_vector_data=0, precision="auto"):
-        """(A, dst_path) with A the (N, N) float64 host array, plus the
-        ``precomputed_array.log`` report of PyCD/core.py:1675-1678."""
+        """(A, dst_path) with A the (N, N) float64 host array and the
+        ``precomputed_array.log`` report of PyCD/core.py:1611-1679.
+
+        User-specified alpha, r_cut and k_cut (or a k_max list) are built
+        directly; any automatic choice ('optimal', 'converge',
+        'simulation_cell') first runs get_ewald_parameters, whose energy scans
+        run on the GPU, and may move dst_path as the reference does.  The
+        report keeps the reference's lines (alpha on line 4, which
+        material_run reads) and adds the k-vector count and build mode."""
         import torch
-        alpha, r_cut, k_cut, kchoice = self._ewald_parameters()
+        a2b = constants.ANG2BOHR
+        if self._user_specified():
+            alpha, r_cut, k_cut, kchoice = self._ewald_parameters()
+            choice = {"alpha": "user-specified", "r_cut": "user-specified",
+                      "k_cut": kchoice}
+            lines = None
+        else:
+            if self.precision_parameters is None:
+                raise ValueError("automatic Ewald parameters need precision_parameters")
+            dst_path = Path(dst_path)
+            params, lines, dst_path = self.get_ewald_parameters([], dst_path)
+            alpha, r_cut, k_cut = (float(params["alpha"]), float(params["r_cut"]),
+                                   float(params["k_cut"]))
+            self._chosen_parameters = (alpha, r_cut, k_cut, "chosen")
         A_dev = self.get_precomputed_array_device(precision)
         torch.cuda.synchronize()
         A = A_dev.cpu().numpy()
         info = self.last_build_info
+        n = self.neighbors.num_system_elements
+        if lines is None:
+            # timing lines from this build's own real / Fourier phases
+            tau_r = info["real_ms"] / max(1, n * n)
+            tau_f = info["fourier_ms"] / max(1, n * n * max(1, info["n_kvec"]))
+            lines = [
+                f"tau_ratio, (tau_r/tau_f): {tau_r / tau_f if tau_f else 0.0:.3e}\n",
+                f"time_ratio, (time_r/time_f): "
+                f"{info['real_ms'] / info['fourier_ms'] if info['fourier_ms'] else 0.0:.3e}\n\n",
+                f"alpha: {alpha * a2b:.3e} / angstrom ({choice['alpha']})\n",
+                f"r_cut: {r_cut / a2b:.3e} angstrom ({choice['r_cut']})\n",
+                f"k_cut: {k_cut * a2b:.3e} / angstrom ({choice['k_cut']})\n"]
+            q = self.base_charge_config_for_accuracy_analysis("full")
+            einsum = float(np.einsum("ii", np.multiply(q.transpose(), q)))
+            lines = self.compute_cutoff_errors(einsum, alpha, r_cut, k_cut,
+                                               np.power(self.system_volume, 1 / 3), lines)
         k_max = info["k_max"]
         num_k_vectors = int(np.ceil(np.prod(2 * k_max + 1) * np.pi / 6 - 1))
-        n = self.neighbors.num_system_elements
-        tau_r = info["real_ms"] / max(1, n * n)
-        tau_f = info["fourier_ms"] / max(1, n * n * max(1, info["n_kvec"]))
-        lines = [
-            f"tau_ratio, (tau_r/tau_f): {tau_r / tau_f if tau_f else 0.0:.3e}\n",
-            f"time_ratio, (time_r/time_f): "
-            f"{info['real_ms'] / info['fourier_ms'] if info['fourier_ms'] else 0.0:.3e}\n\n",
-            f"alpha: {alpha * constants.ANG2BOHR:.3e} / angstrom (user-specified)\n",
-            f"r_cut: {r_cut / constants.ANG2BOHR:.3e} angstrom (user-specified)\n",
-            f"k_cut: {k_cut * constants.ANG2BOHR:.3e} / angstrom ({kchoice})\n",
-            f"k_max: [{k_max[0]}, {k_max[1]}, {k_max[2]}]\n",
-            f"number of k-vectors: {num_k_vectors}\n",
-            f"k-vectors used: {info['n_kvec']}\n",
-            f"build: {info['mode']} on the GPU\n\n",
-        ]
+        lines += [f"k_max: [{k_max[0]}, {k_max[1]}, {k_max[2]}]\n",
+                  f"number of k-vectors: {num_k_vectors}\n\n"]
         if compute_energy_contributions:
-            m = self.material
-            q = np.tile(np.array([m.charge_types["full"][m.element_types[e]]
-                                  for e in m.element_type_index_list]),
-                        self.num_cells)
-            total = float(q @ A @ q)
-            lines.append(f"Total system energy (neutral): "
-                         f"{total / constants.EV2HARTREE} eV\n\n")
+            # core.py:1662-1673, each part's energy on the device
+            ev = self._energy_evaluator("full")
+            e_real = ev.real(alpha, r_cut)
+            e_fourier = ev.fourier(alpha, k_cut)
+            e_self = ev.self_term(alpha)
+            eh = constants.EV2HARTREE
+            lines += [f"Energy contribution from Real space: {e_real / eh} eV\n",
+                      f"Energy contribution from Fourier-space: {e_fourier / eh} eV\n",
+                      f"Energy contribution from self-interactions: {e_self / eh} eV\n",
+                      f"Total system energy (neutral): "
+                      f"{(e_real + e_fourier + e_self) / eh} eV\n\n"]
+        lines += [f"k-vectors used: {info['n_kvec']}\n",
+                  f"build: {info['mode']} on the GPU\n\n"]
         if dst_path is not None:
             Path(dst_path).mkdir(parents=True, exist_ok=True)
             generate_report(self.start_time, Path(dst_path), "precomputed_array",

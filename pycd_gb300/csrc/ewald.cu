@@ -397,6 +397,8 @@ int ewald_validate(const PycdEwaldDesc* d, int mode) {
   PYCD_REQUIRE(d->n_kvec == 0 || d->d_kvec != nullptr, "d_kvec is NULL");
   PYCD_REQUIRE(d->d_cart != nullptr || d->d_pmiv != nullptr,
                "need d_cart or d_pmiv");
+  PYCD_REQUIRE(d->parts >= 0 && d->parts <= PYCD_EWALD_PART_ALL,
+               "parts must be a mask of PYCD_EWALD_PART_* (got %d)", d->parts);
   PYCD_REQUIRE(d->alpha > 0.0 && d->volume > 0.0 && d->dielectric != 0.0,
                "alpha, volume must be > 0 and dielectric != 0");
   PYCD_REQUIRE(mode >= PYCD_EWALD_FP64_DIRECT && mode <= PYCD_EWALD_TF32X3,
@@ -431,7 +433,12 @@ int ewald_build(const PycdEwaldDesc* d, int mode, double* out, void* ws,
   }
   EwaldWs w;
   ewald_ws_layout(d, mode, &w, (char*)ws);
-  const int64_t n = d->n_sites, K = d->n_kvec;
+  const int parts = d->parts ? d->parts : PYCD_EWALD_PART_ALL;
+  const int64_t n = d->n_sites;
+  // a part left out contributes exactly zero: no k-vectors, no pair passes
+  // the cutoff (the diagonal's r = 0 included), a zero self term
+  const int64_t K = (parts & PYCD_EWALD_PART_FOURIER) ? d->n_kvec : 0;
+  const double r_cut = (parts & PYCD_EWALD_PART_REAL) ? d->r_cut : -1.0;
   Mat3 recip, cell, inv;
   for (int c = 0; c < 9; ++c) {
     recip.m[c] = d->recip[c];
@@ -460,11 +467,12 @@ int ewald_build(const PycdEwaldDesc* d, int mode, double* out, void* ws,
   g.pbc[0] = d->pbc[0]; g.pbc[1] = d->pbc[1]; g.pbc[2] = d->pbc[2];
   g.n = n;
   const double sqrt_alpha = sqrt(d->alpha);
-  const double self_term = -(sqrt(d->alpha / M_PI)) / d->dielectric;
+  const double self_term =
+      (parts & PYCD_EWALD_PART_SELF) ? -(sqrt(d->alpha / M_PI)) / d->dielectric : 0.0;
   dim3 grid((unsigned)((n + 255) / 256), (unsigned)n);
   if (mode == PYCD_EWALD_FP64_DIRECT) {
     ewald_pair_kernel<true><<<grid, 256, 512 * 5 * sizeof(double), s>>>(
-        g, sqrt_alpha, d->r_cut, d->dielectric, self_term, w.kc, w.k2,
+        g, sqrt_alpha, r_cut, d->dielectric, self_term, w.kc, w.k2,
         w.ck, K, out);
     PYCD_CUDA(cudaGetLastError());
     if (timing) {
@@ -473,7 +481,7 @@ int ewald_build(const PycdEwaldDesc* d, int mode, double* out, void* ws,
     }
   } else {
     ewald_pair_kernel<false><<<grid, 256, 0, s>>>(
-        g, sqrt_alpha, d->r_cut, d->dielectric, self_term, w.kc, w.k2,
+        g, sqrt_alpha, r_cut, d->dielectric, self_term, w.kc, w.k2,
         w.ck, 0, out);
     PYCD_CUDA(cudaGetLastError());
     if (timing) PYCD_CUDA(cudaEventRecord(e1, s));

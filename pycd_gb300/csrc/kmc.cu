@@ -51,8 +51,14 @@ static int pow2_at_least(int v) {
 
 int kmc_launch(const KmcArgs& a, int max_np, int max_nc,
                const PycdKmcLaunch* launch, cudaStream_t s) {
+  // default: about two processes per lane (the measured optimum for FP64
+  // issue per trajectory) and at least one lane per carrier
   int G = launch && launch->lanes_per_traj ? launch->lanes_per_traj : 0;
-  if (G == 0) G = pow2_at_least(max_np < 16 ? max_np : 16);
+  if (G == 0) {
+    const int half = (max_np + 1) / 2;
+    G = pow2_at_least(half < 32 ? half : 32);
+    if (G < 2 && max_np > 1) G = 2;  // one lane runs only a single process
+  }
   if (G < max_nc) G = pow2_at_least(max_nc);
   PYCD_REQUIRE(G >= 1 && G <= 32 && (G & (G - 1)) == 0,
                "lanes_per_traj must be a power of two in [1, 32] (got %d)", G);
@@ -62,7 +68,8 @@ int kmc_launch(const KmcArgs& a, int max_np, int max_nc,
   const int MAXP = need <= 1 ? 1 : need <= 2 ? 2 : need <= 4 ? 4 : need <= 8 ? 8 : 16;
   PYCD_REQUIRE(MAXP <= 8, "processes per trajectory (%d) exceed 8 per lane at "
                "%d lanes", max_np, G);
-  int wpb = launch && launch->warps_per_block ? launch->warps_per_block : 4;
+  // default one-warp blocks: the finest split of the trajectories over SMs
+  int wpb = launch && launch->warps_per_block ? launch->warps_per_block : 1;
   PYCD_REQUIRE(wpb >= 1 && wpb <= 8, "warps_per_block must be in [1, 8]");
   const int minb = launch && launch->min_blocks_per_sm ? launch->min_blocks_per_sm : 1;
   PYCD_REQUIRE(minb == 1 || (minb == 2 && MAXP <= 2),

@@ -101,12 +101,15 @@ def choose_mode(system, pmiv, requested="auto"):
 
 
 def build_device_array(system, alpha, r_cut, k_cut, precision="auto",
-                       pmiv="system", stream=None, out=None):
+                       pmiv="system", stream=None, out=None, parts=0, kvecs=None):
     """Build the N x N FP64 array on the current CUDA device.
 
     Returns ``(A, info)``: ``A`` a CUDA float64 tensor, ``info`` a dict with
     ``mode``, ``k_max``, ``n_kvec`` and the real / Fourier phase times (ms).
     ``pmiv='system'`` uses ``system.pairwise_min_image_vector_data``.
+    ``parts``: a mask of ``_native.EWALD_PART_*`` (0 = the whole array).
+    ``kvecs``: an explicit (K, 3) integer k list instead of the one k_cut
+    selects.
     """
     import torch
     nat.require_device()
@@ -114,7 +117,8 @@ def build_device_array(system, alpha, r_cut, k_cut, precision="auto",
         pmiv = system.pairwise_min_image_vector_data
     n = int(system.neighbors.num_system_elements)
     mode = choose_mode(system, pmiv, precision)
-    desc, keep, k_max = make_desc(system, alpha, r_cut, k_cut, pmiv)
+    desc, keep, k_max = make_desc(system, alpha, r_cut, k_cut, pmiv, kvecs)
+    desc.parts = int(parts)
     dev = keep[0].device
     L = nat.lib()
     code = nat.EWALD_MODES[mode]
@@ -134,13 +138,16 @@ def build_device_array(system, alpha, r_cut, k_cut, precision="auto",
     return out, info
 
 
-def make_desc(system, alpha, r_cut, k_cut, pmiv=None):
+def make_desc(system, alpha, r_cut, k_cut, pmiv=None, kvecs=None):
     """PycdEwaldDesc for `system` on the current CUDA device.  Returns
     (desc, tensors the descriptor points into, k_max)."""
     import torch
     n = int(system.neighbors.num_system_elements)
     k_max = k_max_for(system, k_cut)
-    kv = effective_k_vectors(system.reciprocal_lattice_matrix, k_max, k_cut)
+    if kvecs is None:
+        kv = effective_k_vectors(system.reciprocal_lattice_matrix, k_max, k_cut)
+    else:
+        kv = np.ascontiguousarray(np.asarray(kvecs, dtype=np.int32).reshape(-1, 3))
     dev = torch.device("cuda", torch.cuda.current_device())
     cart = torch.as_tensor(system.neighbors.bulk_sites.cell_coordinates,
                            dtype=torch.float64).contiguous().to(dev)

@@ -25,6 +25,12 @@ produced by the reference's code or ships with it:
       the 3,600-site lattice with 4 electrons and 4 fixed +1 dopants: the
       reference's event stream for a 2,000-step prefix of two trajectories,
       run on the oracle's array and our hop list (both pinned above).
+  ewald_params.json/.npz
+      get_ewald_parameters of the reference on the Hematite example lattice:
+      automatic r_cut, automatic r_cut and k_cut, automatic alpha (2x2x1,
+      shipped pmiv) and the 'converge' k_cut scan of the unit cell (its pmiv
+      from the reference): the choices, the report lines after the timing
+      lines, and the k_cut convergence / k-vector contribution logs.
   msd.json/.npz
       Analysis.compute_msd of the reference on the shipped Hematite
       trajectory (examples/Hematite/traj1, with the example's MSD parameters)
@@ -533,8 +539,89 @@ def msd(core):
     print("msd:", syn.file_name, syn_prefix.strip().replace("\n", " | "))
 
 
+class _Anything(object):
+    """Stand-in for the matplotlib objects the parameter search draws on."""
+
+    def __getattr__(self, name):
+        return _Anything()
+
+    def __call__(self, *a, **k):
+        return _Anything()
+
+
+def _ref_ewald_parameters(core, mat, nb, hop, pmiv, params, tmp):
+    """Run the reference's get_ewald_parameters; return the choice, the
+    report lines after the two timing lines, and the files it wrote."""
+    core.plt = _Anything()
+    ticker = types.ModuleType("matplotlib.ticker")
+    ticker.FormatStrFormatter = _Anything()
+    sys.modules["matplotlib.ticker"] = ticker
+    sys.modules["matplotlib"].ticker = ticker
+    system = make_system(core, mat, nb, hop, pmiv, params)
+    dst = Path(tmp) / "InputFiles"
+    dst.mkdir(parents=True, exist_ok=True)
+    out = {"exit": False}
+    try:
+        ewald, prefix, dst2 = system.get_ewald_parameters([], dst)
+        out.update(alpha=float(ewald["alpha"]), r_cut=float(ewald["r_cut"]),
+                   k_cut=float(ewald["k_cut"]), lines=prefix[2:],
+                   dst_suffix=str(Path(dst2).relative_to(dst)))
+    except SystemExit:
+        out["exit"] = True
+        out["report"] = (dst / "precomputed_array.log").read_text().split("Time elapsed")[0]
+    files = {}
+    for f in sorted(dst.rglob("*.log")):
+        files[str(f.relative_to(dst))] = f.read_text().split("Time elapsed")[0]
+    out["files"] = files
+    return out
+
+
+def ewald_params(core):
+    """Ewald parameter selection fixtures: the reference's own
+    get_ewald_parameters (core.py:1559-1592) on the Hematite example lattice,
+    one case per scan kind.  Timing-dependent output (the tau/time ratios and
+    the all-automatic alpha) is not recorded."""
+    ex = REF / "examples" / "Hematite"
+    poscar = (ex / "InputFiles" / "POSCAR").read_text()
+    hop = np.load(ex / "InputFiles" / "hop_neighbor_list.npy", allow_pickle=True)[()]
+    pmiv221 = np.load(ex / "InputFiles" / "pairwise_min_image_vector_data.npy")
+    cases = {
+        "rcut_optimal": ([2, 2, 1], dict(alpha=0.6, r_cut="optimal", k_cut=6.998)),
+        "rcut_kcut_optimal": ([2, 2, 1], dict(alpha=0.6, r_cut="optimal", k_cut="optimal")),
+        "alpha_optimal": ([2, 2, 1], dict(alpha="optimal", r_cut=4.0, k_cut=6.998)),
+        "kcut_converge": ([1, 1, 1], dict(alpha=0.6, r_cut=2.0, k_cut="converge")),
+    }
+    cfg, arrays = {}, {}
+    for name, (size, over) in cases.items():
+        tmp = tempfile.mkdtemp()
+        # step_change_data_points reaches np.linspace uncast (core.py:797,
+        # 1029): an int, as YAML would load it
+        params = dict(HEMATITE, precision_parameters=dict(PRECISION, step_change_data_points=10),
+                      **over)
+        mat, nb = material_objects(core, params, poscar, size, [1, 1, 1], tmp)
+        if size == [2, 2, 1]:
+            pmiv = pmiv221
+        else:
+            nb.get_pairwise_min_image_vector_data(Path(tmp))
+            pmiv = np.load(Path(tmp) / "pairwise_min_image_vector_data.npy")
+            arrays[name + "|pmiv"] = pmiv
+        t0 = time.time()
+        res = _ref_ewald_parameters(core, mat, nb, hop, pmiv, params, tmp)
+        res["system_size"], res["params"] = size, over
+        res["reference_seconds"] = time.time() - t0
+        cfg[name] = res
+        print(f"ewald_params {name}: {res.get('alpha')}, {res.get('r_cut')}, "
+              f"{res.get('k_cut')} exit={res['exit']} ({res['reference_seconds']:.1f} s)")
+    cfg["poscar"] = poscar
+    cfg["base_params"] = HEMATITE
+    np.savez_compressed(HERE / "ewald_params.npz", **arrays)
+    (HERE / "ewald_params.json").write_text(json.dumps(cfg, indent=1))
+
+
 def main(parts):
     core = install_shims()
+    if "ewald_params" in parts:
+        ewald_params(core)
     if "msd" in parts:
         msd(core)
     if "hematite" in parts:
@@ -548,4 +635,5 @@ def main(parts):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1:] or ["hematite", "bvo", "corundum324", "corundum3600", "msd"])
+    main(sys.argv[1:] or ["hematite", "bvo", "corundum324", "corundum3600", "msd",
+                          "ewald_params"])
