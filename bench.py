@@ -575,10 +575,54 @@ def msd_bench(args):
     print(json.dumps(line), flush=True)
 
 
+def ewald_params_bench(args):
+    """Ewald parameter selection (get_ewald_parameters) on the Hematite
+    example lattice with device energy scans: the cases of the fixtures in
+    tests/golden/ewald_params.json, timed end to end (host logic included).
+    The reference's own NumPy run of the same cases, recorded when the
+    fixtures were made (1 core, x86 host), is given beside each."""
+    import contextlib
+    import io
+    import tempfile
+    sys.path.insert(0, str(ROOT / "tests"))
+    import golden_io as gio
+    from pycd_gb300 import _native as nat
+    from pycd_gb300.core import System
+    nat.require_device()
+    cfg, arr = gio.load("ewald_params")
+    hem_cfg, hem_arr = gio.load("hematite")
+    hop = gio.hop_list(hem_cfg, hem_arr)
+    for name in ("rcut_optimal", "rcut_kcut_optimal", "kcut_converge"):
+        case = cfg[name]
+        mat, nb = gio.material(hem_cfg, system_size=case["system_size"])
+        pmiv = hem_arr["pmiv"] if case["system_size"] == [2, 2, 1] else arr[name + "|pmiv"]
+        p = dict(cfg["base_params"], **case["params"])
+        prec = dict(p["precision_parameters"], step_change_data_points=10)
+        best, builds, chosen = None, 0, None
+        for _ in range(2):  # the first run also loads the kernels
+            sysm = System(mat, nb, hop, pmiv, p["alpha"], p["r_cut"], p["k_cut"], prec)
+            dst = Path(tempfile.mkdtemp()) / "InputFiles"
+            dst.mkdir()
+            t0 = time.perf_counter()
+            with contextlib.redirect_stdout(io.StringIO()):
+                chosen, _, _ = sysm.get_ewald_parameters([], dst)
+            dt = time.perf_counter() - t0
+            best = dt if best is None else min(best, dt)
+            builds = sysm._energy_evaluator().builds
+        ok = all(abs(chosen[k] / case[k] - 1) < 1e-12 for k in ("alpha", "r_cut", "k_cut"))
+        print(json.dumps({"workload": "ewald-params", "case": name,
+                          "n_sites": int(nb.num_system_elements), "seconds": best,
+                          "device_builds": builds, "same_choice_as_reference": ok,
+                          "reference_recorded_seconds": case["reference_seconds"],
+                          "reference_recorded_on": "NumPy, 1 core, x86 host of this build"}),
+              flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--workload", default="batched",
-                    choices=["batched", "ewald-split", "uneven", "serving", "msd"])
+                    choices=["batched", "ewald-split", "uneven", "serving", "msd",
+                             "ewald-params"])
     ap.add_argument("--jobs", type=int, default=2000)
     ap.add_argument("--max-job-steps", type=int, default=1_000_000)
     ap.add_argument("--sizes", default="")
@@ -606,6 +650,8 @@ def main():
         return serving_bench(args)
     if args.workload == "msd":
         return msd_bench(args)
+    if args.workload == "ewald-params":
+        return ewald_params_bench(args)
 
     import torch
     import torch.distributed as dist
