@@ -9,6 +9,11 @@
 
 namespace pycd {
 
+// 3 x 3 matrix passed by value to kernels (row-major)
+struct Mat3 {
+  double m[9];
+};
+
 // Thread-local last-error text behind pycd_last_error().
 void set_error(const char* fmt, ...);
 void clear_error();

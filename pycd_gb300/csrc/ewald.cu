@@ -23,9 +23,6 @@
 
 namespace pycd {
 
-struct Mat3 {
-  double m[9];
-};
 
 __device__ __forceinline__ void min_image(const Mat3& cell, const Mat3& inv,
                                           const int32_t pbc[3], double d[3]) {
@@ -80,6 +77,7 @@ struct EwaldGeom {
   const double* cart;
   const double* pmiv;
   Mat3 cell, inv;
+  float cell_f[9], inv_f[9];  // FP32 copies for the screen (no per-pair conversions)
   int32_t pbc[3];
   int64_t n;
 };
@@ -93,8 +91,7 @@ __device__ __forceinline__ float min_image_r2_f32(const EwaldGeom& g, int64_t i,
   for (int c = 0; c < 3; ++c) d[c] = (float)(g.cart[j * 3 + c] - g.cart[i * 3 + c]);
 #pragma unroll
   for (int c = 0; c < 3; ++c)
-    f[c] = d[0] * (float)g.inv.m[c] + d[1] * (float)g.inv.m[3 + c] +
-           d[2] * (float)g.inv.m[6 + c];
+    f[c] = d[0] * g.inv_f[c] + d[1] * g.inv_f[3 + c] + d[2] * g.inv_f[6 + c];
 #pragma unroll
   for (int c = 0; c < 3; ++c) f[c] = g.pbc[c] ? f[c] - rintf(f[c]) : f[c];
   float best = 3.0e38f;
@@ -106,8 +103,7 @@ __device__ __forceinline__ float min_image_r2_f32(const EwaldGeom& g, int64_t i,
         float r2 = 0.f;
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
-          const float v = w0 * (float)g.cell.m[c] + w1 * (float)g.cell.m[3 + c] +
-                          w2 * (float)g.cell.m[6 + c];
+          const float v = w0 * g.cell_f[c] + w1 * g.cell_f[3 + c] + w2 * g.cell_f[6 + c];
           r2 += v * v;
         }
         best = fminf(best, r2);
@@ -214,35 +210,103 @@ __global__ void __launch_bounds__(256)
 
 // Feature rows F[i] = [sqrt(w_k) cos(k.r_i), sqrt(w_k) sin(k.r_i)]_k with
 // w_k = 2 c_k / (k^2 eps); rows padded with zeros to `ld` columns.
-__global__ void ewald_features_kernel(const double* __restrict__ cart,
-                                      int64_t n, const double* __restrict__ kc,
-                                      const double* __restrict__ k2,
-                                      const double* __restrict__ ck, int64_t K,
-                                      double eps, int64_t ld,
-                                      double* __restrict__ F) {
-  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const int64_t i = blockIdx.y;
-  if (i >= n) return;
-  if (k >= K) {
-    const int64_t c = 2 * k;
-    if (c < ld) F[i * ld + c] = 0.0;
-    if (c + 1 < ld) F[i * ld + c + 1] = 0.0;
-    return;
-  }
-  const double w = sqrt(2.0 * ck[k] / (k2[k] * eps));
-  const double th = kc[k * 3] * cart[i * 3] + kc[k * 3 + 1] * cart[i * 3 + 1] +
-                    kc[k * 3 + 2] * cart[i * 3 + 2];
-  double s, c;
-  sincos(th, &s, &c);
-  F[i * ld + 2 * k] = w * c;
-  F[i * ld + 2 * k + 1] = w * s;
+//
+// Every k is m0 b0 + m1 b1 + m2 b2 (integers m, reciprocal basis rows b), so
+// e^{i k.r} = e^{i m0 phi0} e^{i m1 phi1} e^{i m2 phi2} with phi_d = b_d . r.
+// A block owns kFeatSites sites: it finds max |m_d| over the k list, tabulates
+// e^{i m phi_d} for |m| <= max |m_d| in shared memory (a few hundred sincos
+// per site instead of K), and forms each feature with two complex products
+// (8 FP64 instructions instead of a sincos).  When the tables would not fit
+// in the block's shared memory the block evaluates sincos(k . r) directly.
+constexpr int kFeatSites = 16;
+constexpr int kFeatThreads = 256;
+constexpr int kFeatSmem = 96 * 1024;
+
+__device__ __forceinline__ double2 cmul(double2 a, double2 b) {
+  return make_double2(fma(a.x, b.x, -__dmul_rn(a.y, b.y)), fma(a.x, b.y, __dmul_rn(a.y, b.x)));
 }
 
-int ewald_features_launch(const double* cart, int64_t n, const double* kc,
-                          const double* k2, const double* ck, int64_t K,
+__global__ void __launch_bounds__(kFeatThreads)
+ewald_features_kernel(const double* __restrict__ cart, int64_t n,
+                      const int32_t* __restrict__ kv, Mat3 recip,
+                      const double* __restrict__ kc, const double* __restrict__ k2,
+                      const double* __restrict__ ck, int64_t K, double eps, int64_t ld,
+                      double* __restrict__ F) {
+  extern __shared__ double2 tab[];  // [kFeatSites][T]
+  __shared__ int mmax[3];
+  __shared__ double phi[kFeatSites][3];
+  const int tid = threadIdx.x;
+  const int64_t site0 = (int64_t)blockIdx.x * kFeatSites;
+  const int ns = (int)min((int64_t)kFeatSites, n - site0);
+  if (tid < 3) mmax[tid] = 0;
+  if (tid < kFeatSites * 3) {
+    const int si = tid / 3, d = tid % 3;
+    double v = 0.0;
+    if (si < ns) {
+      const double* r = cart + (site0 + si) * 3;
+      v = fma(recip.m[d * 3 + 2], r[2], fma(recip.m[d * 3 + 1], r[1], __dmul_rn(recip.m[d * 3], r[0])));
+    }
+    phi[si][d] = v;
+  }
+  __syncthreads();
+  for (int64_t k = tid; k < K; k += kFeatThreads) {
+    atomicMax(&mmax[0], abs(kv[k * 3]));
+    atomicMax(&mmax[1], abs(kv[k * 3 + 1]));
+    atomicMax(&mmax[2], abs(kv[k * 3 + 2]));
+  }
+  __syncthreads();
+  const int M0 = mmax[0], M1 = mmax[1], M2 = mmax[2];
+  const int off1 = 2 * M0 + 1, off2 = off1 + 2 * M1 + 1, T = off2 + 2 * M2 + 1;
+  const bool use_tab = (int64_t)T * kFeatSites * (int64_t)sizeof(double2) <= kFeatSmem;
+  if (use_tab) {
+    for (int e = tid; e < kFeatSites * T; e += kFeatThreads) {
+      const int si = e / T, j = e - si * T;
+      const int d = j < off1 ? 0 : (j < off2 ? 1 : 2);
+      const int m = j - (d == 0 ? M0 : (d == 1 ? off1 + M1 : off2 + M2));
+      double sv, cv;
+      sincos(__dmul_rn((double)m, phi[si][d]), &sv, &cv);
+      tab[e] = make_double2(cv, sv);
+    }
+  }
+  __syncthreads();
+  for (int64_t k = tid; 2 * k < ld; k += kFeatThreads) {
+    const int64_t c = 2 * k;
+    if (k >= K) {
+      for (int si = 0; si < ns; ++si) {
+        double* row = F + (site0 + si) * ld;
+        row[c] = 0.0;
+        if (c + 1 < ld) row[c + 1] = 0.0;
+      }
+      continue;
+    }
+    const double w = sqrt(2.0 * ck[k] / (k2[k] * eps));
+    const int m0 = kv[k * 3], m1 = kv[k * 3 + 1], m2 = kv[k * 3 + 2];
+    for (int si = 0; si < ns; ++si) {
+      double2 z;
+      if (use_tab) {
+        const double2* t = tab + si * T;
+        z = cmul(cmul(t[M0 + m0], t[off1 + M1 + m1]), t[off2 + M2 + m2]);
+      } else {
+        const double* r = cart + (site0 + si) * 3;
+        const double th = kc[k * 3] * r[0] + kc[k * 3 + 1] * r[1] + kc[k * 3 + 2] * r[2];
+        sincos(th, &z.y, &z.x);
+      }
+      double* row = F + (site0 + si) * ld;
+      row[c] = w * z.x;
+      row[c + 1] = w * z.y;
+    }
+  }
+}
+
+int ewald_features_launch(const double* cart, int64_t n, const int32_t* kv, Mat3 recip,
+                          const double* kc, const double* k2, const double* ck, int64_t K,
                           double eps, int64_t ld, double* F, cudaStream_t s) {
-  dim3 fg((unsigned)((ld / 2 + 127) / 128), (unsigned)n);
-  ewald_features_kernel<<<fg, 128, 0, s>>>(cart, n, kc, k2, ck, K, eps, ld, F);
+  // per device and cheap: set on every launch
+  PYCD_CUDA(cudaFuncSetAttribute(ewald_features_kernel,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, kFeatSmem));
+  const unsigned blocks = (unsigned)((n + kFeatSites - 1) / kFeatSites);
+  ewald_features_kernel<<<blocks, kFeatThreads, kFeatSmem, s>>>(cart, n, kv, recip, kc, k2,
+                                                                ck, K, eps, ld, F);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_fail(e, "ewald_features_kernel", __FILE__, __LINE__);
   return PYCD_OK;
@@ -464,6 +528,10 @@ int ewald_build(const PycdEwaldDesc* d, int mode, double* out, void* ws,
   g.pmiv = d->d_pmiv;
   g.cell = cell;
   g.inv = inv;
+  for (int c = 0; c < 9; ++c) {
+    g.cell_f[c] = (float)cell.m[c];
+    g.inv_f[c] = (float)inv.m[c];
+  }
   g.pbc[0] = d->pbc[0]; g.pbc[1] = d->pbc[1]; g.pbc[2] = d->pbc[2];
   g.n = n;
   const double sqrt_alpha = sqrt(d->alpha);
@@ -487,11 +555,9 @@ int ewald_build(const PycdEwaldDesc* d, int mode, double* out, void* ws,
     if (timing) PYCD_CUDA(cudaEventRecord(e1, s));
     if (K > 0) {
       if (mode == PYCD_EWALD_FP64_GEMM) {
-        dim3 fg((unsigned)((w.ld / 2 + 127) / 128), (unsigned)n);
-        ewald_features_kernel<<<fg, 128, 0, s>>>(d->d_cart, n, w.kc, w.k2,
-                                                 w.ck, K, d->dielectric, w.ld,
-                                                 w.F);
-        PYCD_CUDA(cudaGetLastError());
+        rc = ewald_features_launch(d->d_cart, n, d->d_kvec, recip, w.kc, w.k2, w.ck, K,
+                                   d->dielectric, w.ld, w.F, s);
+        if (rc) return rc;
         const unsigned nb = (unsigned)((n + GB - 1) / GB);
         syrk_fp64_kernel<<<dim3(nb, nb), 256, 0, s>>>(w.F, n, w.ld, w.ld, out);
         PYCD_CUDA(cudaGetLastError());

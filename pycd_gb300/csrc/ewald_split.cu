@@ -8,6 +8,14 @@
 // each finished chunk is added in FP64 to the output, which already holds
 // the real-space and self terms, so the cross-chunk sum is FP64.
 //
+// Tile order: the grid is 1-D over blocks of kRaster x kRaster tiles, blocks
+// taken along the upper triangle row by row and tiles row-major inside a
+// block.  The CTAs resident at one time (one per SM) then cover about two
+// blocks, i.e. ~16-24 distinct 128-row operand panels per K slice, and each
+// slice of a panel is read from DRAM once and reused from L2 by the CTAs of
+// its block row / column (a row-major walk over the whole triangle touches
+// one new B panel per CTA).
+//
 // Kernel layout (one CTA per 128 x 128 upper-triangle output tile):
 //   warp 4      TMA producer: Ah, Al (tile rows) and Bh, Bl (tile columns),
 //               128-byte K slices, SWIZZLE_128B, 3-stage ring
@@ -40,6 +48,22 @@ constexpr int kTmemCols = 512;
 // accumulation truncates, so its error grows with the MMA steps per chunk
 constexpr int kChunkCols = 256;
 constexpr uint32_t kWaitLimit = 1u << 24;      // bounded try_wait iterations
+constexpr int kRaster = 8;                     // tiles per raster block side
+
+// (bi, bj) of CTA `cta` in the blocked upper-triangle order; false for the
+// CTAs of diagonal and edge blocks that fall below the diagonal or outside
+__device__ __forceinline__ bool raster_tile(int cta, int nb, int& bi, int& bj) {
+  const int nbb = (nb + kRaster - 1) / kRaster;   // blocks per side
+  int blk = cta / (kRaster * kRaster);
+  const int loc = cta - blk * (kRaster * kRaster);
+  int I = 0;
+  while (I < nbb && blk >= nbb - I) { blk -= nbb - I; ++I; }
+  if (I >= nbb) return false;
+  const int J = I + blk;
+  bi = I * kRaster + loc / kRaster;
+  bj = J * kRaster + loc % kRaster;
+  return bi < nb && bj < nb && bi <= bj;
+}
 
 struct SplitErr {
   int* flag;  // device int, set non-zero on a timed-out wait
@@ -180,11 +204,12 @@ template <bool TF32>
 __global__ void __launch_bounds__(192, 1)
     ewald_split_kernel(const __grid_constant__ CUtensorMap map_h,
                        const __grid_constant__ CUtensorMap map_l, int64_t n,
-                       int k_blocks, int chunk_blocks, double* __restrict__ out,
+                       int k_blocks, int chunk_blocks, int nb, double* __restrict__ out,
                        const double* __restrict__ diag_sum, SplitErr err) {
   const double diag_value = *diag_sum;
-  const int bi = blockIdx.y, bj = blockIdx.x;
-  if (bi > bj) return;  // lower tiles are written as mirrors
+  int bi = 0, bj = 0;
+  // lower tiles are written as mirrors; CTAs without a tile leave at once
+  if (!raster_tile((int)blockIdx.x, nb, bi, bj)) return;
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   uint64_t* full = (uint64_t*)(smem + kStages * kStageBytes);
@@ -465,8 +490,8 @@ size_t ewald_split_workspace_bytes(const PycdEwaldDesc* d, int mode) {
          2 * align256s(es * (size_t)d->n_sites * (size_t)ld) + 256;
 }
 
-int ewald_features_launch(const double* cart, int64_t n, const double* kc,
-                          const double* k2, const double* ck, int64_t K,
+int ewald_features_launch(const double* cart, int64_t n, const int32_t* kv, Mat3 recip,
+                          const double* kc, const double* k2, const double* ck, int64_t K,
                           double eps, int64_t ld, double* F, cudaStream_t s);
 
 int ewald_build_split(const PycdEwaldDesc* d, int mode, double* out,
@@ -492,7 +517,10 @@ int ewald_build_split(const PycdEwaldDesc* d, int mode, double* out,
   double* diag_sum = (double*)(p + 8);
   PYCD_REQUIRE(((uintptr_t)hi & 15) == 0 && ((uintptr_t)lo & 15) == 0,
                "split operands must be 16-byte aligned");
-  int rc = ewald_features_launch(d->d_cart, n, kc, k2, ck, K, d->dielectric, ldf, F, s);
+  Mat3 recip;
+  for (int c = 0; c < 9; ++c) recip.m[c] = d->recip[c];
+  int rc = ewald_features_launch(d->d_cart, n, d->d_kvec, recip, kc, k2, ck, K, d->dielectric,
+                                 ldf, F, s);
   if (rc) return rc;
   weight_sum_kernel<<<1, 256, 0, s>>>(k2, ck, K, d->dielectric, diag_sum);
   PYCD_CUDA(cudaGetLastError());
@@ -527,18 +555,20 @@ int ewald_build_split(const PycdEwaldDesc* d, int mode, double* out,
   const int k_blocks = (int)(ld / (kRowBytes / es));
   const int chunk_blocks = (int)(kChunkCols / (kRowBytes / es));
   const size_t smem = (size_t)kStages * kStageBytes + 1024 + 256;
-  const unsigned nb = (unsigned)((n + kTile - 1) / kTile);
+  const int nb = (int)((n + kTile - 1) / kTile);
+  const int nbb = (nb + kRaster - 1) / kRaster;
+  const unsigned ctas = (unsigned)(nbb * (nbb + 1) / 2 * kRaster * kRaster);
   SplitErr err{flag};
   if (tf32) {
     PYCD_CUDA(cudaFuncSetAttribute(ewald_split_kernel<true>,
                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    ewald_split_kernel<true><<<dim3(nb, nb), 192, smem, s>>>(
-        mh, ml, n, k_blocks, chunk_blocks, out, diag_sum, err);
+    ewald_split_kernel<true><<<ctas, 192, smem, s>>>(
+        mh, ml, n, k_blocks, chunk_blocks, nb, out, diag_sum, err);
   } else {
     PYCD_CUDA(cudaFuncSetAttribute(ewald_split_kernel<false>,
                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    ewald_split_kernel<false><<<dim3(nb, nb), 192, smem, s>>>(
-        mh, ml, n, k_blocks, chunk_blocks, out, diag_sum, err);
+    ewald_split_kernel<false><<<ctas, 192, smem, s>>>(
+        mh, ml, n, k_blocks, chunk_blocks, nb, out, diag_sum, err);
   }
   PYCD_CUDA(cudaGetLastError());
   int h_flag = 0;
