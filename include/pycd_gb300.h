@@ -176,6 +176,15 @@ PYCD_API int pycd_potential_gemv(const double* d_A, int64_t n_sites,
                         const double* d_q, double* d_phi, double* d_energy,
                         void* stream);
 
+/* Energy contribution of every k-vector of desc->d_kvec (n_kvec of them) for
+ * the charges d_q (N), as get_k_vector_energy_contribution
+ * (PyCD/core.py:1171-1184) computes one:
+ *   d_out[k] = sum_ij q_i q_j (2 pi / V) exp(-k^2 / 4 alpha) cos(k . d_ij) / k^2
+ * with d_ij from d_pmiv (or the minimum image of d_cart).  One pass over the
+ * N^2 pairs per k; deterministic.                                           */
+PYCD_API int pycd_ewald_kvector_energies(const PycdEwaldDesc* desc, const double* d_q,
+                                         double* d_out, void* stream);
+
 /* phi[i] = sum_j q[j] A[idx[j]][i] for m charged sites (dopants on an
  * otherwise neutral lattice): the same background potential as
  * pycd_potential_gemv when q is zero elsewhere, reading m rows of the

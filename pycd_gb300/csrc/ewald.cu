@@ -621,6 +621,70 @@ static int noalloc_scratch(void** out) {
   return PYCD_OK;
 }
 
+// One block per k-vector: sum over all pairs of q_i q_j cos(k . d_ij) in a
+// fixed order (thread-strided, then a tree over the block), times the k
+// prefactor (2 pi / V) exp(-k^2 / 4 alpha) / k^2.
+constexpr int kKvecThreads = 256;
+__global__ void __launch_bounds__(kKvecThreads)
+kvector_energy_kernel(EwaldGeom g, const int32_t* __restrict__ kv, Mat3 recip,
+                      double coeff, double alpha4, const double* __restrict__ q,
+                      double* __restrict__ out) {
+  __shared__ double red[kKvecThreads];
+  const int64_t k = blockIdx.x;
+  const double m0 = kv[k * 3], m1 = kv[k * 3 + 1], m2 = kv[k * 3 + 2];
+  double kc[3];
+#pragma unroll
+  for (int c = 0; c < 3; ++c)
+    kc[c] = __dadd_rn(__dadd_rn(__dmul_rn(m0, recip.m[0 * 3 + c]),
+                                __dmul_rn(m1, recip.m[1 * 3 + c])),
+                      __dmul_rn(m2, recip.m[2 * 3 + c]));
+  const double k2 = fma(kc[2], kc[2], fma(kc[1], kc[1], __dmul_rn(kc[0], kc[0])));
+  double acc = 0.0;
+  const int64_t n = g.n, pairs = n * n;
+  for (int64_t p = threadIdx.x; p < pairs; p += kKvecThreads) {
+    const int64_t i = p / n, j = p - i * n;
+    double d[3];
+    pair_vector(g, i, j, d);
+    const double th = fma(d[2], kc[2], fma(d[1], kc[1], __dmul_rn(d[0], kc[0])));
+    acc = fma(__dmul_rn(q[i], q[j]), cos(th), acc);
+  }
+  red[threadIdx.x] = acc;
+  __syncthreads();
+  for (int o = kKvecThreads / 2; o > 0; o >>= 1) {
+    if ((int)threadIdx.x < o) red[threadIdx.x] = __dadd_rn(red[threadIdx.x], red[threadIdx.x + o]);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0)
+    out[k] = __ddiv_rn(__dmul_rn(__dmul_rn(coeff, exp(__ddiv_rn(-k2, alpha4))), red[0]), k2);
+}
+
+int kvector_energies(const PycdEwaldDesc* d, const double* q, double* out, cudaStream_t s) {
+  PYCD_REQUIRE(d != nullptr && q != nullptr && out != nullptr, "NULL argument");
+  PYCD_REQUIRE(d->n_sites > 0 && d->n_kvec >= 0 && (d->n_kvec == 0 || d->d_kvec),
+               "bad n_sites / k list");
+  PYCD_REQUIRE(d->d_cart != nullptr || d->d_pmiv != nullptr, "need d_cart or d_pmiv");
+  PYCD_REQUIRE(d->alpha > 0.0 && d->volume > 0.0, "alpha and volume must be > 0");
+  PYCD_REQUIRE(d->n_kvec <= 0x7fffffff, "too many k-vectors");
+  if (d->n_kvec == 0) return PYCD_OK;
+  EwaldGeom g{};
+  g.cart = d->d_cart;
+  g.pmiv = d->d_pmiv;
+  Mat3 recip;
+  for (int c = 0; c < 9; ++c) {
+    g.cell.m[c] = d->sim_cell[c];
+    g.inv.m[c] = d->sim_cell_inv[c];
+    g.cell_f[c] = (float)d->sim_cell[c];
+    g.inv_f[c] = (float)d->sim_cell_inv[c];
+    recip.m[c] = d->recip[c];
+  }
+  g.pbc[0] = d->pbc[0]; g.pbc[1] = d->pbc[1]; g.pbc[2] = d->pbc[2];
+  g.n = d->n_sites;
+  kvector_energy_kernel<<<(unsigned)d->n_kvec, kKvecThreads, 0, s>>>(
+      g, d->d_kvec, recip, 2.0 * M_PI / d->volume, 4.0 * d->alpha, q, out);
+  PYCD_CUDA(cudaGetLastError());
+  return PYCD_OK;
+}
+
 int potential_gemv(const double* A, int64_t n, const double* q, double* phi,
                    double* energy, cudaStream_t s) {
   PYCD_REQUIRE(A && q && phi && n > 0, "potential_gemv: bad arguments");
@@ -635,6 +699,12 @@ int potential_gemv(const double* A, int64_t n, const double* q, double* phi,
 }
 
 }  // namespace pycd
+
+extern "C" int pycd_ewald_kvector_energies(const PycdEwaldDesc* desc, const double* d_q,
+                                           double* d_out, void* stream) {
+  pycd::clear_error();
+  return pycd::kvector_energies(desc, d_q, d_out, (cudaStream_t)stream);
+}
 
 extern "C" int pycd_ewald_build_noalloc(const PycdEwaldDesc* desc, double* d_out,
                                         void* stream) {

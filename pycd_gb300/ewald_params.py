@@ -50,6 +50,7 @@ class EwaldEnergy(object):
         mode = choose_mode(system, pmiv, "auto")
         self.mode = mode if mode in ("fp64", "fp64_direct") else "fp64"
         self.builds = 0
+        self._kcache = {}
 
     def _energy(self, alpha, r_cut, k_cut, parts, kvecs=None):
         from .ewald import build_device_array
@@ -66,13 +67,52 @@ class EwaldEnergy(object):
         """Energy of get_precomputed_array_real(alpha, r_cut) (core.py:1594-1596)."""
         return self._energy(alpha, r_cut, 0.0, nat.EWALD_PART_REAL)
 
+    # systems up to this many sites take Fourier energies from cached per-k
+    # contributions (one pass over the N^2 pairs per new k) instead of a build
+    PER_K_MAX_SITES = 1024
+
     def fourier(self, alpha, k_cut):
-        """Energy of get_precomputed_array_fourier(alpha, k_cut)[0] (core.py:1598-1602)."""
-        return self._energy(alpha, 0.0, k_cut, nat.EWALD_PART_FOURIER)
+        """Energy of get_precomputed_array_fourier(alpha, k_cut)[0] (core.py:1598-1602).
+
+        Small systems: (2 / eps) times the sum of the per-k contributions of
+        the k list, each contribution computed once per alpha and cached, so a
+        k_cut scan costs one pass per distinct k.  Identical k lists give
+        identical sums.  Larger systems: one device build of the part."""
+        if self.n > self.PER_K_MAX_SITES:
+            return self._energy(alpha, 0.0, k_cut, nat.EWALD_PART_FOURIER)
+        from .ewald import effective_k_vectors, k_max_for
+        kv = effective_k_vectors(self.system.reciprocal_lattice_matrix,
+                                 k_max_for(self.system, k_cut), k_cut)
+        cache = self._kcache.setdefault(float(alpha), {})
+        keys = [tuple(r) for r in kv.tolist()]
+        new = [k for k in dict.fromkeys(keys) if k not in cache]
+        if new:
+            for k, e in zip(new, self.k_vectors(alpha, np.array(new, np.int32))):
+                cache[k] = float(e)
+        total = 0.0
+        for k in keys:
+            total += cache[k]
+        return 2.0 * total / self.system.material.dielectric_constant
 
     def self_term(self, alpha):
         """Energy of the self-interaction diagonal (core.py:1656)."""
         return self._energy(alpha, 0.0, 0.0, nat.EWALD_PART_SELF)
+
+    def k_vectors(self, alpha, k_vectors):
+        """get_k_vector_energy_contribution (core.py:1171-1184) of every row
+        of the (K, 3) integer array, in one device pass over the pairs per k."""
+        import torch
+        from .ewald import make_desc
+        kv = np.ascontiguousarray(np.asarray(k_vectors, np.int32).reshape(-1, 3))
+        if len(kv) == 0:
+            return np.zeros(0)
+        pmiv = self.system.pairwise_min_image_vector_data
+        desc, keep, _ = make_desc(self.system, alpha, 0.0, 0.0, pmiv, kvecs=kv)
+        out = torch.empty(len(kv), dtype=torch.float64, device=self.q.device)
+        nat.check(nat.lib().pycd_ewald_kvector_energies(
+            nat.C.byref(desc), self.q.data_ptr(), out.data_ptr(), nat.stream_handle()))
+        self.builds += 1
+        return out.cpu().numpy()
 
     def k_vector(self, alpha, k_vector):
         """get_k_vector_energy_contribution (core.py:1171-1184): the sum over
@@ -329,7 +369,7 @@ class EwaldParameterSearch(object):
             new.extend(self.get_new_k_vectors(k0, k1))
         new = np.asarray(new)
         print(f'Identified a total of {len(new)} k-vectors contributing towards energy changes')
-        contrib = np.array([ev.k_vector(alpha, k) for k in new])
+        contrib = ev.k_vectors(alpha, new)
         order = np.argsort(contrib)[::-1]
         prefix_list.append('k-vectors sorted in the decreasing order of their energy '
                            'contributions\n')

@@ -117,3 +117,26 @@ def test_automatic_parameters_flow_into_the_build(cuda_ready, tmp_path):
     assert log[4].startswith("r_cut: ") and "(optimal)" in log[4]
     assert float(log[4].split()[1]) == pytest.approx(case["r_cut"] * 0.529177210903, rel=2e-3)
     assert any(l.startswith("Total system energy (neutral): ") for l in log)
+
+
+def test_kvector_energies_equal_one_vector_builds(cuda_ready):
+    """pycd_ewald_kvector_energies (all k in one pass) against one Fourier
+    build per k-vector, both the reference's get_k_vector_energy_contribution."""
+    sysm, _ = _system("kcut_converge")
+    ev = sysm._energy_evaluator()
+    kv = np.array([[1, 0, 0], [0, 1, 0], [1, 1, 0], [-1, 2, 1], [2, 0, -3], [0, 0, 1]])
+    batch = ev.k_vectors(sysm.alpha, kv)
+    single = np.array([ev.k_vector(sysm.alpha, k) for k in kv])
+    scale = np.abs(single).max()
+    assert np.abs(batch - single).max() <= 1e-12 * scale
+
+
+def test_fourier_energy_from_per_k_cache_equals_build(cuda_ready):
+    """The cached per-k Fourier energy of a small system equals the energy of
+    the part-only device build at several cutoffs."""
+    sysm, _ = _system("kcut_converge")
+    ev = sysm._energy_evaluator()
+    for k_cut in (1.0, 2.5, 4.0):
+        via_cache = ev.fourier(sysm.alpha, k_cut)
+        via_build = ev._energy(sysm.alpha, 0.0, k_cut, 2)
+        assert abs(via_cache - via_build) <= 1e-12 * max(abs(via_build), 1e-300)
