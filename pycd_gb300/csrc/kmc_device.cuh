@@ -386,19 +386,32 @@ __device__ __forceinline__ void fresh_sums(const PycdKmcSystem& sy, int g,
 // sum_c' rp[occ_c'] in carrier order from +0, loads issued U at a time
 // (every lane runs the shuffles; lanes with act == false load nothing)
 template <int G, int U>
+__device__ __forceinline__ void carrier_row_block(const double* __restrict__ rp, bool act,
+                                                  int NC, unsigned gmask, int occ, int c0,
+                                                  double (&v)[U]) {
+#pragma unroll
+  for (int u = 0; u < U; ++u) {
+    const int sc = gshfl<G>(gmask, occ, min(c0 + u, NC - 1));
+    v[u] = (act && c0 + u < NC) ? __ldg(rp + sc) : 0.0;
+  }
+}
+
+// The loads of the next block are issued before the current block is summed,
+// so a row of many carriers costs about one memory round trip, not one per
+// block (the array rows of large systems come from DRAM).
+template <int G, int U>
 __device__ __forceinline__ double carrier_row_sum(const double* __restrict__ rp, bool act,
                                                   int NC, unsigned gmask, int occ) {
   double sum = 0.0;
+  double cur[U], nxt[U];
+  carrier_row_block<G, U>(rp, act, NC, gmask, occ, 0, cur);
   for (int c0 = 0; c0 < NC; c0 += U) {
-    double v[U];
-#pragma unroll
-    for (int u = 0; u < U; ++u) {
-      const int sc = gshfl<G>(gmask, occ, min(c0 + u, NC - 1));
-      v[u] = (act && c0 + u < NC) ? __ldg(rp + sc) : 0.0;
-    }
+    if (c0 + U < NC) carrier_row_block<G, U>(rp, act, NC, gmask, occ, c0 + U, nxt);
 #pragma unroll
     for (int u = 0; u < U; ++u)
-      if (c0 + u < NC) sum = dadd(sum, v[u]);
+      if (c0 + u < NC) sum = dadd(sum, cur[u]);
+#pragma unroll
+    for (int u = 0; u < U; ++u) cur[u] = nxt[u];
   }
   return sum;
 }

@@ -11,10 +11,12 @@ a seed) arrive over time.  The server keeps:
 * trajectory slots in buckets keyed by (process count, carrier count), each
   a resident ``KmcBatch`` advanced by the persistent kernel.
 
-Each ``step()`` admits arrived jobs into free slots while the budget allows,
-advances every occupied slot by one chunk, and retires finished jobs.  A
-job's uniforms come from the Philox stream of its job id, so its result is
-the same alone and in any mix.  Latency = retirement time - arrival time.
+Buckets run independently on their own streams: whenever a bucket's chunk
+has finished, its finished jobs retire, arrived jobs of its class take the
+free slots and its next chunk is launched, while the other buckets keep
+running.  A job's uniforms come from the Philox stream of its job id, so its
+result is the same alone and in any mix.  Latency = retirement time -
+arrival time.
 """
 import time
 
@@ -87,6 +89,10 @@ class LatticeCache(object):
 
 
 class _Bucket(object):
+    """Slots of one (process count, carrier count) class with their own
+    system table, engine, stream and completion event.  A bucket is touched
+    by the host (retire, admit, table upload) only between its chunks."""
+
     def __init__(self, np_bound, nc_bound, capacity, max_carriers):
         import torch
         self.np_bound, self.nc_bound = np_bound, nc_bound
@@ -98,12 +104,47 @@ class _Bucket(object):
         self.batch.status.fill_(nat.TRAJ_DONE)  # free slots are never advanced
         self.ids = torch.zeros(capacity, dtype=torch.int64, device="cuda")
         self.free = list(range(capacity - 1, -1, -1))
-        self.jobs = {}  # slot -> job
+        self.jobs = {}            # slot -> job
+        self.tables = []          # this bucket's per-job tables (sys_index space)
+        self.table_free = []
         self.engine = None
-        self.stream = None
+        self.dirty = True
+        self.stream = torch.cuda.Stream()
+        self.event = None         # recorded after the chunk in flight
+        self.running = False
+
+    def add_table(self, tab):
+        if self.table_free:
+            ti = self.table_free.pop()
+            self.tables[ti] = tab
+        else:
+            ti = len(self.tables)
+            self.tables.append(tab)
+        self.dirty = True
+        return ti
+
+    def drop_table(self, ti):
+        self.tables[ti] = None
+        self.table_free.append(ti)
+
+    def upload(self):
+        """Rebuild this bucket's system table (only between its chunks)."""
+        live = [t for t in self.tables if t is not None]
+        self.engine = KmcEngine([t if t is not None else live[0] for t in self.tables])
+        self.engine.launch.max_processes = self.np_bound
+        self.engine.launch.max_carriers = self.nc_bound
+        self.engine.upload(self.stream)
+        self.engine.launch.max_processes = self.np_bound
+        self.engine.launch.max_carriers = self.nc_bound
+        self.dirty = False
 
 
 class KmcServer(object):
+    """Buckets run independently: whenever one bucket's chunk has finished,
+    its finished jobs are retired, arrived jobs of its class are admitted and
+    its next chunk is launched on its own stream, while the other buckets keep
+    running.  No bucket waits for another."""
+
     def __init__(self, budget_bytes=150e9, chunk_steps=5000, slots_per_bucket=1024,
                  precision="bf16x3", seed=0, max_carriers=32):
         self.cache = LatticeCache(budget_bytes, precision)
@@ -113,11 +154,8 @@ class KmcServer(object):
         self.max_carriers = int(max_carriers)
         self.buckets = {}
         self.pending = []
+        self.waiting = {}         # bucket key -> prepared jobs waiting for a slot
         self.done = []
-        self.table = []        # system-table entries (per-job KmcTables)
-        self.table_free = []
-        self.master = None
-        self.table_dirty = True
         self.t0 = None
 
     # -- jobs ------------------------------------------------------------
@@ -140,7 +178,9 @@ class KmcServer(object):
             self.buckets[key] = b
         return b
 
-    def _admit(self, job):
+    def _prepare(self, job):
+        """Lattice and job tables of an arrived job; False when the HBM
+        budget cannot hold its lattice now."""
         lat = self.cache.get(job["lattice"], job["cells"])
         if lat is None:
             return False
@@ -152,21 +192,25 @@ class KmcServer(object):
         q[dopants] = 1.0
         tab = lat["tables"].with_charges(q, job["carriers"])
         b = self._bucket(job["carriers"] * tab.n_slots, job["carriers"])
-        if not b.free:
-            return False
-        slot = b.free.pop()
-        if self.table_free:
-            ti = self.table_free.pop()
-            self.table[ti] = tab
-        else:
-            ti = len(self.table)
-            self.table.append(tab)
         lat["refs"] += 1
-        job.update(table_index=ti, lattice_entry=lat, slot=slot, bucket=b,
-                   carrier_sites=carriers, dopant_sites=dopants, admitted=self.now())
-        b.jobs[slot] = job
-        self.table_dirty = True
+        job.update(lattice_entry=lat, bucket=b, tab=tab, carrier_sites=carriers,
+                   dopant_sites=dopants)
+        self.waiting.setdefault(id(b), []).append(job)
         return True
+
+    def _admit_into(self, b):
+        """Give free slots of idle bucket b to its waiting jobs."""
+        queue = self.waiting.get(id(b), [])
+        new = []
+        while queue and b.free:
+            job = queue.pop(0)
+            slot = b.free.pop()
+            job.update(slot=slot, table_index=b.add_table(job.pop("tab")),
+                       admitted=self.now())
+            b.jobs[slot] = job
+            new.append(job)
+        self._write_slots(b, new)
+        return new
 
     def _write_slots(self, b, new):
         import torch
@@ -191,56 +235,49 @@ class KmcServer(object):
         bt.last_row[idx] = 0.0
         bt.status[idx] = nat.TRAJ_RUNNING
 
-    def _upload(self):
-        if not self.table_dirty:
-            return
-        live = [t for t in self.table if t is not None]
-        if not live:
-            return
-        self.master = KmcEngine([t if t is not None else live[0] for t in self.table])
-        self.master.upload()
-        for b in self.buckets.values():
-            b.engine = KmcEngine(None, share=self.master)
-            b.engine.launch.max_processes = b.np_bound
-            b.engine.launch.max_carriers = b.nc_bound
-        self.table_dirty = False
+    def _launch(self, b):
+        """Next chunk of idle bucket b on its stream (after the host-side
+        writes and table builds made on the current stream)."""
+        import torch
+        b.stream.wait_stream(torch.cuda.current_stream())
+        if b.dirty:
+            b.upload()
+        b.engine.advance(b.batch, self.chunk_for(b),
+                         b.engine.rng_struct(seed=self.seed, traj_ids=b.ids),
+                         stream=b.stream)
+        b.event = torch.cuda.Event()
+        b.event.record(b.stream)
+        b.running = True
+
+    def _collect(self, b):
+        """Retire the finished jobs of bucket b, whose chunk has completed."""
+        b.running = False
+        st = b.batch.status.cpu().numpy()
+        t_ret = self.now()
+        out = []
+        for slot, job in list(b.jobs.items()):
+            if st[slot] != nat.TRAJ_RUNNING:
+                self._retire(b, slot, job, int(st[slot]), t_ret)
+                out.append(job)
+        return out
 
     def step(self):
-        """Admit, advance one chunk, retire.  Returns the jobs retired."""
-        import torch
+        """One scheduling pass: prepare arrived jobs, then for every bucket
+        whose chunk has finished retire, admit and relaunch.  Returns the
+        jobs retired."""
         now = self.now()
         arrived = [j for j in self.pending if j["arrival"] <= now]
-        admitted = []
         for j in arrived:
-            if self._admit(j):
-                admitted.append(j)
-        for j in admitted:
-            self.pending.remove(j)
-        for b in self.buckets.values():
-            self._write_slots(b, [j for j in admitted if j["bucket"] is b])
-        self._upload()
-        active = [b for b in self.buckets.values() if b.jobs]
-        # buckets run concurrently, each on its own stream
-        cur = torch.cuda.current_stream()
-        ready = torch.cuda.Event()
-        ready.record(cur)
-        for b in active:
-            if b.stream is None:
-                b.stream = torch.cuda.Stream()
-            b.stream.wait_event(ready)
-            b.engine.advance(b.batch, self.chunk_for(b),
-                             b.engine.rng_struct(seed=self.seed, traj_ids=b.ids),
-                             stream=b.stream)
+            if self._prepare(j):
+                self.pending.remove(j)
         retired = []
-        if active:
-            torch.cuda.synchronize()
-            t_ret = self.now()
-            for b in active:
-                st = b.batch.status.cpu().numpy()
-                for slot, job in list(b.jobs.items()):
-                    if st[slot] != nat.TRAJ_RUNNING:
-                        self._retire(b, slot, job, int(st[slot]), t_ret)
-                        retired.append(job)
+        for b in list(self.buckets.values()):
+            if b.running and b.event.query():
+                retired += self._collect(b)
+            if not b.running:
+                self._admit_into(b)
+                if b.jobs:
+                    self._launch(b)
         return retired
 
     def _retire(self, b, slot, job, status, t_ret):
@@ -255,8 +292,7 @@ class KmcServer(object):
         bt.status[slot] = nat.TRAJ_DONE
         del b.jobs[slot]
         b.free.append(slot)
-        self.table[job["table_index"]] = None
-        self.table_free.append(job["table_index"])
+        b.drop_table(job["table_index"])
         job["lattice_entry"]["refs"] -= 1
         for k in ("bucket", "lattice_entry"):
             job.pop(k, None)
@@ -269,7 +305,8 @@ class KmcServer(object):
         return max(500, int(self.chunk_steps * 8 / max(8, b.nc_bound)))
 
     def busy(self):
-        return bool(self.pending) or any(b.jobs for b in self.buckets.values())
+        return (bool(self.pending) or any(self.waiting.values())
+                or any(b.jobs for b in self.buckets.values()))
 
     def run(self, jobs, max_seconds=600.0, log=None):
         """Serve `jobs` (arrival-time ordered) to completion; `log` is an
@@ -285,13 +322,20 @@ class KmcServer(object):
                 active = sum(len(b.jobs) for b in self.buckets.values())
                 print(f"[serving] t={self.now():.1f}s done={len(self.done)} "
                       f"active={active} pending={len(self.pending)}", file=log, flush=True)
-            if not any(b.jobs for b in self.buckets.values()):
-                nxt = min(j["arrival"] for j in self.pending)
-                wait = nxt - self.now()
-                if wait > 0:
-                    time.sleep(min(wait, 0.05))
-            for j in self.step():
+            retired = self.step()
+            for j in retired:
                 steps += j["steps_done"]
+            if not retired:
+                if not any(b.running for b in self.buckets.values()) and self.pending:
+                    wait = min(j["arrival"] for j in self.pending) - self.now()
+                    if wait > 0:
+                        time.sleep(min(wait, 0.05))
+                else:
+                    time.sleep(0.0005)  # chunks in flight: poll their events
+        for b in self.buckets.values():
+            if b.running:
+                b.event.synchronize()
+                b.running = False
         wall = self.now()
         lat = np.array([j["latency"] for j in self.done]) if self.done else np.zeros(1)
         return {"jobs": len(self.done), "wall_s": wall, "steps": steps,
