@@ -383,6 +383,103 @@ __device__ __forceinline__ void fresh_sums(const PycdKmcSystem& sy, int g,
     if (doit[j] && !ownq[j]) pc.Q[j] = pc.Q[j - 1];
 }
 
+// After carrier c_sel moved to n_sel: rebuild its S processes (slot s:
+// o = n_sel, n = nbr[n_sel, s]) and their sums, as setup_processes and
+// fresh_sums would give them.  Jobs i = 0..S (slot i for i < S; the carrier's
+// Q, row n_sel, for i = S) are done JB per round:
+//   * lane c holds carrier c's site, so it loads A[row_i, occ_c] of every job
+//     of the round at once: one memory round trip for all the rows;
+//   * lane u sums job u in carrier order from +0, pulling the values with
+//     shuffles: the order of fresh_sums, hence the same doubles;
+//   * lane u builds the constants of slot job u.
+// Owner lanes pull the results.  Returns true on a bad index (no load is
+// issued with one).
+template <int G, int MAXP, int JB>
+__device__ __forceinline__ bool rebuild_moved_jb(const PycdKmcSystem& sy,
+                                                 const double2* __restrict__ coef,
+                                                 int g, unsigned gmask, int occ,
+                                                 int c_sel, int n_sel,
+                                                 ProcCache<MAXP>& pc) {
+  const int64_t N = sy.n_sites;
+  const int S = sy.n_slots;
+  const int NC = sy.n_carriers;
+  const double* __restrict__ A = sy.d_A;
+  const int64_t ro = (int64_t)n_sel * N;
+  bool bad = false;
+  for (int i0 = 0; i0 <= S; i0 += JB) {
+    int row[JB];
+#pragma unroll
+    for (int u = 0; u < JB; ++u) {
+      int r = n_sel;
+      if (i0 + u < S) {
+        r = sy.d_nbr[(int64_t)n_sel * S + i0 + u];
+        if (r < 0 || r >= N) { bad = true; r = n_sel; }
+      }
+      row[u] = r;
+    }
+    double v[JB];
+#pragma unroll
+    for (int u = 0; u < JB; ++u)
+      v[u] = (g < NC && i0 + u <= S) ? __ldg(A + (int64_t)row[u] * N + occ) : 0.0;
+    double sum = 0.0;
+    for (int c = 0; c < NC; ++c) {
+      double mine = 0.0;
+#pragma unroll
+      for (int u = 0; u < JB; ++u) {
+        const double t = gshfl<G>(gmask, v[u], c);
+        if (g == u) mine = t;
+      }
+      sum = dadd(sum, mine);
+    }
+    int n = n_sel;
+#pragma unroll
+    for (int u = 0; u < JB; ++u)
+      if (g == u) n = row[u];
+    double dphi = 0.0, t02q = 0.0, de = 0.0, lam = 0.0;
+    double2 cf = make_double2(0.0, 0.0);
+    if (g < JB && i0 + g < S) {
+      const int64_t slot = (int64_t)n_sel * S + i0 + g;
+      dphi = dsub(__ldg(sy.d_phi_bg + n), __ldg(sy.d_phi_bg + n_sel));
+      t02q = dmul(sy.carrier_charge, dsub(__ldg(A + ro + n_sel), __ldg(A + ro + n)));
+      de = dsub(__ldg(sy.d_e_rel + n), __ldg(sy.d_e_rel + n_sel));
+      lam = __ldg(sy.d_lam + slot);
+      cf = __ldg(coef + slot);
+    }
+    // the carrier's Q is summed in the round that holds job S
+    const int qsrc = S - i0;
+    double qv = 0.0;
+    if (qsrc < JB) qv = gshfl<G>(gmask, sum, qsrc);
+#pragma unroll
+    for (int j = 0; j < MAXP; ++j) {
+      const bool mine = pc.valid[j] && pc.carrier[j] == c_sel;
+      const int src = g * MAXP + j - c_sel * S - i0;
+      const bool take = mine && src >= 0 && src < JB;
+      const int sl = take ? src : 0;
+      const int nn = gshfl<G>(gmask, n, sl);
+      const double v_dphi = gshfl<G>(gmask, dphi, sl);
+      const double v_t02q = gshfl<G>(gmask, t02q, sl);
+      const double v_de = gshfl<G>(gmask, de, sl);
+      const double v_lam = gshfl<G>(gmask, lam, sl);
+      const double v_c1 = gshfl<G>(gmask, cf.x, sl);
+      const double v_c0 = gshfl<G>(gmask, cf.y, sl);
+      const double v_p = gshfl<G>(gmask, sum, sl);
+      if (take) {
+        pc.oldsite[j] = n_sel;
+        pc.newsite[j] = nn;
+        pc.dphi[j] = v_dphi;
+        pc.t02q[j] = v_t02q;
+        pc.de[j] = v_de;
+        pc.lam[j] = v_lam;
+        pc.c1[j] = v_c1;
+        pc.c0[j] = v_c0;
+        pc.P[j] = v_p;
+      }
+      if (mine && qsrc < JB) pc.Q[j] = qv;
+    }
+  }
+  return bad;
+}
+
 // sum_c' rp[occ_c'] in carrier order from +0, loads issued U at a time
 // (every lane runs the shuffles; lanes with act == false load nothing)
 template <int G, int U>
@@ -416,14 +513,11 @@ __device__ __forceinline__ double carrier_row_sum(const double* __restrict__ rp,
   return sum;
 }
 
-// After carrier c_sel moved to n_sel: rebuild its S processes (slot s:
-// o = n_sel, n = nbr[n_sel, s]) and their sums, which setup_processes and
-// fresh_sums would give, with job i = i0 + g on lane g: slot i for i < S and
-// the carrier's Q (row n_sel) for i = S.  Owner lanes pull the results, so
-// the FP64 work is spread over the group instead of being issued by every
-// lane for the few lanes that own the carrier.  Returns true on a bad index.
+// The moved carrier's rebuild for few carriers: job i = i0 + g on lane g (slot
+// i for i < S, the carrier's Q for i = S), each job lane loading its own row
+// entries; owner lanes pull the results.  Same doubles as rebuild_moved_jb.
 template <int G, int MAXP>
-__device__ __forceinline__ bool rebuild_moved(const PycdKmcSystem& sy,
+__device__ __forceinline__ bool rebuild_moved_direct(const PycdKmcSystem& sy,
                                               const double2* __restrict__ coef,
                                               int g, unsigned gmask, int occ,
                                               int c_sel, int n_sel,
@@ -491,6 +585,20 @@ __device__ __forceinline__ bool rebuild_moved(const PycdKmcSystem& sy,
     }
   }
   return bad;
+}
+
+// Few carriers: the job lanes load their rows directly (no value
+// shuffles).  Many carriers: lane-parallel row loads (one round trip).
+template <int G, int MAXP>
+__device__ __forceinline__ bool rebuild_moved(const PycdKmcSystem& sy,
+                                              const double2* __restrict__ coef,
+                                              int g, unsigned gmask, int occ,
+                                              int c_sel, int n_sel,
+                                              ProcCache<MAXP>& pc) {
+  constexpr int JB = G < 8 ? G : 8;
+  if (sy.n_carriers <= 8)
+    return rebuild_moved_direct<G, MAXP>(sy, coef, g, gmask, occ, c_sel, n_sel, pc);
+  return rebuild_moved_jb<G, MAXP, JB>(sy, coef, g, gmask, occ, c_sel, n_sel, pc);
 }
 
 // Rates of this lane's processes (core.py:1989-2050):
