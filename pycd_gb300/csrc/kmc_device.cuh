@@ -18,6 +18,8 @@
 //           term02 = q (A[o,o] - A[o,n])
 //   rate  = exp(c1 (lam + dE0)^2 + c0),  c1 = -1/(4 lam kT),
 //           c0 = (V_ab + shift)/kT + ln vn   (= vn exp(-dG/kT), core.py:2045-2047)
+//   The carrier sums in term01 are balanced binary trees over the carrier
+//   index, kept incrementally between exact refreshes.
 //   k_tot and every cumulative rate are sums over a fixed balanced binary
 //   tree over the process index (zero-padded to a power of two), so the
 //   event stream does not depend on G or MAXP: a trajectory advanced alone
@@ -318,88 +320,127 @@ __device__ __forceinline__ bool setup_processes(const PycdKmcSystem& sy,
   return bad;
 }
 
-// Carriers in blocks of U: all loads of a block are issued before any of
-// their sums, so a step waits for a few memory round trips instead of one
-// per carrier; the additions keep carrier order (identical results for any U).
+// Every carrier sum of this kernel, P = sum_c' A[n, occ_c'] and
+// Q = sum_c' A[o, occ_c'], is the balanced binary tree over carrier index
+// 0..31 with +0 leaves for missing carriers (which leave every node
+// unchanged).  A lane forms it from 8-carrier blocks; the rebuild of a moved
+// carrier forms it across lanes; both give the same doubles, and the tree
+// has log2 depth instead of one dependent addition per carrier.
+template <int U>
+__device__ __forceinline__ double tree_reduce(double (&v)[U]) {
+#pragma unroll
+  for (int w = U / 2; w >= 1; w /= 2) {
+#pragma unroll
+    for (int i = 0; i < w; ++i) v[i] = dadd(v[2 * i], v[2 * i + 1]);
+  }
+  return v[0];
+}
+
+// Exact carrier sums for this lane's processes in the tree order; U = 4 for
+// at most 4 carriers (one block), else 8 (up to 4 blocks, combined as
+// (b0 + b1) + (b2 + b3)).  Q is evaluated once per carrier and shared by its
+// processes.  Every lane runs the shuffles.
 template <int G, int MAXP, int U>
-__device__ __forceinline__ void fresh_sums_block(const double* __restrict__ A,
-                                                 int64_t N, int NC, unsigned gmask,
-                                                 int occ, const bool (&doit)[MAXP],
-                                                 const bool (&ownq)[MAXP],
-                                                 ProcCache<MAXP>& pc) {
-  for (int c0 = 0; c0 < NC; c0 += U) {
-    int sc[U];
+__device__ __forceinline__ void fresh_sums_tree(const double* __restrict__ A, int64_t N,
+                                                int NC, unsigned gmask, int occ,
+                                                ProcCache<MAXP>& pc) {
 #pragma unroll
-    for (int u = 0; u < U; ++u) sc[u] = gshfl<G>(gmask, occ, min(c0 + u, NC - 1));
+  for (int j = 0; j < MAXP; ++j) {
+    const bool doit = pc.valid[j], ownq = doit && pc.firstq[j];
+    const double* rn = A + (int64_t)(doit ? pc.newsite[j] : 0) * N;
+    const double* ro = A + (int64_t)(doit ? pc.oldsite[j] : 0) * N;
+    double p_lo = 0.0, p_hi = 0.0, q_lo = 0.0, q_hi = 0.0;
 #pragma unroll
-    for (int j = 0; j < MAXP; ++j) {
-      if (doit[j]) {
-        const double* rn = A + (int64_t)pc.newsite[j] * N;
-        const double* ro = A + (int64_t)pc.oldsite[j] * N;
+    for (int b = 0; b < (U == 4 ? 1 : 4); ++b) {
+      if (b * U < NC) {
         double vn[U], vo[U];
 #pragma unroll
         for (int u = 0; u < U; ++u) {
-          vn[u] = (c0 + u < NC) ? __ldg(rn + sc[u]) : 0.0;
-          vo[u] = (ownq[j] && c0 + u < NC) ? __ldg(ro + sc[u]) : 0.0;
+          const int c = b * U + u;
+          const int sc = gshfl<G>(gmask, occ, min(c, NC - 1));
+          vn[u] = (doit && c < NC) ? __ldg(rn + sc) : 0.0;
+          vo[u] = (ownq && c < NC) ? __ldg(ro + sc) : 0.0;
         }
-#pragma unroll
-        for (int u = 0; u < U; ++u) {
-          if (c0 + u < NC) {
-            pc.P[j] = dadd(pc.P[j], vn[u]);
-            if (ownq[j]) pc.Q[j] = dadd(pc.Q[j], vo[u]);
-          }
-        }
+        const double bp = tree_reduce<U>(vn);
+        const double bq = tree_reduce<U>(vo);
+        if (b == 0) { p_lo = bp; q_lo = bq; }
+        if (b == 1) { p_lo = dadd(p_lo, bp); q_lo = dadd(q_lo, bq); }
+        if (b == 2) { p_hi = bp; q_hi = bq; }
+        if (b == 3) { p_hi = dadd(p_hi, bp); q_hi = dadd(q_hi, bq); }
       }
+    }
+    if (doit) {
+      pc.P[j] = (NC > 16) ? dadd(p_lo, p_hi) : p_lo;
+      if (ownq) pc.Q[j] = (NC > 16) ? dadd(q_lo, q_hi) : q_lo;
+      else if (j > 0) pc.Q[j] = pc.Q[j - 1];
     }
   }
 }
 
-// Exact carrier sums for this lane's processes: P = sum_c' A[n, occ_c'],
-// Q = sum_c' A[o, occ_c'] in carrier order; Q is evaluated once per carrier
-// and shared by its processes.
 template <int G, int MAXP>
 __device__ __forceinline__ void fresh_sums(const PycdKmcSystem& sy, int g,
                                            unsigned gmask, int occ,
                                            ProcCache<MAXP>& pc) {
-  const int64_t N = sy.n_sites;
-  const int NC = sy.n_carriers;
-  const double* __restrict__ A = sy.d_A;
-  bool doit[MAXP], ownq[MAXP];
-#pragma unroll
-  for (int j = 0; j < MAXP; ++j) {
-    doit[j] = pc.valid[j];
-    ownq[j] = pc.firstq[j];
-    if (doit[j]) {
-      pc.P[j] = 0.0;
-      if (ownq[j]) pc.Q[j] = 0.0;
-    }
-  }
-  if (NC <= 4)
-    fresh_sums_block<G, MAXP, 4>(A, N, NC, gmask, occ, doit, ownq, pc);
+  if (sy.n_carriers <= 4)
+    fresh_sums_tree<G, MAXP, 4>(sy.d_A, sy.n_sites, sy.n_carriers, gmask, occ, pc);
   else
-    fresh_sums_block<G, MAXP, 8>(A, N, NC, gmask, occ, doit, ownq, pc);
+    fresh_sums_tree<G, MAXP, 8>(sy.d_A, sy.n_sites, sy.n_carriers, gmask, occ, pc);
+}
+
+// Lane holding the sum of job u after job_sums (3-bit reversal of u; also
+// every lane 8k + that).
+__device__ __forceinline__ int job_lane(int u) {
+  return ((u & 1) << 2) | (u & 2) | ((u >> 2) & 1);
+}
+
+// Reduce-scatter of 8 jobs over the G lanes (G = 16 or 32): v[u] is lane g's
+// leaf (carrier g) of job u; lane g returns the sum of job
+// ((g & 1) << 2 | (g & 2) | ((g >> 2) & 1)).  Level l adds the partial sums
+// of lanes g and g ^ 2^l, i.e. the subtrees of 2^(l+1) carriers: the
+// balanced tree over carriers 0..31, with 9 additions and 9 shuffles for all
+// 8 jobs.
+template <int G>
+__device__ __forceinline__ double job_sums(unsigned gmask, int g, const double (&v)[8]) {
+  double w[4];
+  const bool b0 = g & 1, b1 = g & 2, b2 = g & 4;
 #pragma unroll
-  for (int j = 1; j < MAXP; ++j)
-    if (doit[j] && !ownq[j]) pc.Q[j] = pc.Q[j - 1];
+  for (int i = 0; i < 4; ++i) {
+    const double keep = b0 ? v[4 + i] : v[i];
+    const double send = b0 ? v[i] : v[4 + i];
+    w[i] = dadd(keep, __shfl_xor_sync(gmask, send, 1, G));
+  }
+  double x[2];
+#pragma unroll
+  for (int i = 0; i < 2; ++i) {
+    const double keep = b1 ? w[2 + i] : w[i];
+    const double send = b1 ? w[i] : w[2 + i];
+    x[i] = dadd(keep, __shfl_xor_sync(gmask, send, 2, G));
+  }
+  const double keep = b2 ? x[1] : x[0];
+  const double send = b2 ? x[0] : x[1];
+  double y = dadd(keep, __shfl_xor_sync(gmask, send, 4, G));
+#pragma unroll
+  for (int m = 8; m < G; m *= 2) y = dadd(y, __shfl_xor_sync(gmask, y, m, G));
+  return y;
 }
 
 // After carrier c_sel moved to n_sel: rebuild its S processes (slot s:
 // o = n_sel, n = nbr[n_sel, s]) and their sums, as setup_processes and
 // fresh_sums would give them.  Jobs i = 0..S (slot i for i < S; the carrier's
-// Q, row n_sel, for i = S) are done JB per round:
+// Q, row n_sel, for i = S) are done 8 per round:
 //   * lane c holds carrier c's site, so it loads A[row_i, occ_c] of every job
 //     of the round at once: one memory round trip for all the rows;
-//   * lane u sums job u in carrier order from +0, pulling the values with
-//     shuffles: the order of fresh_sums, hence the same doubles;
+//   * job_sums adds them across lanes in the tree order;
 //   * lane u builds the constants of slot job u.
 // Owner lanes pull the results.  Returns true on a bad index (no load is
-// issued with one).
-template <int G, int MAXP, int JB>
+// issued with one).  For more than 8 carriers (G = 16 or 32).
+template <int G, int MAXP>
 __device__ __forceinline__ bool rebuild_moved_jb(const PycdKmcSystem& sy,
                                                  const double2* __restrict__ coef,
                                                  int g, unsigned gmask, int occ,
                                                  int c_sel, int n_sel,
                                                  ProcCache<MAXP>& pc) {
+  constexpr int JB = 8;
   const int64_t N = sy.n_sites;
   const int S = sy.n_slots;
   const int NC = sy.n_carriers;
@@ -421,16 +462,7 @@ __device__ __forceinline__ bool rebuild_moved_jb(const PycdKmcSystem& sy,
 #pragma unroll
     for (int u = 0; u < JB; ++u)
       v[u] = (g < NC && i0 + u <= S) ? __ldg(A + (int64_t)row[u] * N + occ) : 0.0;
-    double sum = 0.0;
-    for (int c = 0; c < NC; ++c) {
-      double mine = 0.0;
-#pragma unroll
-      for (int u = 0; u < JB; ++u) {
-        const double t = gshfl<G>(gmask, v[u], c);
-        if (g == u) mine = t;
-      }
-      sum = dadd(sum, mine);
-    }
+    const double sum = job_sums<G>(gmask, g, v);
     int n = n_sel;
 #pragma unroll
     for (int u = 0; u < JB; ++u)
@@ -448,7 +480,7 @@ __device__ __forceinline__ bool rebuild_moved_jb(const PycdKmcSystem& sy,
     // the carrier's Q is summed in the round that holds job S
     const int qsrc = S - i0;
     double qv = 0.0;
-    if (qsrc < JB) qv = gshfl<G>(gmask, sum, qsrc);
+    if (qsrc < JB) qv = gshfl<G>(gmask, sum, job_lane(qsrc));
 #pragma unroll
     for (int j = 0; j < MAXP; ++j) {
       const bool mine = pc.valid[j] && pc.carrier[j] == c_sel;
@@ -462,7 +494,7 @@ __device__ __forceinline__ bool rebuild_moved_jb(const PycdKmcSystem& sy,
       const double v_lam = gshfl<G>(gmask, lam, sl);
       const double v_c1 = gshfl<G>(gmask, cf.x, sl);
       const double v_c0 = gshfl<G>(gmask, cf.y, sl);
-      const double v_p = gshfl<G>(gmask, sum, sl);
+      const double v_p = gshfl<G>(gmask, sum, job_lane(sl));
       if (take) {
         pc.oldsite[j] = n_sel;
         pc.newsite[j] = nn;
@@ -480,42 +512,23 @@ __device__ __forceinline__ bool rebuild_moved_jb(const PycdKmcSystem& sy,
   return bad;
 }
 
-// sum_c' rp[occ_c'] in carrier order from +0, loads issued U at a time
-// (every lane runs the shuffles; lanes with act == false load nothing)
+// A row's carrier sum for at most U carriers (one block of the tree order;
+// every lane runs the shuffles; lanes with act == false load nothing)
 template <int G, int U>
-__device__ __forceinline__ void carrier_row_block(const double* __restrict__ rp, bool act,
-                                                  int NC, unsigned gmask, int occ, int c0,
-                                                  double (&v)[U]) {
+__device__ __forceinline__ double carrier_row_tree(const double* __restrict__ rp, bool act,
+                                                   int NC, unsigned gmask, int occ) {
+  double v[U];
 #pragma unroll
   for (int u = 0; u < U; ++u) {
-    const int sc = gshfl<G>(gmask, occ, min(c0 + u, NC - 1));
-    v[u] = (act && c0 + u < NC) ? __ldg(rp + sc) : 0.0;
+    const int sc = gshfl<G>(gmask, occ, min(u, NC - 1));
+    v[u] = (act && u < NC) ? __ldg(rp + sc) : 0.0;
   }
+  return tree_reduce<U>(v);
 }
 
-// The loads of the next block are issued before the current block is summed,
-// so a row of many carriers costs about one memory round trip, not one per
-// block (the array rows of large systems come from DRAM).
-template <int G, int U>
-__device__ __forceinline__ double carrier_row_sum(const double* __restrict__ rp, bool act,
-                                                  int NC, unsigned gmask, int occ) {
-  double sum = 0.0;
-  double cur[U], nxt[U];
-  carrier_row_block<G, U>(rp, act, NC, gmask, occ, 0, cur);
-  for (int c0 = 0; c0 < NC; c0 += U) {
-    if (c0 + U < NC) carrier_row_block<G, U>(rp, act, NC, gmask, occ, c0 + U, nxt);
-#pragma unroll
-    for (int u = 0; u < U; ++u)
-      if (c0 + u < NC) sum = dadd(sum, cur[u]);
-#pragma unroll
-    for (int u = 0; u < U; ++u) cur[u] = nxt[u];
-  }
-  return sum;
-}
-
-// The moved carrier's rebuild for few carriers: job i = i0 + g on lane g (slot
-// i for i < S, the carrier's Q for i = S), each job lane loading its own row
-// entries; owner lanes pull the results.  Same doubles as rebuild_moved_jb.
+// The moved carrier's rebuild for at most 8 carriers: job i = i0 + g on lane
+// g (slot i for i < S, the carrier's Q for i = S), each job lane loading its
+// own row entries; owner lanes pull the results.
 template <int G, int MAXP>
 __device__ __forceinline__ bool rebuild_moved_direct(const PycdKmcSystem& sy,
                                               const double2* __restrict__ coef,
@@ -550,8 +563,8 @@ __device__ __forceinline__ bool rebuild_moved_direct(const PycdKmcSystem& sy,
       }
     }
     const double* rp = A + (int64_t)(act ? n : 0) * N;
-    const double sum = (NC <= 4) ? carrier_row_sum<G, 4>(rp, act, NC, gmask, occ)
-                                 : carrier_row_sum<G, 8>(rp, act, NC, gmask, occ);
+    const double sum = (NC <= 4) ? carrier_row_tree<G, 4>(rp, act, NC, gmask, occ)
+                                 : carrier_row_tree<G, 8>(rp, act, NC, gmask, occ);
     // the carrier's Q is computed in the round that holds job S
     const int qsrc = S - i0;
     double qv = 0.0;
@@ -587,18 +600,22 @@ __device__ __forceinline__ bool rebuild_moved_direct(const PycdKmcSystem& sy,
   return bad;
 }
 
-// Few carriers: the job lanes load their rows directly (no value
-// shuffles).  Many carriers: lane-parallel row loads (one round trip).
+// At most 8 carriers: the job lanes load their rows directly (no value
+// shuffles).  More: lane-parallel row loads (one round trip) and a
+// reduce-scatter of the sums (G >= 16 then, since G >= n_carriers).
 template <int G, int MAXP>
 __device__ __forceinline__ bool rebuild_moved(const PycdKmcSystem& sy,
                                               const double2* __restrict__ coef,
                                               int g, unsigned gmask, int occ,
                                               int c_sel, int n_sel,
                                               ProcCache<MAXP>& pc) {
-  constexpr int JB = G < 8 ? G : 8;
-  if (sy.n_carriers <= 8)
+  if constexpr (G < 16) {
     return rebuild_moved_direct<G, MAXP>(sy, coef, g, gmask, occ, c_sel, n_sel, pc);
-  return rebuild_moved_jb<G, MAXP, JB>(sy, coef, g, gmask, occ, c_sel, n_sel, pc);
+  } else {
+    if (sy.n_carriers <= 8)
+      return rebuild_moved_direct<G, MAXP>(sy, coef, g, gmask, occ, c_sel, n_sel, pc);
+    return rebuild_moved_jb<G, MAXP>(sy, coef, g, gmask, occ, c_sel, n_sel, pc);
+  }
 }
 
 // Rates of this lane's processes (core.py:1989-2050):
