@@ -297,9 +297,15 @@ typedef struct PycdKmcRng {
  * shape maxima are filled by pycd_kmc_upload_systems and are required by
  * pycd_kmc_advance_uploaded (pycd_kmc_advance computes them itself).       */
 typedef struct PycdKmcLaunch {
-  int32_t lanes_per_traj;       /* 1..32 (power of two); 0 = about 2 processes
-                                 * per lane, at least one lane per carrier   */
-  int32_t warps_per_block;      /* 1..8; 0 = 1                               */
+  int32_t lanes_per_traj;       /* 1..32 (power of two): lanes of one warp;
+                                 * 64 or 128: one block of 2 or 4 warps per
+                                 * trajectory (its FP64 work spread over 2 or
+                                 * 4 SM sub-partitions; same events and
+                                 * doubles); 0 = about 2 processes per lane,
+                                 * at least one lane per carrier, and the
+                                 * block form for more than 32 processes when
+                                 * trajectories x warps <= 4 x SMs          */
+  int32_t warps_per_block;      /* 1..8; 0 = 1 (ignored by the block form)  */
   int32_t blocks;               /* grid size; 0 = cover all trajectories     */
   int32_t max_processes;        /* max n_carriers * n_slots over the systems */
   int32_t max_carriers;         /* max n_carriers over the systems           */

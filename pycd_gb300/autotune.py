@@ -3,8 +3,8 @@
 The kernel's event streams do not depend on its launch shape (cumulative
 rates are fixed balanced-tree sums over the process index), so the shape is
 a pure performance choice.  ``tune`` times short probes of every candidate
-(lanes per trajectory x warps per block x register variant) on the real
-batch, restoring the
+(lanes per trajectory x warps per block x register variant, and one block
+of 2 or 4 warps per trajectory) on the real batch, restoring the
 batch state after each probe, and keeps the fastest.  Results are cached per
 (process count, carrier count, trajectory count) in-process.
 """
@@ -25,6 +25,12 @@ def candidates(max_processes, max_carriers):
             for minb in ((1, 2) if per_lane <= 2 else (1,)):
                 out.append({"lanes_per_traj": lanes, "warps_per_block": warps,
                             "min_blocks_per_sm": minb})
+    # one block of 2 or 4 warps per trajectory (more than 32 processes)
+    if max_processes > 32 and max_carriers <= 32:
+        for lanes in (64, 128):
+            if -(-max_processes // lanes) <= 4:
+                out.append({"lanes_per_traj": lanes, "warps_per_block": lanes // 32,
+                            "min_blocks_per_sm": 1})
     return out
 
 

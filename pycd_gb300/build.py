@@ -22,7 +22,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC",
               "-Xcompiler", "-fvisibility=hidden", "--expt-relaxed-constexpr"]
 SOURCES = ["capi.cu", "ewald.cu", "ewald_split.cu", "kmc.cu", "kmc_capped.cu",
-           "msd.cu"]
+           "kmc_cta.cu", "msd.cu"]
 
 
 def _nvcc():

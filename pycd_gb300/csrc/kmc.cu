@@ -49,11 +49,53 @@ static int pow2_at_least(int v) {
   return p;
 }
 
+static int sm_count() {
+  static int n = 0;
+  if (n == 0) {
+    int dev = 0, v = 0;
+    if (cudaGetDevice(&dev) == cudaSuccess &&
+        cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess && v > 0)
+      n = v;
+    else
+      return 1;
+  }
+  return n;
+}
+
+// One block of W = G / 32 warps per trajectory (G = 64 or 128).
+static int kmc_launch_blocks(const KmcArgs& a, int G, int max_np,
+                             const PycdKmcLaunch* launch, cudaStream_t s) {
+  PYCD_REQUIRE(G == 64 || G == 128,
+               "lanes_per_traj above 32 must be 64 or 128 (got %d)", G);
+  const int W = G / 32;
+  const int need = (max_np + G - 1) / G;
+  const int MAXP = need <= 1 ? 1 : need <= 2 ? 2 : need <= 4 ? 4 : 8;
+  PYCD_REQUIRE(MAXP <= 4, "processes per trajectory (%d) exceed 4 per lane at "
+               "%d lanes", max_np, G);
+  int64_t blocks = launch && launch->blocks ? launch->blocks : a.st.n_traj;
+  if (blocks < 1) blocks = 1;
+  if (blocks > 0x7fffffff) blocks = 0x7fffffff;
+  bool found = false;
+  const cudaError_t e = kmc_launch_cta(a, W, MAXP, (int)blocks, s, &found);
+  PYCD_REQUIRE(found, "no block-per-trajectory instance for %d warps x %d "
+               "processes per lane", W, MAXP);
+  if (e != cudaSuccess) return cuda_fail(e, "kmc_cta_kernel launch", __FILE__, __LINE__);
+  return PYCD_OK;
+}
+
 int kmc_launch(const KmcArgs& a, int max_np, int max_nc,
                const PycdKmcLaunch* launch, cudaStream_t s) {
   // default: about two processes per lane (the measured optimum for FP64
-  // issue per trajectory) and at least one lane per carrier
+  // issue per trajectory) and at least one lane per carrier; trajectories of
+  // more than 32 processes that are too few to give every SM sub-partition
+  // a warp run one block of 2 or 4 warps each (the FP64 issue of one
+  // trajectory is then spread over 2 or 4 sub-partitions)
   int G = launch && launch->lanes_per_traj ? launch->lanes_per_traj : 0;
+  if (G == 0 && max_np > 32) {
+    const int W = max_np > 64 ? 4 : 2;
+    if (a.st.n_traj * W <= 4 * (int64_t)sm_count()) G = 32 * W;
+  }
+  if (G > 32) return kmc_launch_blocks(a, G, max_np, launch, s);
   if (G == 0) {
     const int half = (max_np + 1) / 2;
     G = pow2_at_least(half < 32 ? half : 32);
@@ -108,6 +150,7 @@ int kmc_preload() {
   PYCD_KMC_SHAPES(PYCD_KMC_LOAD)
 #undef PYCD_KMC_LOAD
   if (e == cudaSuccess) e = kmc_preload_capped();
+  if (e == cudaSuccess) e = kmc_preload_cta();
   if (e != cudaSuccess) return cuda_fail(e, "cudaFuncGetAttributes", __FILE__, __LINE__);
   return PYCD_OK;
 }

@@ -387,40 +387,40 @@ __device__ __forceinline__ void fresh_sums(const PycdKmcSystem& sy, int g,
     fresh_sums_tree<G, MAXP, 8>(sy.d_A, sy.n_sites, sy.n_carriers, gmask, occ, pc);
 }
 
-// Lane holding the sum of job u after job_sums (3-bit reversal of u; also
-// every lane 8k + that).
+// Lane holding the sum of job u after job_sums<G, J>: the log2(J)-bit
+// reversal of u (and every lane J k + that).
+template <int J>
 __device__ __forceinline__ int job_lane(int u) {
-  return ((u & 1) << 2) | (u & 2) | ((u >> 2) & 1);
+  int r = 0;
+#pragma unroll
+  for (int b = 1; b < J; b *= 2) {
+    r = (r << 1) | (u & 1);
+    u >>= 1;
+  }
+  return r;
 }
 
-// Reduce-scatter of 8 jobs over the G lanes (G = 16 or 32): v[u] is lane g's
-// leaf (carrier g) of job u; lane g returns the sum of job
-// ((g & 1) << 2 | (g & 2) | ((g >> 2) & 1)).  Level l adds the partial sums
-// of lanes g and g ^ 2^l, i.e. the subtrees of 2^(l+1) carriers: the
-// balanced tree over carriers 0..31, with 9 additions and 9 shuffles for all
-// 8 jobs.
-template <int G>
-__device__ __forceinline__ double job_sums(unsigned gmask, int g, const double (&v)[8]) {
-  double w[4];
-  const bool b0 = g & 1, b1 = g & 2, b2 = g & 4;
+// Reduce-scatter of J jobs (J = 1, 2, 4 or 8) over G lanes: v[u] is lane
+// g's leaf (carrier g) of job u; lane g returns the sum of the job whose
+// job_lane<J> is g mod J.  Level l adds the partial sums of lanes g and
+// g ^ 2^l, i.e. the subtrees of 2^(l+1) carriers: the balanced tree over
+// carriers 0..G-1, with J - 1 + log2(G/J) additions and as many shuffles
+// for all J jobs.
+template <int G, int J>
+__device__ __forceinline__ double job_sums(unsigned gmask, int g, double (&v)[J]) {
 #pragma unroll
-  for (int i = 0; i < 4; ++i) {
-    const double keep = b0 ? v[4 + i] : v[i];
-    const double send = b0 ? v[i] : v[4 + i];
-    w[i] = dadd(keep, __shfl_xor_sync(gmask, send, 1, G));
+  for (int l = 0, n = J / 2; n >= 1; ++l, n /= 2) {
+    const bool up = (g >> l) & 1;
+#pragma unroll
+    for (int i = 0; i < n; ++i) {
+      const double keep = up ? v[n + i] : v[i];
+      const double send = up ? v[i] : v[n + i];
+      v[i] = dadd(keep, __shfl_xor_sync(gmask, send, 1 << l, G));
+    }
   }
-  double x[2];
+  double y = v[0];
 #pragma unroll
-  for (int i = 0; i < 2; ++i) {
-    const double keep = b1 ? w[2 + i] : w[i];
-    const double send = b1 ? w[i] : w[2 + i];
-    x[i] = dadd(keep, __shfl_xor_sync(gmask, send, 2, G));
-  }
-  const double keep = b2 ? x[1] : x[0];
-  const double send = b2 ? x[0] : x[1];
-  double y = dadd(keep, __shfl_xor_sync(gmask, send, 4, G));
-#pragma unroll
-  for (int m = 8; m < G; m *= 2) y = dadd(y, __shfl_xor_sync(gmask, y, m, G));
+  for (int m = J; m < G; m *= 2) y = dadd(y, __shfl_xor_sync(gmask, y, m, G));
   return y;
 }
 
@@ -462,7 +462,7 @@ __device__ __forceinline__ bool rebuild_moved_jb(const PycdKmcSystem& sy,
 #pragma unroll
     for (int u = 0; u < JB; ++u)
       v[u] = (g < NC && i0 + u <= S) ? __ldg(A + (int64_t)row[u] * N + occ) : 0.0;
-    const double sum = job_sums<G>(gmask, g, v);
+    const double sum = job_sums<G, JB>(gmask, g, v);
     int n = n_sel;
 #pragma unroll
     for (int u = 0; u < JB; ++u)
@@ -480,7 +480,7 @@ __device__ __forceinline__ bool rebuild_moved_jb(const PycdKmcSystem& sy,
     // the carrier's Q is summed in the round that holds job S
     const int qsrc = S - i0;
     double qv = 0.0;
-    if (qsrc < JB) qv = gshfl<G>(gmask, sum, job_lane(qsrc));
+    if (qsrc < JB) qv = gshfl<G>(gmask, sum, job_lane<JB>(qsrc));
 #pragma unroll
     for (int j = 0; j < MAXP; ++j) {
       const bool mine = pc.valid[j] && pc.carrier[j] == c_sel;
@@ -494,7 +494,7 @@ __device__ __forceinline__ bool rebuild_moved_jb(const PycdKmcSystem& sy,
       const double v_lam = gshfl<G>(gmask, lam, sl);
       const double v_c1 = gshfl<G>(gmask, cf.x, sl);
       const double v_c0 = gshfl<G>(gmask, cf.y, sl);
-      const double v_p = gshfl<G>(gmask, sum, job_lane(sl));
+      const double v_p = gshfl<G>(gmask, sum, job_lane<JB>(sl));
       if (take) {
         pc.oldsite[j] = n_sel;
         pc.newsite[j] = nn;

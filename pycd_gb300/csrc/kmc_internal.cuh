@@ -33,6 +33,11 @@ int kmc_preload();
 cudaError_t kmc_launch_capped(const KmcArgs& a, int G, int MAXP, int warps_per_block,
                               int blocks, cudaStream_t s, bool* found);
 cudaError_t kmc_preload_capped();
+// the block-per-trajectory instances (kmc_cta.cu): W warps per trajectory;
+// *found = false when there is no instance for (W, MAXP)
+cudaError_t kmc_launch_cta(const KmcArgs& a, int W, int MAXP, int blocks,
+                           cudaStream_t s, bool* found);
+cudaError_t kmc_preload_cta();
 int kmc_coef_launch(const PycdKmcSystem& s, double2* coef, cudaStream_t st);
 int exp_probe_launch(const double* x, int64_t n, double* ours, double* ref,
                      cudaStream_t s);

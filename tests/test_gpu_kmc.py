@@ -234,8 +234,9 @@ def test_event_stream_independent_of_launch_shape(cuda_ready):
     rng = np.random.default_rng(5)
     occ = np.stack([rng.choice(3600, size=4, replace=False) for _ in range(T)])
     results = []
-    shapes = [(4, 1), (8, 1), (8, 2), (16, 1), (16, 2), (32, 1), (32, 2)]
-    for lanes, minb in shapes:  # minb 2: the 128-register variant
+    shapes = [(4, 1), (8, 1), (8, 2), (16, 1), (16, 2), (32, 1), (32, 2), (64, 1),
+              (128, 1)]
+    for lanes, minb in shapes:  # minb 2: the 128-register variant; > 32: block form
         eng = KmcEngine(tables, launch={"lanes_per_traj": lanes,
                                         "min_blocks_per_sm": minb})
         b = KmcBatch(occ, step_capacity=n)
@@ -281,7 +282,60 @@ def test_deferred_times_equal_exact_chain_across_shapes(cuda_ready):
 
     ref = run_until_done(8, exact=True)
     assert ref["step"].min() > 10 * rows  # many crossings per trajectory
-    for lanes in (4, 8, 16, 32):  # 2 and 1 or 4 processes per lane
+    for lanes in (4, 8, 16, 32, 64, 128):  # 2 and 1 or 4 processes per lane
         got = run_until_done(lanes, exact=False)
         for k in ref:
             assert np.array_equal(got[k], ref[k]), (lanes, k)
+
+
+@pytest.mark.parametrize("n_carriers", [16, 32])
+def test_block_per_trajectory_equals_warp_form(cuda_ready, n_carriers):
+    """One block of 2 or 4 warps per trajectory forms the same balanced trees
+    as one warp (its warp totals are the top nodes of the process tree; its
+    rebuild sums are the same carrier trees), so events, times, sites,
+    energies, displacements and the stored carrier sums must equal the warp
+    form's bit for bit, across a chunk boundary off the refresh period."""
+    import torch
+    sysm, tables, run, cfg, arr = _corundum3600(n_carriers)
+    T, n, seed = 24, 2000, 4242
+    rng = np.random.default_rng(11)
+    occ = np.stack([rng.choice(3600, size=n_carriers, replace=False) for _ in range(T)])
+    shapes = (16, 32, 64, 128) if n_carriers == 16 else (32, 64, 128)
+    keys = ("step_proc", "step_time", "occ", "csum", "energy", "disp", "time")
+    results = []
+    for lanes in shapes:
+        eng = KmcEngine(tables, launch={"lanes_per_traj": lanes})
+        b = KmcBatch(occ, step_capacity=n)
+        eng.advance(b, n // 3, eng.rng_struct(seed=seed))
+        eng.advance(b, n - n // 3, eng.rng_struct(seed=seed))
+        torch.cuda.synchronize()
+        assert (b.step.cpu().numpy() == n).all(), lanes
+        results.append({k: getattr(b, k).cpu().numpy() for k in keys})
+    for lanes, r in zip(shapes[1:], results[1:]):
+        for k in keys:
+            assert np.array_equal(r[k], results[0][k]), (lanes, k)
+
+
+def test_block_form_matches_oracle_with_32_carriers(cuda_ready):
+    """A 32-carrier trajectory (128 processes) in the 4-warp block form
+    against the oracle fed the same Philox uniforms: identical events,
+    times within 1e-12 relative."""
+    import torch
+    sysm, tables, run, cfg, arr = _corundum3600(32)
+    seed, m = 2024, 600
+    occ0 = np.random.default_rng(21).choice(3600, size=32, replace=False)
+    eng = KmcEngine(tables, launch={"lanes_per_traj": 128})
+    b = KmcBatch(occ0[None], step_capacity=m)
+    eng.advance(b, m, eng.rng_struct(seed=seed))
+    torch.cuda.synchronize()
+    assert int(b.step.item()) == m
+    A = tables.A.cpu().numpy()
+    q_fixed = np.zeros(3600)
+    q_fixed[cfg["dopants"]] = cfg["dopant_charge"]
+    otab = ko.Tables(sysm.hop_neighbor_list, "Fe:Fe", np.zeros(3600, int), 12, 0, 12,
+                     sysm.material.lambda_values["Fe:Fe"], sysm.material.v_ab["Fe:Fe"])
+    u = np.array([v for s in range(m) for v in philox.step_uniforms(seed, 0, s)])
+    o = ko.run(A, otab, list(occ0), q_fixed, -1.0, np.zeros(3600), sysm.material.vn,
+               run.temp, u, run.time_interval, tables.n_path_steps)
+    assert np.array_equal(o["proc"], b.step_proc[0, :m].cpu().numpy())
+    assert np.abs(o["time"][1:] / b.step_time[0, :m].cpu().numpy() - 1).max() < TIME_RTOL

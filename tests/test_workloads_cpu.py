@@ -38,11 +38,17 @@ def test_poisson_arrivals_statistics():
 
 def test_autotune_candidates_respect_kernel_limits():
     for npr, nc in ((4, 1), (16, 4), (64, 16), (128, 32), (96, 32)):
-        for c in candidates(npr, nc):
+        cands = candidates(npr, nc)
+        for c in cands:
             lanes = c["lanes_per_traj"]
             assert lanes >= nc and -(-npr // lanes) <= 8
             # the register-capped instances exist for <= 2 processes per lane
             assert c["min_blocks_per_sm"] == 1 or -(-npr // lanes) <= 2
+            # block-per-trajectory instances: 2 or 4 warps, <= 4 processes per lane
+            if lanes > 32:
+                assert lanes in (64, 128) and c["warps_per_block"] == lanes // 32
+                assert -(-npr // lanes) <= 4 and npr > 32
+        assert any(c["lanes_per_traj"] > 32 for c in cands) == (npr > 32)
 
 
 def test_monoclinic_hop_shells_have_three_neighbours():
