@@ -118,7 +118,7 @@ def time_plain(tables, occ, n_steps=20000):
     import torch
     from pycd_gb300.kmc import KmcBatch, KmcEngine
     best = 0.0
-    for lanes in (8, 16, 32):
+    for lanes in (8, 16, 32, 64, 128):  # 64, 128: one block of 2 or 4 warps
         eng = KmcEngine(tables, launch={"lanes_per_traj": lanes})
         b = KmcBatch(occ[:1])
         eng.advance(b, 2000, eng.rng_struct(seed=SEED))
@@ -604,7 +604,7 @@ def plain_bench(args):
     u = np.random.default_rng(0).random(2 * n_steps)
     u_dev = torch.as_tensor(u).cuda()[None, :]
     best, proc, times = None, None, None
-    for lanes in (8, 16, 32):  # the plain form at its fastest lane count
+    for lanes in (8, 16, 32, 64, 128):  # the plain form at its fastest lane count
         eng = KmcEngine(tables, launch={"lanes_per_traj": lanes})
         for rep in range(2):
             b = KmcBatch([[site]], step_capacity=n_steps,

@@ -349,6 +349,15 @@ PYCD_API int pycd_kmc_advance_uploaded(int32_t n_systems, const PycdKmcState* st
                               void* d_workspace, size_t workspace_bytes,
                               void* stream);
 
+/* The lanes per trajectory the launcher picks when PycdKmcLaunch leaves
+ * them at 0, for n_traj trajectories of at most max_processes processes
+ * and max_carriers carriers on the current device (a caller that launches
+ * a batch whose running trajectories are fewer than its slots passes the
+ * running count).  No counterpart in the reference (its loop has no launch
+ * shape).                                                                  */
+PYCD_API int pycd_kmc_default_lanes(int32_t max_processes, int32_t max_carriers,
+                           int64_t n_traj, int32_t* lanes);
+
 /* Philox4x32-10 uniforms exactly as the kernels draw them (for tests and
  * for replaying a batched trajectory in another form): fills
  * h_or_d_out[2*i + {0,1}] for steps [step0, step0 + n_steps) of trajectory

@@ -144,6 +144,8 @@ _PROTOS = {
                                             C.c_int64, P(KmcLaunch),
                                             C.c_void_p, C.c_size_t,
                                             C.c_void_p]),
+    "pycd_kmc_default_lanes": (C.c_int, [C.c_int32, C.c_int32, C.c_int64,
+                                         P(C.c_int32)]),
     "pycd_philox_uniforms": (C.c_int, [C.c_uint64, C.c_uint64, C.c_int64,
                                        C.c_int64, C.c_void_p, C.c_void_p]),
     "pycd_kmc_rate_coefficients": (C.c_int, [P(KmcSystem), C.c_void_p, C.c_void_p]),

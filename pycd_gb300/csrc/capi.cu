@@ -275,6 +275,16 @@ int pycd_kmc_upload_systems(const PycdKmcSystem* systems, int32_t n_systems,
   return PYCD_OK;
 }
 
+int pycd_kmc_default_lanes(int32_t max_processes, int32_t max_carriers,
+                           int64_t n_traj, int32_t* lanes) {
+  clear_error();
+  PYCD_REQUIRE(lanes && max_processes > 0 && max_carriers > 0 && max_carriers <= 32 &&
+                   n_traj >= 0,
+               "pycd_kmc_default_lanes: bad arguments");
+  *lanes = kmc_default_lanes(max_processes, max_carriers, n_traj);
+  return PYCD_OK;
+}
+
 int pycd_kmc_advance_uploaded(int32_t n_systems, const PycdKmcState* state,
                               const PycdKmcOutputs* out, const PycdKmcRng* rng,
                               int64_t max_steps, const PycdKmcLaunch* launch,

@@ -83,24 +83,31 @@ static int kmc_launch_blocks(const KmcArgs& a, int G, int max_np,
   return PYCD_OK;
 }
 
+// Lanes per trajectory when the launch leaves them open.  The fewest lanes
+// (about two processes per lane, at least one lane per carrier) spend the
+// fewest FP64 instructions per step; more lanes, up to one block of 4 warps,
+// shorten a step by spreading its FP64 instructions over more SM
+// sub-partitions.  Measured on GB300 (8 to 32 carriers, 38 to 4,864
+// trajectories): widening pays while the launch keeps at most 2 warps per
+// sub-partition, i.e. 8 warps per SM.
+int kmc_default_lanes(int max_np, int max_nc, int64_t n_traj) {
+  const int half = (max_np + 1) / 2;
+  int G = pow2_at_least(half < 32 ? half : 32);
+  if (G < 2 && max_np > 1) G = 2;  // one lane runs only a single process
+  if (G < max_nc) G = pow2_at_least(max_nc);
+  const int wide = 2 * pow2_at_least(max_np > 1 ? max_np : 1);
+  const int cap = wide < 32 ? 32 : wide > 128 ? 128 : wide;
+  const int64_t warp_budget = 8 * (int64_t)sm_count();
+  const int64_t T = n_traj > 0 ? n_traj : 1;
+  while (2 * G <= cap && T * 2 * G <= 32 * warp_budget) G *= 2;
+  return G;
+}
+
 int kmc_launch(const KmcArgs& a, int max_np, int max_nc,
                const PycdKmcLaunch* launch, cudaStream_t s) {
-  // default: about two processes per lane (the measured optimum for FP64
-  // issue per trajectory) and at least one lane per carrier; trajectories of
-  // more than 32 processes that are too few to give every SM sub-partition
-  // a warp run one block of 2 or 4 warps each (the FP64 issue of one
-  // trajectory is then spread over 2 or 4 sub-partitions)
-  int G = launch && launch->lanes_per_traj ? launch->lanes_per_traj : 0;
-  if (G == 0 && max_np > 32) {
-    const int W = max_np > 64 ? 4 : 2;
-    if (a.st.n_traj * W <= 4 * (int64_t)sm_count()) G = 32 * W;
-  }
+  int G = launch && launch->lanes_per_traj ? launch->lanes_per_traj
+                                           : kmc_default_lanes(max_np, max_nc, a.st.n_traj);
   if (G > 32) return kmc_launch_blocks(a, G, max_np, launch, s);
-  if (G == 0) {
-    const int half = (max_np + 1) / 2;
-    G = pow2_at_least(half < 32 ? half : 32);
-    if (G < 2 && max_np > 1) G = 2;  // one lane runs only a single process
-  }
   if (G < max_nc) G = pow2_at_least(max_nc);
   PYCD_REQUIRE(G >= 1 && G <= 32 && (G & (G - 1)) == 0,
                "lanes_per_traj must be a power of two in [1, 32] (got %d)", G);

@@ -28,6 +28,7 @@ struct KmcArgs {
 int kmc_launch(const KmcArgs& a, int max_np, int max_nc,
                const PycdKmcLaunch* launch, cudaStream_t s);
 int kmc_preload();
+int kmc_default_lanes(int max_np, int max_nc, int64_t n_traj);
 // the register-capped instances (kmc_capped.cu); *found = false when
 // there is no instance for (G, MAXP)
 cudaError_t kmc_launch_capped(const KmcArgs& a, int G, int MAXP, int warps_per_block,

@@ -22,6 +22,17 @@ def _dev():
     return torch.device("cuda", torch.cuda.current_device())
 
 
+def default_lanes(max_processes, max_carriers, n_traj):
+    """Lanes per trajectory the launcher picks for ``n_traj`` trajectories
+    (64 or 128: one block of 2 or 4 warps per trajectory).  A batch whose
+    running trajectories are fewer than its slots passes the running count
+    and sets the result on its launch."""
+    out = C.c_int32(0)
+    nat.check(nat.lib().pycd_kmc_default_lanes(int(max_processes), int(max_carriers),
+                                               int(n_traj), C.byref(out)))
+    return int(out.value)
+
+
 class KmcTables(object):
     """Device tables of one system (see module docstring)."""
 

@@ -23,7 +23,7 @@ import time
 import numpy as np
 
 from . import _native as nat
-from .kmc import KmcBatch, KmcEngine
+from .kmc import KmcBatch, KmcEngine, default_lanes
 
 
 def _pow2(v):
@@ -242,6 +242,9 @@ class KmcServer(object):
         b.stream.wait_stream(torch.cuda.current_stream())
         if b.dirty:
             b.upload()
+        # launch shape for the jobs now in the bucket, not its slot count
+        b.engine.launch.lanes_per_traj = default_lanes(b.np_bound, b.nc_bound,
+                                                       max(1, len(b.jobs)))
         b.engine.advance(b.batch, self.chunk_for(b),
                          b.engine.rng_struct(seed=self.seed, traj_ids=b.ids),
                          stream=b.stream)

@@ -28,6 +28,24 @@ def test_library_exports_every_declared_symbol():
     assert lib.pycd_abi_version() == 2
 
 
+def test_default_lanes_rule():
+    """The launcher's default shape: at least one lane per carrier, about two
+    processes per lane for large batches, a block of 4 warps for a single
+    128-process trajectory, never more than 4 processes per lane in a block
+    (whatever the SM count of the device, or 1 without one)."""
+    from pycd_gb300.kmc import default_lanes
+    assert default_lanes(16, 4, 10**6) == 8
+    assert default_lanes(128, 32, 1) == 128
+    assert default_lanes(64, 16, 1) == 128
+    for npr, nc in ((4, 1), (16, 4), (32, 8), (64, 16), (128, 32), (96, 32)):
+        for T in (1, 10, 100, 1000, 10**4, 10**6):
+            g = default_lanes(npr, nc, T)
+            assert g & (g - 1) == 0 and nc <= g <= 128
+            assert -(-npr // g) <= (4 if g > 32 else 8)
+    with pytest.raises(nat.NativeError):
+        default_lanes(16, 33, 1)
+
+
 def test_library_reports_missing_device_as_error():
     import torch
     if torch.cuda.is_available():
