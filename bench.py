@@ -501,6 +501,81 @@ def serving_bench(args):
     print(json.dumps(line), flush=True)
 
 
+def heavy_bench(args):
+    """Trajectories of many carriers (corundum 10x10x3 = 3,600 sites, 16 and
+    32 electrons, no dopants): per-step latency and aggregate steps/s of the
+    warp form (one warp per trajectory) and the block forms (2 or 4 warps
+    per trajectory) for 1, 152 and 608 trajectories, and the shape the
+    default launcher picks.  Events are the same in every form; the line
+    also checks that on the first trajectory."""
+    import torch
+    from pycd_gb300 import _native as nat
+    from pycd_gb300 import workloads as wl
+    from pycd_gb300.kmc import KmcBatch, KmcEngine, default_lanes
+    nat.require_device()
+    system = wl.corundum(N_CELLS)
+    A = system.get_precomputed_array_device("fp64")
+    n_steps, warm = args.heavy_steps, 300
+    trajs = [args.traj] if args.traj != N_TRAJ else [1, 152, 608]
+    rows = []
+    for nc in (16, 32):
+        tables, run = wl.batched_tables(system, A, nc, [], 1.0, t_final=1e30,
+                                        time_interval=1e27)
+        shapes = [args.lanes] if args.lanes else [32, 64, 128]
+        for T in trajs:
+            occ = np.stack([np.random.default_rng(SEED + i).choice(3600, nc, replace=False)
+                            for i in range(T)]).astype(np.int32)
+            procs = {}
+            for lanes in shapes:
+                eng = KmcEngine(tables, launch={"lanes_per_traj": lanes})
+                b = KmcBatch(occ, step_capacity=warm)
+                eng.advance(b, warm, eng.rng_struct(seed=SEED))
+                torch.cuda.synchronize()
+                procs[lanes] = b.step_proc[0].cpu().numpy()
+                # timed steps record no per-step output (no exact time per step)
+                b.step_time = b.step_proc = None
+                b.step_capacity = 0
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record()
+                eng.advance(b, n_steps, eng.rng_struct(seed=SEED))
+                e1.record()
+                torch.cuda.synchronize()
+                ms = e0.elapsed_time(e1)
+                rows.append({"carriers": nc, "trajectories": T, "lanes": lanes,
+                             "us_per_step": 1e3 * ms / n_steps,
+                             "steps_per_s": T * n_steps / (ms / 1e3)})
+            same = all(np.array_equal(v, procs[shapes[0]]) for v in procs.values())
+            rows.append({"carriers": nc, "trajectories": T,
+                         "default_lanes": default_lanes(4 * nc, nc, T),
+                         "events_equal_across_forms": bool(same)})
+    line = {"workload": "heavy", "metric": "KMC step latency and steps/s, many carriers",
+            "unit": "us/step", "dtype": "f64", "data": "synthetic",
+            "config": {"lattice": "corundum 10x10x3 = 3,600 sites", "slots": 4,
+                       "timed_steps": n_steps, "warmup_steps": warm,
+                       "lanes": "32 = one warp; 64 / 128 = one block of 2 / 4 warps"},
+            "rows": rows}
+    if not args.no_cpu_baseline:
+        from oracle import kmc_oracle as ko
+        from oracle import philox
+        tables, run = wl.batched_tables(system, A, 32, [], 1.0, t_final=1e30,
+                                        time_interval=1e27)
+        m = system.material
+        otab = ko.Tables(system.hop_neighbor_list, "Fe:Fe", np.zeros(3600, int), 12, 0, 12,
+                         m.lambda_values["Fe:Fe"], m.v_ab["Fe:Fe"])
+        occ0 = np.random.default_rng(SEED).choice(3600, 32, replace=False)
+        k = 200
+        u = np.array([v for st in range(k) for v in philox.step_uniforms(SEED, 0, st)])
+        Ah = A.cpu().numpy()
+        t0 = time.perf_counter()
+        ko.run(Ah, otab, list(occ0), np.zeros(3600), -1.0, np.zeros(3600), m.vn, run.temp,
+               u, run.time_interval, tables.n_path_steps, max_steps=k)
+        dt = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": 1e6 * dt / k, "unit": "us/step", "cores": 1,
+                                "kind": "port", "sample": "one 32-carrier trajectory, "
+                                "%d steps, oracle port of the reference loop" % k}
+    print(json.dumps(line), flush=True)
+
+
 def msd_bench(args):
     """MSD analysis (Analysis.compute_msd) on device: the parameters of the
     reference's Hematite example (t_final 1e-4 s, interval 1e-8 s -> 10,001
@@ -698,7 +773,8 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--workload", default="batched",
                     choices=["batched", "plain", "ewald-split", "uneven", "serving",
-                             "msd", "ewald-params"])
+                             "msd", "ewald-params", "heavy"])
+    ap.add_argument("--heavy-steps", type=int, default=2000)
     ap.add_argument("--jobs", type=int, default=2000)
     ap.add_argument("--max-job-steps", type=int, default=1_000_000)
     ap.add_argument("--sizes", default="")
@@ -730,6 +806,8 @@ def main():
         return plain_bench(args)
     if args.workload == "ewald-params":
         return ewald_params_bench(args)
+    if args.workload == "heavy":
+        return heavy_bench(args)
 
     import torch
     import torch.distributed as dist
