@@ -23,72 +23,119 @@ namespace pycd {
 
 constexpr int kCtaMaxJobs = 33;  // n_slots + 1 rebuild jobs, n_slots <= 32
 
+// Neighbour lists of the processes' destination sites are cached per process
+// (in registers) for up to this many slots, so that the moved carrier's new
+// neighbours are known when the event is: its rebuild then needs no
+// dependent load of the neighbour table.
+constexpr int kNbrCache = 4;
+
 struct CtaShared {
   double wsum[4];
   double de_sel, k_sel;
   int sel, n_sel, o_sel, pad;
+  int nb[kNbrCache];  // neighbours of n_sel (from the selected process' cache)
   // rebuilt processes of the moved carrier: job i < S is slot i, job S its Q
   double jp[kCtaMaxJobs], jdphi[kCtaMaxJobs], jt02q[kCtaMaxJobs], jde[kCtaMaxJobs];
   double jlam[kCtaMaxJobs], jc1[kCtaMaxJobs], jc0[kCtaMaxJobs];
   int jn[kCtaMaxJobs];
 };
 
-// The moved carrier's jobs (slot i for i < S: site n = nbr[n_sel, i], its
-// constants and P; job S: the carrier's Q, row n_sel), 8 per round, job
-// i0 + w + W u on warp w: its lane c loads A[row, occ_c] for its jobs,
-// job_sums adds them in the tree order, and the results go to shared
-// memory.  Returns true on a bad index (no load is issued with one).
-template <int W>
-__device__ __forceinline__ bool cta_rebuild_jobs(const PycdKmcSystem& sy,
-                                                 const double2* __restrict__ coef,
-                                                 int w, int l, int occ, int n_sel,
-                                                 CtaShared& sh) {
+// The carrier sums after carrier c_sel hopped o_sel -> n_sel.
+//   * Other carriers' processes: P += A[n, n_sel] - A[n, o_sel] (and Q).
+//   * The moved carrier's jobs (slot i < S: site n = nbr[n_sel, i], its
+//     constants and P; job S: the carrier's Q, row n_sel), 8 per round, job
+//     i0 + w + W u on warp w: its lane c loads A[row, occ_c], job_sums adds
+//     them in the tree order, and the results go to shared memory.
+// Every load of the first round (the incremental entries, the job rows and
+// the slot constants) is issued before any of them is used, and the rows
+// come from the neighbour cache (nbc, S <= kNbrCache): one memory round trip.
+// Returns true on a bad index (no load is issued with one).
+template <int W, int MAXP>
+__device__ __forceinline__ bool cta_update_sums(const PycdKmcSystem& sy,
+                                                const double2* __restrict__ coef,
+                                                int w, int l, int occ, int c_sel,
+                                                int o_sel, int n_sel, const int* nbc,
+                                                ProcCache<MAXP>& pc, CtaShared& sh) {
   constexpr int JW = 8 / W;
   const int64_t N = sy.n_sites;
   const int S = sy.n_slots;
   const int NC = sy.n_carriers;
   const double* __restrict__ A = sy.d_A;
   const int64_t ro = (int64_t)n_sel * N;
+  // incremental entries
+  double an[MAXP], ao[MAXP], qn[MAXP], qo[MAXP];
+  bool upd[MAXP], updq[MAXP];
+#pragma unroll
+  for (int j = 0; j < MAXP; ++j) {
+    upd[j] = pc.valid[j] && pc.carrier[j] != c_sel;
+    updq[j] = upd[j] && (pc.firstq[j] || j == 0);
+    const int64_t rn = (int64_t)pc.newsite[j] * N, rq = (int64_t)pc.oldsite[j] * N;
+    an[j] = upd[j] ? __ldg(A + rn + n_sel) : 0.0;
+    ao[j] = upd[j] ? __ldg(A + rn + o_sel) : 0.0;
+    qn[j] = updq[j] ? __ldg(A + rq + n_sel) : 0.0;
+    qo[j] = updq[j] ? __ldg(A + rq + o_sel) : 0.0;
+  }
   bool bad = false;
   for (int i0 = 0; i0 <= S; i0 += 8) {
     int row[JW];
-    double v[JW];
 #pragma unroll
     for (int u = 0; u < JW; ++u) {
       const int i = i0 + w + W * u;
       int r = n_sel;
       if (i < S) {
-        r = sy.d_nbr[(int64_t)n_sel * S + i];
+        r = nbc ? nbc[i] : sy.d_nbr[(int64_t)n_sel * S + i];
         if (r < 0 || r >= N) { bad = true; r = n_sel; }
       }
       row[u] = r;
     }
+    double v[JW];
 #pragma unroll
     for (int u = 0; u < JW; ++u)
       v[u] = (l < NC && i0 + w + W * u <= S) ? __ldg(A + (int64_t)row[u] * N + occ) : 0.0;
+    // slot constants of job i0 + w + W l on lane l < JW
+    const int ic = i0 + w + W * l;
+    const bool cst = l < JW && ic < S;
+    int n = n_sel;
+#pragma unroll
+    for (int u = 0; u < JW; ++u)
+      if (u == l) n = row[u];
+    const int64_t slot = (int64_t)n_sel * S + (cst ? ic : 0);
+    double2 cf = make_double2(0.0, 0.0);
+    double phn = 0.0, ph0 = 0.0, en = 0.0, e0 = 0.0, aoo = 0.0, aon = 0.0, lam = 0.0;
+    if (cst) {
+      cf = __ldg(coef + slot);
+      phn = __ldg(sy.d_phi_bg + n);
+      ph0 = __ldg(sy.d_phi_bg + n_sel);
+      en = __ldg(sy.d_e_rel + n);
+      e0 = __ldg(sy.d_e_rel + n_sel);
+      aoo = __ldg(A + ro + n_sel);
+      aon = __ldg(A + ro + n);
+      lam = __ldg(sy.d_lam + slot);
+    }
+    if (i0 == 0) {
+#pragma unroll
+      for (int j = 0; j < MAXP; ++j) {
+        if (upd[j]) pc.P[j] = dadd(pc.P[j], dsub(an[j], ao[j]));
+        if (updq[j])
+          pc.Q[j] = dadd(pc.Q[j], dsub(qn[j], qo[j]));
+        else if (upd[j])
+          pc.Q[j] = pc.Q[j > 0 ? j - 1 : 0];
+      }
+    }
     const double sum = job_sums<32, JW>(0xffffffffu, l, v);
 #pragma unroll
     for (int u = 0; u < JW; ++u) {
       const int i = i0 + w + W * u;
       if (i <= S && l == job_lane<JW>(u)) sh.jp[i] = sum;
     }
-    if (l < JW) {
-      const int i = i0 + w + W * l;
-      int n = n_sel;
-#pragma unroll
-      for (int u = 0; u < JW; ++u)
-        if (u == l) n = row[u];
-      if (i < S) {
-        const int64_t slot = (int64_t)n_sel * S + i;
-        const double2 cf = __ldg(coef + slot);
-        sh.jn[i] = n;
-        sh.jdphi[i] = dsub(__ldg(sy.d_phi_bg + n), __ldg(sy.d_phi_bg + n_sel));
-        sh.jt02q[i] = dmul(sy.carrier_charge, dsub(__ldg(A + ro + n_sel), __ldg(A + ro + n)));
-        sh.jde[i] = dsub(__ldg(sy.d_e_rel + n), __ldg(sy.d_e_rel + n_sel));
-        sh.jlam[i] = __ldg(sy.d_lam + slot);
-        sh.jc1[i] = cf.x;
-        sh.jc0[i] = cf.y;
-      }
+    if (cst) {
+      sh.jn[ic] = n;
+      sh.jdphi[ic] = dsub(phn, ph0);
+      sh.jt02q[ic] = dmul(sy.carrier_charge, dsub(aoo, aon));
+      sh.jde[ic] = dsub(en, e0);
+      sh.jlam[ic] = lam;
+      sh.jc1[ic] = cf.x;
+      sh.jc0[ic] = cf.y;
     }
   }
   return bad;
@@ -175,6 +222,16 @@ __device__ void advance_trajectory_cta(const KmcArgs& a, int64_t t, CtaShared& s
   if (__syncthreads_or(bad)) {
     if (g == 0) st.d_status[t] = PYCD_TRAJ_BAD_INDEX;
     return;
+  }
+  // neighbours of each process' destination site (checked where used)
+  const bool use_nbc = S <= kNbrCache;
+  int nbrc[MAXP][kNbrCache];
+#pragma unroll
+  for (int j = 0; j < MAXP; ++j) {
+#pragma unroll
+    for (int s = 0; s < kNbrCache; ++s)
+      nbrc[j][s] = (use_nbc && pc.valid[j] && s < S)
+                       ? __ldg(sy.d_nbr + (int64_t)pc.newsite[j] * S + s) : 0;
   }
   if (csum && (step & (R - 1)) != 0) {
 #pragma unroll
@@ -285,7 +342,18 @@ __device__ void advance_trajectory_cta(const KmcArgs& a, int64_t t, CtaShared& s
         const int os = __shfl_sync(full, pc.oldsite[j], base);
         if (j == jsel) { de_s = d; k_s = kk; n_s = ns; o_s = os; }
       }
+      int cand[kNbrCache];
+#pragma unroll
+      for (int s = 0; s < kNbrCache; ++s) {
+        cand[s] = 0;
+#pragma unroll
+        for (int j = 0; j < MAXP; ++j)
+          if (j == jsel) cand[s] = nbrc[j][s];
+        cand[s] = __shfl_sync(full, cand[s], base);
+      }
       if (l == 0) {
+#pragma unroll
+        for (int s = 0; s < kNbrCache; ++s) sh.nb[s] = cand[s];
         sh.sel = (wsel * 32 + base) * MAXP + jsel;
         sh.de_sel = de_s;
         sh.k_sel = k_s;
@@ -342,18 +410,8 @@ __device__ void advance_trajectory_cta(const KmcArgs& a, int64_t t, CtaShared& s
     if (ubase) ucur += 2;
 
     // ---- carrier sums after the move o_sel -> n_sel ----------------------
-#pragma unroll
-    for (int j = 0; j < MAXP; ++j) {
-      if (pc.valid[j] && pc.carrier[j] != c_sel) {
-        const int64_t rn = (int64_t)pc.newsite[j] * N, ro = (int64_t)pc.oldsite[j] * N;
-        pc.P[j] = dadd(pc.P[j], dsub(__ldg(A + rn + n_sel), __ldg(A + rn + o_sel)));
-        if (pc.firstq[j] || j == 0)
-          pc.Q[j] = dadd(pc.Q[j], dsub(__ldg(A + ro + n_sel), __ldg(A + ro + o_sel)));
-        else
-          pc.Q[j] = pc.Q[j > 0 ? j - 1 : 0];
-      }
-    }
-    bad = cta_rebuild_jobs<W>(sy, coef, w, l, occ, n_sel, sh);
+    bad = cta_update_sums<W, MAXP>(sy, coef, w, l, occ, c_sel, o_sel, n_sel,
+                                   use_nbc ? sh.nb : nullptr, pc, sh);
     if (__syncthreads_or(bad)) { status = PYCD_TRAJ_BAD_INDEX; break; }
 #pragma unroll
     for (int j = 0; j < MAXP; ++j) {
@@ -369,6 +427,11 @@ __device__ void advance_trajectory_cta(const KmcArgs& a, int64_t t, CtaShared& s
         pc.c0[j] = sh.jc0[s];
         pc.P[j] = sh.jp[s];
         pc.Q[j] = sh.jp[S];
+        // the new destination's neighbours, used when this process is next selected
+#pragma unroll
+        for (int u = 0; u < kNbrCache; ++u)
+          nbrc[j][u] = (use_nbc && u < S)
+                           ? __ldg(sy.d_nbr + (int64_t)pc.newsite[j] * S + u) : 0;
       }
     }
 
