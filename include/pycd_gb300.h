@@ -323,8 +323,9 @@ typedef struct PycdKmcLaunch {
  * The same device step function serves the one-trajectory (plain) form and
  * the batched form, so their event streams are identical.
  * Workspace: pycd_kmc_workspace_size(systems, n_systems) bytes; it holds the
- * device copy of the descriptors and per-slot rate coefficients derived from
- * lam, V_ab, the field shift, kT and vn.                                    */
+ * device copy of the descriptors, per-slot rate coefficients derived from
+ * lam, V_ab, the field shift, kT and vn, and per-slot constants derived from
+ * phi_bg, e_rel, A and the carrier charge (32 bytes per site and slot).    */
 PYCD_API int pycd_kmc_workspace_size(const PycdKmcSystem* systems,
                                      int32_t n_systems, size_t* bytes);
 

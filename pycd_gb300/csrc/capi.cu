@@ -48,7 +48,8 @@ int potential_sparse(const double* A, int64_t n, const int32_t* idx,
 using namespace pycd;
 
 // KMC workspace layout: a 256-byte header with the shape maxima, the device
-// descriptors (KmcSysDev), then one (c1, c0) coefficient array per system.
+// descriptors (KmcSysDev), one (c1, c0) coefficient array per system that
+// does not bring its own, then one slot-constant array per system.
 struct KmcTableHeader {
   int32_t n_systems;
   int32_t max_np;
@@ -68,9 +69,13 @@ static size_t kmc_coef_bytes(const PycdKmcSystem& s) {
                        : align256(sizeof(double2) * (size_t)s.n_sites * (size_t)s.n_slots);
 }
 
+static size_t kmc_slotc_bytes(const PycdKmcSystem& s) {
+  return align256(2 * sizeof(double2) * (size_t)s.n_sites * (size_t)s.n_slots);
+}
+
 static size_t kmc_ws_bytes(const PycdKmcSystem* systems, int32_t n_systems) {
   size_t b = kmc_table_bytes(n_systems);
-  for (int i = 0; i < n_systems; ++i) b += kmc_coef_bytes(systems[i]);
+  for (int i = 0; i < n_systems; ++i) b += kmc_coef_bytes(systems[i]) + kmc_slotc_bytes(systems[i]);
   return b;
 }
 
@@ -254,13 +259,18 @@ int pycd_kmc_upload_systems(const PycdKmcSystem* systems, int32_t n_systems,
     dev[i].coef = systems[i].d_rate_coef
                       ? (const double2*)systems[i].d_rate_coef
                       : (const double2*)(coef_base + off);
-    dev[i].pad = 0;
     off += kmc_coef_bytes(systems[i]);
+  }
+  for (int i = 0; i < n_systems; ++i) {
+    dev[i].slotc = (const double2*)(coef_base + off);
+    off += kmc_slotc_bytes(systems[i]);
   }
   cudaStream_t s = (cudaStream_t)stream;
   PYCD_CUDA(cudaMemcpyAsync(d_workspace, host.data(), host.size(),
                             cudaMemcpyHostToDevice, s));
   for (int i = 0; i < n_systems; ++i) {
+    rc = kmc_slotc_launch(systems[i], (double2*)dev[i].slotc, s);
+    if (rc) return rc;
     if (systems[i].d_rate_coef) continue;
     rc = kmc_coef_launch(systems[i], (double2*)dev[i].coef, s);
     if (rc) return rc;

@@ -7,7 +7,9 @@ ACM TOMS 15(2), 1989) for a table of 2^(j/256), as C source.
 * kInvL = 256/ln2 rounded to double;
 * kL1 = ln2/256 truncated to 34 significant bits, so that N * kL1 is exact
   for |N| < 2^19 (|x| < 745 gives |N| < 2.8e5); kL2 = ln2/256 - kL1 rounded;
-* 2^(j/256) = hi + lo, hi = RN(2^(j/256)), lo = RN(2^(j/256) - hi).
+* 2^(j/256) = hi + lo, hi = RN(2^(j/256)), lo = RN(2^(j/256) - hi); then
+  |lo| < ulp(hi)/2, so hi + lo rounds to hi in double (checked below; the
+  kernels rely on it).
 
 Values come from 200-bit arithmetic (mpmath).  Run:
     python pycd_gb300/csrc/exp_table.py > /tmp/table.inc
@@ -33,6 +35,7 @@ def main():
     print("// kInvL = %r, kL1 = %r, kL2 = %r" % (float(TB / ln2), float(L1), float(L - L1)))
     hi = [mp.mpf(float(mp.mpf(2) ** (mp.mpf(j) / TB))) for j in range(TB)]
     lo = [mp.mpf(2) ** (mp.mpf(j) / TB) - h for j, h in enumerate(hi)]
+    assert all(float(h) + float(l) == float(h) for h, l in zip(hi, lo))
     for name, vals in (("kExp2Hi", hi), ("kExp2Lo", lo)):
         print("static __device__ const unsigned long long %s[%d] = {" % (name, TB))
         for i in range(0, TB, 4):

@@ -20,6 +20,28 @@ __global__ void kmc_coef_kernel(const double* __restrict__ lam,
   coef[i] = make_double2(-1.0 / (4.0 * l * kT), v / kT + log(vn));
 }
 
+// Per-slot constants of the rate that change only with the slot's own site
+// (core.py:2004-2026, 2041), with n = nbr[o, s]:
+//   {phi_bg[n] - phi_bg[o], q (A[o,o] - A[o,n])}, {e_rel[n] - e_rel[o], lam},
+// the operations the step would do on every rebuild, done once per system.
+// A slot with an out-of-range neighbour gets zeros; the step stops on that
+// index before it uses them.
+__global__ void kmc_slotc_kernel(PycdKmcSystem s, double2* __restrict__ out) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t N = s.n_sites;
+  if (i >= N * s.n_slots) return;
+  const int64_t o = i / s.n_slots;
+  const int n = s.d_nbr[i];
+  double2 a = make_double2(0.0, 0.0), b = make_double2(0.0, s.d_lam[i]);
+  if (n >= 0 && n < N) {
+    a.x = dsub(s.d_phi_bg[n], s.d_phi_bg[o]);
+    a.y = dmul(s.carrier_charge, dsub(s.d_A[o * N + o], s.d_A[o * N + n]));
+    b.x = dsub(s.d_e_rel[n], s.d_e_rel[o]);
+  }
+  out[2 * i] = a;
+  out[2 * i + 1] = b;
+}
+
 __global__ void exp_probe_kernel(const double* __restrict__ x, int64_t n,
                                  double* __restrict__ ours,
                                  double* __restrict__ ref) {
@@ -168,6 +190,14 @@ int kmc_coef_launch(const PycdKmcSystem& s, double2* coef, cudaStream_t st) {
       s.d_lam, s.d_vab, s.d_field_shift, n, s.kT, s.vn, coef);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_fail(e, "kmc_coef_kernel", __FILE__, __LINE__);
+  return PYCD_OK;
+}
+
+int kmc_slotc_launch(const PycdKmcSystem& s, double2* slotc, cudaStream_t st) {
+  const int64_t n = s.n_sites * (int64_t)s.n_slots;
+  kmc_slotc_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(s, slotc);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(e, "kmc_slotc_kernel", __FILE__, __LINE__);
   return PYCD_OK;
 }
 

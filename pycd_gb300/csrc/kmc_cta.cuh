@@ -53,6 +53,7 @@ struct CtaShared {
 template <int W, int MAXP>
 __device__ __forceinline__ bool cta_update_sums(const PycdKmcSystem& sy,
                                                 const double2* __restrict__ coef,
+                                                const double2* __restrict__ slotc,
                                                 int w, int l, int occ, int c_sel,
                                                 int o_sel, int n_sel, const int* nbc,
                                                 ProcCache<MAXP>& pc, CtaShared& sh) {
@@ -61,7 +62,6 @@ __device__ __forceinline__ bool cta_update_sums(const PycdKmcSystem& sy,
   const int S = sy.n_slots;
   const int NC = sy.n_carriers;
   const double* __restrict__ A = sy.d_A;
-  const int64_t ro = (int64_t)n_sel * N;
   // incremental entries
   double an[MAXP], ao[MAXP], qn[MAXP], qo[MAXP];
   bool upd[MAXP], updq[MAXP];
@@ -100,17 +100,11 @@ __device__ __forceinline__ bool cta_update_sums(const PycdKmcSystem& sy,
     for (int u = 0; u < JW; ++u)
       if (u == l) n = row[u];
     const int64_t slot = (int64_t)n_sel * S + (cst ? ic : 0);
-    double2 cf = make_double2(0.0, 0.0);
-    double phn = 0.0, ph0 = 0.0, en = 0.0, e0 = 0.0, aoo = 0.0, aon = 0.0, lam = 0.0;
+    double2 cf = make_double2(0.0, 0.0), sa = cf, sb = cf;
     if (cst) {
       cf = __ldg(coef + slot);
-      phn = __ldg(sy.d_phi_bg + n);
-      ph0 = __ldg(sy.d_phi_bg + n_sel);
-      en = __ldg(sy.d_e_rel + n);
-      e0 = __ldg(sy.d_e_rel + n_sel);
-      aoo = __ldg(A + ro + n_sel);
-      aon = __ldg(A + ro + n);
-      lam = __ldg(sy.d_lam + slot);
+      sa = __ldg(slotc + 2 * slot);
+      sb = __ldg(slotc + 2 * slot + 1);
     }
     if (i0 == 0) {
 #pragma unroll
@@ -130,10 +124,10 @@ __device__ __forceinline__ bool cta_update_sums(const PycdKmcSystem& sy,
     }
     if (cst) {
       sh.jn[ic] = n;
-      sh.jdphi[ic] = dsub(phn, ph0);
-      sh.jt02q[ic] = dmul(sy.carrier_charge, dsub(aoo, aon));
-      sh.jde[ic] = dsub(en, e0);
-      sh.jlam[ic] = lam;
+      sh.jdphi[ic] = sa.x;
+      sh.jt02q[ic] = sa.y;
+      sh.jde[ic] = sb.x;
+      sh.jlam[ic] = sb.y;
       sh.jc1[ic] = cf.x;
       sh.jc0[ic] = cf.y;
     }
@@ -170,6 +164,7 @@ __device__ void advance_trajectory_cta(const KmcArgs& a, int64_t t, CtaShared& s
                       qbits >= 0x3f70000000000000LL && qbits <= 0x4070000000000000LL;
   const double* __restrict__ A = sy.d_A;
   const double2* __restrict__ coef = sd.coef;
+  const double2* __restrict__ slotc = sd.slotc;
   const double dt_grid = sy.time_interval;
   if (NP > L * MAXP || NC > 32 || S + 1 > kCtaMaxJobs ||
       (st.d_csum && 2 * NP > st.csum_stride)) {
@@ -218,7 +213,7 @@ __device__ void advance_trajectory_cta(const KmcArgs& a, int64_t t, CtaShared& s
   int64_t pre_base = -33;
 
   ProcCache<MAXP> pc;
-  bool bad = setup_processes<32, MAXP>(sy, coef, g, full, occ, pc);
+  bool bad = setup_processes<32, MAXP>(sy, coef, slotc, g, full, occ, pc);
   if (__syncthreads_or(bad)) {
     if (g == 0) st.d_status[t] = PYCD_TRAJ_BAD_INDEX;
     return;
@@ -410,7 +405,7 @@ __device__ void advance_trajectory_cta(const KmcArgs& a, int64_t t, CtaShared& s
     if (ubase) ucur += 2;
 
     // ---- carrier sums after the move o_sel -> n_sel ----------------------
-    bad = cta_update_sums<W, MAXP>(sy, coef, w, l, occ, c_sel, o_sel, n_sel,
+    bad = cta_update_sums<W, MAXP>(sy, coef, slotc, w, l, occ, c_sel, o_sel, n_sel,
                                    use_nbc ? sh.nb : nullptr, pc, sh);
     if (__syncthreads_or(bad)) { status = PYCD_TRAJ_BAD_INDEX; break; }
 #pragma unroll

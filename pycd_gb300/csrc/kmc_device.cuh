@@ -203,8 +203,9 @@ __device__ __forceinline__ double exp_tang_core(double x, int& m) {
   p = fma(dmul(p, r), r, r);
   const double shi = __longlong_as_double((long long)kExp2Hi[j]);
   const double slo = __longlong_as_double((long long)kExp2Lo[j]);
-  // 2^(j/256) (1 + p) = shi + (slo + (shi + slo) p)
-  return dadd(shi, fma(dadd(shi, slo), p, slo));
+  // 2^(j/256) (1 + p) = shi + (slo + (shi + slo) p), where shi + slo rounds
+  // to shi (|slo| < ulp(shi)/2 for every entry, by construction of the table)
+  return dadd(shi, fma(shi, p, slo));
 }
 
 static __device__ __noinline__ double exp_tang_wide(double x) {
@@ -277,6 +278,7 @@ struct ProcCache {
 template <int G, int MAXP>
 __device__ __forceinline__ bool setup_processes(const PycdKmcSystem& sy,
                                                 const double2* __restrict__ coef,
+                                                const double2* __restrict__ slotc,
                                                 int g, unsigned gmask, int occ,
                                                 ProcCache<MAXP>& pc) {
   const int64_t N = sy.n_sites;
@@ -303,11 +305,11 @@ __device__ __forceinline__ bool setup_processes(const PycdKmcSystem& sy,
         continue;
       }
       const int64_t slot = (int64_t)o * S + s;
-      pc.dphi[j] = dsub(__ldg(sy.d_phi_bg + n), __ldg(sy.d_phi_bg + o));
-      pc.t02q[j] = dmul(sy.carrier_charge,
-                        dsub(__ldg(A + (int64_t)o * N + o), __ldg(A + (int64_t)o * N + n)));
-      pc.de[j] = dsub(__ldg(sy.d_e_rel + n), __ldg(sy.d_e_rel + o));
-      pc.lam[j] = __ldg(sy.d_lam + slot);
+      const double2 sa = __ldg(slotc + 2 * slot), sb = __ldg(slotc + 2 * slot + 1);
+      pc.dphi[j] = sa.x;
+      pc.t02q[j] = sa.y;
+      pc.de[j] = sb.x;
+      pc.lam[j] = sb.y;
       const double2 cf = __ldg(coef + slot);
       pc.c1[j] = cf.x;
       pc.c0[j] = cf.y;
@@ -437,6 +439,7 @@ __device__ __forceinline__ double job_sums(unsigned gmask, int g, double (&v)[J]
 template <int G, int MAXP>
 __device__ __forceinline__ bool rebuild_moved_jb(const PycdKmcSystem& sy,
                                                  const double2* __restrict__ coef,
+                                                 const double2* __restrict__ slotc,
                                                  int g, unsigned gmask, int occ,
                                                  int c_sel, int n_sel,
                                                  ProcCache<MAXP>& pc) {
@@ -445,7 +448,6 @@ __device__ __forceinline__ bool rebuild_moved_jb(const PycdKmcSystem& sy,
   const int S = sy.n_slots;
   const int NC = sy.n_carriers;
   const double* __restrict__ A = sy.d_A;
-  const int64_t ro = (int64_t)n_sel * N;
   bool bad = false;
   for (int i0 = 0; i0 <= S; i0 += JB) {
     int row[JB];
@@ -471,10 +473,11 @@ __device__ __forceinline__ bool rebuild_moved_jb(const PycdKmcSystem& sy,
     double2 cf = make_double2(0.0, 0.0);
     if (g < JB && i0 + g < S) {
       const int64_t slot = (int64_t)n_sel * S + i0 + g;
-      dphi = dsub(__ldg(sy.d_phi_bg + n), __ldg(sy.d_phi_bg + n_sel));
-      t02q = dmul(sy.carrier_charge, dsub(__ldg(A + ro + n_sel), __ldg(A + ro + n)));
-      de = dsub(__ldg(sy.d_e_rel + n), __ldg(sy.d_e_rel + n_sel));
-      lam = __ldg(sy.d_lam + slot);
+      const double2 sa = __ldg(slotc + 2 * slot), sb = __ldg(slotc + 2 * slot + 1);
+      dphi = sa.x;
+      t02q = sa.y;
+      de = sb.x;
+      lam = sb.y;
       cf = __ldg(coef + slot);
     }
     // the carrier's Q is summed in the round that holds job S
@@ -532,6 +535,7 @@ __device__ __forceinline__ double carrier_row_tree(const double* __restrict__ rp
 template <int G, int MAXP>
 __device__ __forceinline__ bool rebuild_moved_direct(const PycdKmcSystem& sy,
                                               const double2* __restrict__ coef,
+                                              const double2* __restrict__ slotc,
                                               int g, unsigned gmask, int occ,
                                               int c_sel, int n_sel,
                                               ProcCache<MAXP>& pc) {
@@ -539,7 +543,6 @@ __device__ __forceinline__ bool rebuild_moved_direct(const PycdKmcSystem& sy,
   const int S = sy.n_slots;
   const int NC = sy.n_carriers;
   const double* __restrict__ A = sy.d_A;
-  const int64_t ro = (int64_t)n_sel * N;
   bool bad = false;
   for (int i0 = 0; i0 <= S; i0 += G) {
     const int i = i0 + g;
@@ -555,10 +558,11 @@ __device__ __forceinline__ bool rebuild_moved_direct(const PycdKmcSystem& sy,
         bad = true;
         act = false;
       } else {
-        dphi = dsub(__ldg(sy.d_phi_bg + n), __ldg(sy.d_phi_bg + n_sel));
-        t02q = dmul(sy.carrier_charge, dsub(__ldg(A + ro + n_sel), __ldg(A + ro + n)));
-        de = dsub(__ldg(sy.d_e_rel + n), __ldg(sy.d_e_rel + n_sel));
-        lam = __ldg(sy.d_lam + slot);
+        const double2 sa = __ldg(slotc + 2 * slot), sb = __ldg(slotc + 2 * slot + 1);
+        dphi = sa.x;
+        t02q = sa.y;
+        de = sb.x;
+        lam = sb.y;
         cf = __ldg(coef + slot);
       }
     }
@@ -606,15 +610,16 @@ __device__ __forceinline__ bool rebuild_moved_direct(const PycdKmcSystem& sy,
 template <int G, int MAXP>
 __device__ __forceinline__ bool rebuild_moved(const PycdKmcSystem& sy,
                                               const double2* __restrict__ coef,
+                                              const double2* __restrict__ slotc,
                                               int g, unsigned gmask, int occ,
                                               int c_sel, int n_sel,
                                               ProcCache<MAXP>& pc) {
   if constexpr (G < 16) {
-    return rebuild_moved_direct<G, MAXP>(sy, coef, g, gmask, occ, c_sel, n_sel, pc);
+    return rebuild_moved_direct<G, MAXP>(sy, coef, slotc, g, gmask, occ, c_sel, n_sel, pc);
   } else {
     if (sy.n_carriers <= 8)
-      return rebuild_moved_direct<G, MAXP>(sy, coef, g, gmask, occ, c_sel, n_sel, pc);
-    return rebuild_moved_jb<G, MAXP>(sy, coef, g, gmask, occ, c_sel, n_sel, pc);
+      return rebuild_moved_direct<G, MAXP>(sy, coef, slotc, g, gmask, occ, c_sel, n_sel, pc);
+    return rebuild_moved_jb<G, MAXP>(sy, coef, slotc, g, gmask, occ, c_sel, n_sel, pc);
   }
 }
 
@@ -745,6 +750,7 @@ __device__ void advance_trajectory(const KmcArgs& a, int64_t t, int g,
                       qbits >= 0x3f70000000000000LL && qbits <= 0x4070000000000000LL;
   const double* __restrict__ A = sy.d_A;
   const double2* __restrict__ coef = sd.coef;
+  const double2* __restrict__ slotc = sd.slotc;
   const double dt_grid = sy.time_interval;
   if (NP > G * MAXP || NC > G || (st.d_csum && 2 * NP > st.csum_stride)) {
     // launch shape or carrier-sum storage too small for this system
@@ -799,7 +805,7 @@ __device__ void advance_trajectory(const KmcArgs& a, int64_t t, int g,
 
   // ---- process cache: geometry, constants, carrier sums ----------------
   ProcCache<MAXP> pc;
-  bool bad = setup_processes<G, MAXP>(sy, coef, g, gmask, occ, pc);
+  bool bad = setup_processes<G, MAXP>(sy, coef, slotc, g, gmask, occ, pc);
   if (__ballot_sync(gmask, bad) & gmask) {
     if (g == 0) st.d_status[t] = PYCD_TRAJ_BAD_INDEX;
     return;
@@ -965,7 +971,7 @@ __device__ void advance_trajectory(const KmcArgs& a, int64_t t, int g,
           pc.Q[j] = pc.Q[j > 0 ? j - 1 : 0];
       }
     }
-    bad = rebuild_moved<G, MAXP>(sy, coef, g, gmask, occ, c_sel, n_sel, pc);
+    bad = rebuild_moved<G, MAXP>(sy, coef, slotc, g, gmask, occ, c_sel, n_sel, pc);
     if (__ballot_sync(gmask, bad) & gmask) { status = PYCD_TRAJ_BAD_INDEX; break; }
 
     // ---- path-grid rows (core.py:2847-2861) ---------------------------
