@@ -22,21 +22,25 @@ __global__ void kmc_coef_kernel(const double* __restrict__ lam,
 
 // Per-slot constants of the rate that change only with the slot's own site
 // (core.py:2004-2026, 2041), with n = nbr[o, s]:
-//   {phi_bg[n] - phi_bg[o], q (A[o,o] - A[o,n])}, {e_rel[n] - e_rel[o], lam},
-// the operations the step would do on every rebuild, done once per system.
-// A slot with an out-of-range neighbour gets zeros; the step stops on that
-// index before it uses them.
+//   cq = (phi_bg[n] - phi_bg[o]) + q (A[o,o] - A[o,n]),
+//   dl = (e_rel[n] - e_rel[o]) + lam,   de = e_rel[n] - e_rel[o],
+// stored as {cq, dl}, {de, lam} and computed once per system.  A slot with
+// an out-of-range neighbour gets zeros; the step stops on that index before
+// it uses them.
 __global__ void kmc_slotc_kernel(PycdKmcSystem s, double2* __restrict__ out) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int64_t N = s.n_sites;
   if (i >= N * s.n_slots) return;
   const int64_t o = i / s.n_slots;
   const int n = s.d_nbr[i];
-  double2 a = make_double2(0.0, 0.0), b = make_double2(0.0, s.d_lam[i]);
+  const double lam = s.d_lam[i];
+  double2 a = make_double2(0.0, 0.0), b = make_double2(0.0, lam);
   if (n >= 0 && n < N) {
-    a.x = dsub(s.d_phi_bg[n], s.d_phi_bg[o]);
-    a.y = dmul(s.carrier_charge, dsub(s.d_A[o * N + o], s.d_A[o * N + n]));
-    b.x = dsub(s.d_e_rel[n], s.d_e_rel[o]);
+    const double dphi = dsub(s.d_phi_bg[n], s.d_phi_bg[o]);
+    const double t02q = dmul(s.carrier_charge, dsub(s.d_A[o * N + o], s.d_A[o * N + n]));
+    const double de = dsub(s.d_e_rel[n], s.d_e_rel[o]);
+    a = make_double2(dadd(dphi, t02q), dadd(de, lam));
+    b.x = de;
   }
   out[2 * i] = a;
   out[2 * i + 1] = b;

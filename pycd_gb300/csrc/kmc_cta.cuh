@@ -35,8 +35,8 @@ struct CtaShared {
   int sel, n_sel, o_sel, pad;
   int nb[kNbrCache];  // neighbours of n_sel (from the selected process' cache)
   // rebuilt processes of the moved carrier: job i < S is slot i, job S its Q
-  double jp[kCtaMaxJobs], jdphi[kCtaMaxJobs], jt02q[kCtaMaxJobs], jde[kCtaMaxJobs];
-  double jlam[kCtaMaxJobs], jc1[kCtaMaxJobs], jc0[kCtaMaxJobs];
+  double jp[kCtaMaxJobs], jcq[kCtaMaxJobs], jdl[kCtaMaxJobs], jde[kCtaMaxJobs];
+  double jc1[kCtaMaxJobs], jc0[kCtaMaxJobs];
   int jn[kCtaMaxJobs];
 };
 
@@ -124,10 +124,9 @@ __device__ __forceinline__ bool cta_update_sums(const PycdKmcSystem& sy,
     }
     if (cst) {
       sh.jn[ic] = n;
-      sh.jdphi[ic] = sa.x;
-      sh.jt02q[ic] = sa.y;
+      sh.jcq[ic] = sa.x;
+      sh.jdl[ic] = sa.y;
       sh.jde[ic] = sb.x;
-      sh.jlam[ic] = sb.y;
       sh.jc1[ic] = cf.x;
       sh.jc0[ic] = cf.y;
     }
@@ -159,9 +158,6 @@ __device__ void advance_trajectory_cta(const KmcArgs& a, int64_t t, CtaShared& s
   const int MC = st.max_carriers;
   const double q = sy.carrier_charge;
   const double two_q = dmul(2.0, q);
-  const long long qbits = __double_as_longlong(q) & 0x7fffffffffffffffLL;
-  const bool q_pow2 = (qbits & 0x000fffffffffffffLL) == 0 &&
-                      qbits >= 0x3f70000000000000LL && qbits <= 0x4070000000000000LL;
   const double* __restrict__ A = sy.d_A;
   const double2* __restrict__ coef = sd.coef;
   const double2* __restrict__ slotc = sd.slotc;
@@ -264,11 +260,8 @@ __device__ void advance_trajectory_cta(const KmcArgs& a, int64_t t, CtaShared& s
     if (it > 0 && (step & (R - 1)) == 0) fresh_sums<32, MAXP>(sy, g, full, occ, pc);
 
     // ---- rates ----------------------------------------------------------
-    double kp[MAXP], dE[MAXP];
-    if (q_pow2)
-      process_rates<MAXP, true>(pc, q, two_q, kp, dE);
-    else
-      process_rates<MAXP, false>(pc, q, two_q, kp, dE);
+    double kp[MAXP], term[MAXP];
+    process_rates<MAXP>(pc, q, two_q, kp, term);
 
     // ---- tree: lane, warp, then the W warp totals -----------------------
     LocalTree<MAXP> lt;
@@ -327,16 +320,18 @@ __device__ void advance_trajectory_cta(const KmcArgs& a, int64_t t, CtaShared& s
         if (!nonneg_gt(s, thr)) { acc = s; node = 2 * node + 1; } else { node = 2 * node; }
       }
       const int jsel = node - MAXP;
-      double de_s = 0.0, k_s = 0.0;
+      double term_s = 0.0, dslot_s = 0.0, k_s = 0.0;
       int n_s = 0, o_s = 0;
 #pragma unroll
       for (int j = 0; j < MAXP; ++j) {
-        const double d = __shfl_sync(full, dE[j], base);
+        const double d = __shfl_sync(full, term[j], base);
+        const double e = __shfl_sync(full, pc.de[j], base);
         const double kk = __shfl_sync(full, kp[j], base);
         const int ns = __shfl_sync(full, pc.newsite[j], base);
         const int os = __shfl_sync(full, pc.oldsite[j], base);
-        if (j == jsel) { de_s = d; k_s = kk; n_s = ns; o_s = os; }
+        if (j == jsel) { term_s = d; dslot_s = e; k_s = kk; n_s = ns; o_s = os; }
       }
+      const double de_s = fma(two_q, term_s, dslot_s);  // dE0 of the event
       int cand[kNbrCache];
 #pragma unroll
       for (int s = 0; s < kNbrCache; ++s) {
@@ -414,10 +409,9 @@ __device__ void advance_trajectory_cta(const KmcArgs& a, int64_t t, CtaShared& s
         const int s = g * MAXP + j - c_sel * S;
         pc.oldsite[j] = n_sel;
         pc.newsite[j] = sh.jn[s];
-        pc.dphi[j] = sh.jdphi[s];
-        pc.t02q[j] = sh.jt02q[s];
+        pc.cq[j] = sh.jcq[s];
+        pc.dl[j] = sh.jdl[s];
         pc.de[j] = sh.jde[s];
-        pc.lam[j] = sh.jlam[s];
         pc.c1[j] = sh.jc1[s];
         pc.c0[j] = sh.jc0[s];
         pc.P[j] = sh.jp[s];

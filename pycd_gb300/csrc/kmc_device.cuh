@@ -18,6 +18,10 @@
 //           term02 = q (A[o,o] - A[o,n])
 //   rate  = exp(c1 (lam + dE0)^2 + c0),  c1 = -1/(4 lam kT),
 //           c0 = (V_ab + shift)/kT + ln vn   (= vn exp(-dG/kT), core.py:2045-2047)
+//   associated as term = q (P - Q) + cq and lam + dE0 = 2q term + dl, with
+//   the per-slot constants cq = (phi_bg[n] - phi_bg[o]) + term02 and
+//   dl = (E_rel[n] - E_rel[o]) + lam computed once per system: five FP64
+//   instructions per process before the exponential.
 //   The carrier sums in term01 are balanced binary trees over the carrier
 //   index, kept incrementally between exact refreshes.
 //   k_tot and every cumulative rate are sums over a fixed balanced binary
@@ -261,13 +265,13 @@ struct LocalTree {
 };
 
 // Per-process cache of one lane: geometry, constants that change only when
-// the process' own carrier moves, and the two carrier-potential sums.
-// t02q = q (A[o,o] - A[o,n]); firstq marks the first of the lane's processes
-// of a carrier (the one that evaluates the carrier's Q).
+// the process' own carrier moves (the slot constants cq, dl, de, c1, c0),
+// and the two carrier-potential sums.  firstq marks the first of the lane's
+// processes of a carrier (the one that evaluates the carrier's Q).
 template <int MAXP>
 struct ProcCache {
   int oldsite[MAXP], newsite[MAXP], carrier[MAXP];
-  double dphi[MAXP], t02q[MAXP], de[MAXP], lam[MAXP], c1[MAXP], c0[MAXP];
+  double cq[MAXP], dl[MAXP], de[MAXP], c1[MAXP], c0[MAXP];
   double P[MAXP], Q[MAXP];
   bool valid[MAXP], firstq[MAXP];
 };
@@ -306,10 +310,9 @@ __device__ __forceinline__ bool setup_processes(const PycdKmcSystem& sy,
       }
       const int64_t slot = (int64_t)o * S + s;
       const double2 sa = __ldg(slotc + 2 * slot), sb = __ldg(slotc + 2 * slot + 1);
-      pc.dphi[j] = sa.x;
-      pc.t02q[j] = sa.y;
+      pc.cq[j] = sa.x;
+      pc.dl[j] = sa.y;
       pc.de[j] = sb.x;
-      pc.lam[j] = sb.y;
       const double2 cf = __ldg(coef + slot);
       pc.c1[j] = cf.x;
       pc.c0[j] = cf.y;
@@ -469,15 +472,14 @@ __device__ __forceinline__ bool rebuild_moved_jb(const PycdKmcSystem& sy,
 #pragma unroll
     for (int u = 0; u < JB; ++u)
       if (g == u) n = row[u];
-    double dphi = 0.0, t02q = 0.0, de = 0.0, lam = 0.0;
+    double cq = 0.0, dl = 0.0, de = 0.0;
     double2 cf = make_double2(0.0, 0.0);
     if (g < JB && i0 + g < S) {
       const int64_t slot = (int64_t)n_sel * S + i0 + g;
       const double2 sa = __ldg(slotc + 2 * slot), sb = __ldg(slotc + 2 * slot + 1);
-      dphi = sa.x;
-      t02q = sa.y;
+      cq = sa.x;
+      dl = sa.y;
       de = sb.x;
-      lam = sb.y;
       cf = __ldg(coef + slot);
     }
     // the carrier's Q is summed in the round that holds job S
@@ -491,20 +493,18 @@ __device__ __forceinline__ bool rebuild_moved_jb(const PycdKmcSystem& sy,
       const bool take = mine && src >= 0 && src < JB;
       const int sl = take ? src : 0;
       const int nn = gshfl<G>(gmask, n, sl);
-      const double v_dphi = gshfl<G>(gmask, dphi, sl);
-      const double v_t02q = gshfl<G>(gmask, t02q, sl);
+      const double v_cq = gshfl<G>(gmask, cq, sl);
+      const double v_dl = gshfl<G>(gmask, dl, sl);
       const double v_de = gshfl<G>(gmask, de, sl);
-      const double v_lam = gshfl<G>(gmask, lam, sl);
       const double v_c1 = gshfl<G>(gmask, cf.x, sl);
       const double v_c0 = gshfl<G>(gmask, cf.y, sl);
       const double v_p = gshfl<G>(gmask, sum, job_lane<JB>(sl));
       if (take) {
         pc.oldsite[j] = n_sel;
         pc.newsite[j] = nn;
-        pc.dphi[j] = v_dphi;
-        pc.t02q[j] = v_t02q;
+        pc.cq[j] = v_cq;
+        pc.dl[j] = v_dl;
         pc.de[j] = v_de;
-        pc.lam[j] = v_lam;
         pc.c1[j] = v_c1;
         pc.c0[j] = v_c0;
         pc.P[j] = v_p;
@@ -548,7 +548,7 @@ __device__ __forceinline__ bool rebuild_moved_direct(const PycdKmcSystem& sy,
     const int i = i0 + g;
     const bool is_slot = i < S;
     int n = n_sel;
-    double dphi = 0.0, t02q = 0.0, de = 0.0, lam = 0.0;
+    double cq = 0.0, dl = 0.0, de = 0.0;
     double2 cf = make_double2(0.0, 0.0);
     bool act = i <= S;
     if (is_slot) {
@@ -559,10 +559,9 @@ __device__ __forceinline__ bool rebuild_moved_direct(const PycdKmcSystem& sy,
         act = false;
       } else {
         const double2 sa = __ldg(slotc + 2 * slot), sb = __ldg(slotc + 2 * slot + 1);
-        dphi = sa.x;
-        t02q = sa.y;
+        cq = sa.x;
+        dl = sa.y;
         de = sb.x;
-        lam = sb.y;
         cf = __ldg(coef + slot);
       }
     }
@@ -580,20 +579,18 @@ __device__ __forceinline__ bool rebuild_moved_direct(const PycdKmcSystem& sy,
       const bool take = mine && src >= 0 && src < G;
       const int sl = take ? src : 0;
       const int nn = gshfl<G>(gmask, n, sl);
-      const double v_dphi = gshfl<G>(gmask, dphi, sl);
-      const double v_t02q = gshfl<G>(gmask, t02q, sl);
+      const double v_cq = gshfl<G>(gmask, cq, sl);
+      const double v_dl = gshfl<G>(gmask, dl, sl);
       const double v_de = gshfl<G>(gmask, de, sl);
-      const double v_lam = gshfl<G>(gmask, lam, sl);
       const double v_c1 = gshfl<G>(gmask, cf.x, sl);
       const double v_c0 = gshfl<G>(gmask, cf.y, sl);
       const double v_p = gshfl<G>(gmask, sum, sl);
       if (take) {
         pc.oldsite[j] = n_sel;
         pc.newsite[j] = nn;
-        pc.dphi[j] = v_dphi;
-        pc.t02q[j] = v_t02q;
+        pc.cq[j] = v_cq;
+        pc.dl[j] = v_dl;
         pc.de[j] = v_de;
-        pc.lam[j] = v_lam;
         pc.c1[j] = v_c1;
         pc.c0[j] = v_c0;
         pc.P[j] = v_p;
@@ -624,29 +621,19 @@ __device__ __forceinline__ bool rebuild_moved(const PycdKmcSystem& sy,
 }
 
 // Rates of this lane's processes (core.py:1989-2050):
-//   dE0 = 2q ((dphi + q (P - Q)) + q t02) + de,  k = exp(c1 (lam + dE0)^2 + c0).
-// QPOW2: |q| is a power of two, so q y and 2q y are exact and
-// add(d, mul(q, y)) == fma(q, y, d): the same doubles with two FP64
-// instructions fewer per process.
-template <int MAXP, bool QPOW2>
+//   term = q (P - Q) + cq,   x = lam + dE0 = 2q term + dl,
+//   k = exp(c1 x^2 + c0),    dE0 = 2q term + de (for the selected process).
+template <int MAXP>
 __device__ __forceinline__ void process_rates(const ProcCache<MAXP>& pc, double q,
                                               double two_q, double (&kp)[MAXP],
-                                              double (&dE)[MAXP]) {
+                                              double (&term)[MAXP]) {
 #pragma unroll
   for (int j = 0; j < MAXP; ++j) {
     kp[j] = 0.0;
-    dE[j] = 0.0;
+    term[j] = 0.0;
     if (pc.valid[j]) {
-      double de0;
-      if (QPOW2) {
-        const double term01 = fma(q, dsub(pc.P[j], pc.Q[j]), pc.dphi[j]);
-        de0 = fma(two_q, dadd(term01, pc.t02q[j]), pc.de[j]);
-      } else {
-        const double term01 = dadd(pc.dphi[j], dmul(q, dsub(pc.P[j], pc.Q[j])));
-        de0 = dadd(dmul(two_q, dadd(term01, pc.t02q[j])), pc.de[j]);
-      }
-      const double x = dadd(pc.lam[j], de0);
-      dE[j] = de0;
+      term[j] = fma(q, dsub(pc.P[j], pc.Q[j]), pc.cq[j]);
+      const double x = fma(two_q, term[j], pc.dl[j]);
       kp[j] = exp_tang(fma(dmul(x, x), pc.c1[j], pc.c0[j]));
     }
   }
@@ -743,11 +730,6 @@ __device__ void advance_trajectory(const KmcArgs& a, int64_t t, int g,
   const int MC = st.max_carriers;
   const double q = sy.carrier_charge;
   const double two_q = dmul(2.0, q);
-  // |q| = 2^k with |k| <= 8 (full and partial carrier charges): products by
-  // q and 2q of the potentials (|y| >> 2^-1000) are exact
-  const long long qbits = __double_as_longlong(q) & 0x7fffffffffffffffLL;
-  const bool q_pow2 = (qbits & 0x000fffffffffffffLL) == 0 &&
-                      qbits >= 0x3f70000000000000LL && qbits <= 0x4070000000000000LL;
   const double* __restrict__ A = sy.d_A;
   const double2* __restrict__ coef = sd.coef;
   const double2* __restrict__ slotc = sd.slotc;
@@ -848,11 +830,8 @@ __device__ void advance_trajectory(const KmcArgs& a, int64_t t, int g,
     if (it > 0 && (step & (R - 1)) == 0) fresh_sums<G, MAXP>(sy, g, gmask, occ, pc);
 
     // ---- rates (core.py:1989-2050) ------------------------------------
-    double kp[MAXP], dE[MAXP];
-    if (q_pow2)
-      process_rates<MAXP, true>(pc, q, two_q, kp, dE);
-    else
-      process_rates<MAXP, false>(pc, q, two_q, kp, dE);
+    double kp[MAXP], term[MAXP];
+    process_rates<MAXP>(pc, q, two_q, kp, term);
 
     // ---- selection (core.py:2796-2800) on the balanced tree ------------
     LocalTree<MAXP> lt;
@@ -911,16 +890,18 @@ __device__ void advance_trajectory(const KmcArgs& a, int64_t t, int g,
     }
 
     // broadcast the selected process' data from its owner lane
-    double de_sel = 0.0, k_sel = 0.0;
+    double term_sel = 0.0, de_slot = 0.0, k_sel = 0.0;
     int n_sel = 0, o_sel = 0;
 #pragma unroll
     for (int j = 0; j < MAXP; ++j) {
-      const double d = gshfl<G>(gmask, dE[j], base);
+      const double d = gshfl<G>(gmask, term[j], base);
+      const double e = gshfl<G>(gmask, pc.de[j], base);
       const double kk = gshfl<G>(gmask, kp[j], base);
       const int ns = gshfl<G>(gmask, pc.newsite[j], base);
       const int os = gshfl<G>(gmask, pc.oldsite[j], base);
-      if (j == jsel) { de_sel = d; k_sel = kk; n_sel = ns; o_sel = os; }
+      if (j == jsel) { term_sel = d; de_slot = e; k_sel = kk; n_sel = ns; o_sel = os; }
     }
+    const double de_sel = fma(two_q, term_sel, de_slot);  // dE0 of the event
     const int c_sel = sel / S, s_sel = sel - c_sel * S;
 
     // delG0 grid rows [start, end) (core.py:2807-2809)
