@@ -269,10 +269,11 @@ int pycd_kmc_upload_systems(const PycdKmcSystem* systems, int32_t n_systems,
   PYCD_CUDA(cudaMemcpyAsync(d_workspace, host.data(), host.size(),
                             cudaMemcpyHostToDevice, s));
   for (int i = 0; i < n_systems; ++i) {
-    rc = kmc_slotc_launch(systems[i], (double2*)dev[i].slotc, s);
-    if (rc) return rc;
-    if (systems[i].d_rate_coef) continue;
-    rc = kmc_coef_launch(systems[i], (double2*)dev[i].coef, s);
+    if (!systems[i].d_rate_coef) {
+      rc = kmc_coef_launch(systems[i], (double2*)dev[i].coef, s);
+      if (rc) return rc;
+    }
+    rc = kmc_slotc_launch(systems[i], dev[i].coef, (double2*)dev[i].slotc, s);
     if (rc) return rc;
   }
   PYCD_CUDA(cudaStreamSynchronize(s));

@@ -21,26 +21,30 @@ __global__ void kmc_coef_kernel(const double* __restrict__ lam,
 }
 
 // Per-slot constants of the rate that change only with the slot's own site
-// (core.py:2004-2026, 2041), with n = nbr[o, s]:
+// (core.py:2004-2026, 2041-2047), with n = nbr[o, s] and the slot's
+// exponent coefficients (c1, c0) = coef[slot]:
 //   cq = (phi_bg[n] - phi_bg[o]) + q (A[o,o] - A[o,n]),
-//   dl = (e_rel[n] - e_rel[o]) + lam,   de = e_rel[n] - e_rel[o],
-// stored as {cq, dl}, {de, lam} and computed once per system.  A slot with
-// an out-of-range neighbour gets zeros; the step stops on that index before
-// it uses them.
-__global__ void kmc_slotc_kernel(PycdKmcSystem s, double2* __restrict__ out) {
+//   de = e_rel[n] - e_rel[o],   w = sqrt(-c1),
+//   xa = 2q w,   xb = (de + lam) w,
+// stored as {cq, xb}, {de, xa} and computed once per system.  The step then
+// forms x' = w (lam + dE0) = xa term + xb and c1 (lam + dE0)^2 + c0 =
+// c0 - x'^2.  A slot with an out-of-range neighbour gets zeros; the step
+// stops on that index before it uses them.
+__global__ void kmc_slotc_kernel(PycdKmcSystem s, const double2* __restrict__ coef,
+                                 double2* __restrict__ out) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int64_t N = s.n_sites;
   if (i >= N * s.n_slots) return;
   const int64_t o = i / s.n_slots;
   const int n = s.d_nbr[i];
-  const double lam = s.d_lam[i];
-  double2 a = make_double2(0.0, 0.0), b = make_double2(0.0, lam);
+  double2 a = make_double2(0.0, 0.0), b = make_double2(0.0, 0.0);
   if (n >= 0 && n < N) {
+    const double w = __dsqrt_rn(-coef[i].x);
     const double dphi = dsub(s.d_phi_bg[n], s.d_phi_bg[o]);
     const double t02q = dmul(s.carrier_charge, dsub(s.d_A[o * N + o], s.d_A[o * N + n]));
     const double de = dsub(s.d_e_rel[n], s.d_e_rel[o]);
-    a = make_double2(dadd(dphi, t02q), dadd(de, lam));
-    b.x = de;
+    a = make_double2(dadd(dphi, t02q), dmul(dadd(de, s.d_lam[i]), w));
+    b = make_double2(de, dmul(dmul(2.0, s.carrier_charge), w));
   }
   out[2 * i] = a;
   out[2 * i + 1] = b;
@@ -197,9 +201,10 @@ int kmc_coef_launch(const PycdKmcSystem& s, double2* coef, cudaStream_t st) {
   return PYCD_OK;
 }
 
-int kmc_slotc_launch(const PycdKmcSystem& s, double2* slotc, cudaStream_t st) {
+int kmc_slotc_launch(const PycdKmcSystem& s, const double2* coef, double2* slotc,
+                     cudaStream_t st) {
   const int64_t n = s.n_sites * (int64_t)s.n_slots;
-  kmc_slotc_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(s, slotc);
+  kmc_slotc_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(s, coef, slotc);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_fail(e, "kmc_slotc_kernel", __FILE__, __LINE__);
   return PYCD_OK;

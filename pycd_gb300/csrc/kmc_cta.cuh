@@ -35,8 +35,8 @@ struct CtaShared {
   int sel, n_sel, o_sel, pad;
   int nb[kNbrCache];  // neighbours of n_sel (from the selected process' cache)
   // rebuilt processes of the moved carrier: job i < S is slot i, job S its Q
-  double jp[kCtaMaxJobs], jcq[kCtaMaxJobs], jdl[kCtaMaxJobs], jde[kCtaMaxJobs];
-  double jc1[kCtaMaxJobs], jc0[kCtaMaxJobs];
+  double jp[kCtaMaxJobs], jcq[kCtaMaxJobs], jxb[kCtaMaxJobs], jde[kCtaMaxJobs];
+  double jxa[kCtaMaxJobs], jc0[kCtaMaxJobs];
   int jn[kCtaMaxJobs];
 };
 
@@ -125,9 +125,9 @@ __device__ __forceinline__ bool cta_update_sums(const PycdKmcSystem& sy,
     if (cst) {
       sh.jn[ic] = n;
       sh.jcq[ic] = sa.x;
-      sh.jdl[ic] = sa.y;
+      sh.jxb[ic] = sa.y;
       sh.jde[ic] = sb.x;
-      sh.jc1[ic] = cf.x;
+      sh.jxa[ic] = sb.y;
       sh.jc0[ic] = cf.y;
     }
   }
@@ -410,9 +410,9 @@ __device__ void advance_trajectory_cta(const KmcArgs& a, int64_t t, CtaShared& s
         pc.oldsite[j] = n_sel;
         pc.newsite[j] = sh.jn[s];
         pc.cq[j] = sh.jcq[s];
-        pc.dl[j] = sh.jdl[s];
+        pc.xb[j] = sh.jxb[s];
         pc.de[j] = sh.jde[s];
-        pc.c1[j] = sh.jc1[s];
+        pc.xa[j] = sh.jxa[s];
         pc.c0[j] = sh.jc0[s];
         pc.P[j] = sh.jp[s];
         pc.Q[j] = sh.jp[S];

@@ -18,10 +18,12 @@
 //           term02 = q (A[o,o] - A[o,n])
 //   rate  = exp(c1 (lam + dE0)^2 + c0),  c1 = -1/(4 lam kT),
 //           c0 = (V_ab + shift)/kT + ln vn   (= vn exp(-dG/kT), core.py:2045-2047)
-//   associated as term = q (P - Q) + cq and lam + dE0 = 2q term + dl, with
-//   the per-slot constants cq = (phi_bg[n] - phi_bg[o]) + term02 and
-//   dl = (E_rel[n] - E_rel[o]) + lam computed once per system: five FP64
-//   instructions per process before the exponential.
+//   associated as term = q (P - Q) + cq and sqrt(-c1) (lam + dE0) =
+//   xa term + xb, with per-slot constants cq = (phi_bg[n] - phi_bg[o]) +
+//   term02, xa = 2q sqrt(-c1) and xb = ((E_rel[n] - E_rel[o]) + lam) sqrt(-c1)
+//   computed once per system: four FP64 instructions per process before the
+//   exponential (the rates move by ~1e-15 relative, as any association of
+//   the reference's np.dot does).
 //   The carrier sums in term01 are balanced binary trees over the carrier
 //   index, kept incrementally between exact refreshes.
 //   k_tot and every cumulative rate are sums over a fixed balanced binary
@@ -265,13 +267,13 @@ struct LocalTree {
 };
 
 // Per-process cache of one lane: geometry, constants that change only when
-// the process' own carrier moves (the slot constants cq, dl, de, c1, c0),
+// the process' own carrier moves (the slot constants cq, xa, xb, de, c0),
 // and the two carrier-potential sums.  firstq marks the first of the lane's
 // processes of a carrier (the one that evaluates the carrier's Q).
 template <int MAXP>
 struct ProcCache {
   int oldsite[MAXP], newsite[MAXP], carrier[MAXP];
-  double cq[MAXP], dl[MAXP], de[MAXP], c1[MAXP], c0[MAXP];
+  double cq[MAXP], xa[MAXP], xb[MAXP], de[MAXP], c0[MAXP];
   double P[MAXP], Q[MAXP];
   bool valid[MAXP], firstq[MAXP];
 };
@@ -311,11 +313,10 @@ __device__ __forceinline__ bool setup_processes(const PycdKmcSystem& sy,
       const int64_t slot = (int64_t)o * S + s;
       const double2 sa = __ldg(slotc + 2 * slot), sb = __ldg(slotc + 2 * slot + 1);
       pc.cq[j] = sa.x;
-      pc.dl[j] = sa.y;
+      pc.xb[j] = sa.y;
       pc.de[j] = sb.x;
-      const double2 cf = __ldg(coef + slot);
-      pc.c1[j] = cf.x;
-      pc.c0[j] = cf.y;
+      pc.xa[j] = sb.y;
+      pc.c0[j] = __ldg(coef + slot).y;
     } else {
       pc.carrier[j] = -1;
       pc.oldsite[j] = 0;
@@ -472,15 +473,15 @@ __device__ __forceinline__ bool rebuild_moved_jb(const PycdKmcSystem& sy,
 #pragma unroll
     for (int u = 0; u < JB; ++u)
       if (g == u) n = row[u];
-    double cq = 0.0, dl = 0.0, de = 0.0;
-    double2 cf = make_double2(0.0, 0.0);
+    double cq = 0.0, xb = 0.0, de = 0.0, xa = 0.0, c0 = 0.0;
     if (g < JB && i0 + g < S) {
       const int64_t slot = (int64_t)n_sel * S + i0 + g;
       const double2 sa = __ldg(slotc + 2 * slot), sb = __ldg(slotc + 2 * slot + 1);
       cq = sa.x;
-      dl = sa.y;
+      xb = sa.y;
       de = sb.x;
-      cf = __ldg(coef + slot);
+      xa = sb.y;
+      c0 = __ldg(coef + slot).y;
     }
     // the carrier's Q is summed in the round that holds job S
     const int qsrc = S - i0;
@@ -494,18 +495,18 @@ __device__ __forceinline__ bool rebuild_moved_jb(const PycdKmcSystem& sy,
       const int sl = take ? src : 0;
       const int nn = gshfl<G>(gmask, n, sl);
       const double v_cq = gshfl<G>(gmask, cq, sl);
-      const double v_dl = gshfl<G>(gmask, dl, sl);
+      const double v_xb = gshfl<G>(gmask, xb, sl);
       const double v_de = gshfl<G>(gmask, de, sl);
-      const double v_c1 = gshfl<G>(gmask, cf.x, sl);
-      const double v_c0 = gshfl<G>(gmask, cf.y, sl);
+      const double v_xa = gshfl<G>(gmask, xa, sl);
+      const double v_c0 = gshfl<G>(gmask, c0, sl);
       const double v_p = gshfl<G>(gmask, sum, job_lane<JB>(sl));
       if (take) {
         pc.oldsite[j] = n_sel;
         pc.newsite[j] = nn;
         pc.cq[j] = v_cq;
-        pc.dl[j] = v_dl;
+        pc.xb[j] = v_xb;
         pc.de[j] = v_de;
-        pc.c1[j] = v_c1;
+        pc.xa[j] = v_xa;
         pc.c0[j] = v_c0;
         pc.P[j] = v_p;
       }
@@ -548,8 +549,7 @@ __device__ __forceinline__ bool rebuild_moved_direct(const PycdKmcSystem& sy,
     const int i = i0 + g;
     const bool is_slot = i < S;
     int n = n_sel;
-    double cq = 0.0, dl = 0.0, de = 0.0;
-    double2 cf = make_double2(0.0, 0.0);
+    double cq = 0.0, xb = 0.0, de = 0.0, xa = 0.0, c0 = 0.0;
     bool act = i <= S;
     if (is_slot) {
       const int64_t slot = (int64_t)n_sel * S + i;
@@ -560,9 +560,10 @@ __device__ __forceinline__ bool rebuild_moved_direct(const PycdKmcSystem& sy,
       } else {
         const double2 sa = __ldg(slotc + 2 * slot), sb = __ldg(slotc + 2 * slot + 1);
         cq = sa.x;
-        dl = sa.y;
+        xb = sa.y;
         de = sb.x;
-        cf = __ldg(coef + slot);
+        xa = sb.y;
+        c0 = __ldg(coef + slot).y;
       }
     }
     const double* rp = A + (int64_t)(act ? n : 0) * N;
@@ -580,18 +581,18 @@ __device__ __forceinline__ bool rebuild_moved_direct(const PycdKmcSystem& sy,
       const int sl = take ? src : 0;
       const int nn = gshfl<G>(gmask, n, sl);
       const double v_cq = gshfl<G>(gmask, cq, sl);
-      const double v_dl = gshfl<G>(gmask, dl, sl);
+      const double v_xb = gshfl<G>(gmask, xb, sl);
       const double v_de = gshfl<G>(gmask, de, sl);
-      const double v_c1 = gshfl<G>(gmask, cf.x, sl);
-      const double v_c0 = gshfl<G>(gmask, cf.y, sl);
+      const double v_xa = gshfl<G>(gmask, xa, sl);
+      const double v_c0 = gshfl<G>(gmask, c0, sl);
       const double v_p = gshfl<G>(gmask, sum, sl);
       if (take) {
         pc.oldsite[j] = n_sel;
         pc.newsite[j] = nn;
         pc.cq[j] = v_cq;
-        pc.dl[j] = v_dl;
+        pc.xb[j] = v_xb;
         pc.de[j] = v_de;
-        pc.c1[j] = v_c1;
+        pc.xa[j] = v_xa;
         pc.c0[j] = v_c0;
         pc.P[j] = v_p;
       }
@@ -621,8 +622,8 @@ __device__ __forceinline__ bool rebuild_moved(const PycdKmcSystem& sy,
 }
 
 // Rates of this lane's processes (core.py:1989-2050):
-//   term = q (P - Q) + cq,   x = lam + dE0 = 2q term + dl,
-//   k = exp(c1 x^2 + c0),    dE0 = 2q term + de (for the selected process).
+//   term = q (P - Q) + cq,   x' = sqrt(-c1) (lam + dE0) = xa term + xb,
+//   k = exp(c0 - x'^2),      dE0 = 2q term + de (for the selected process).
 template <int MAXP>
 __device__ __forceinline__ void process_rates(const ProcCache<MAXP>& pc, double q,
                                               double two_q, double (&kp)[MAXP],
@@ -633,8 +634,8 @@ __device__ __forceinline__ void process_rates(const ProcCache<MAXP>& pc, double 
     term[j] = 0.0;
     if (pc.valid[j]) {
       term[j] = fma(q, dsub(pc.P[j], pc.Q[j]), pc.cq[j]);
-      const double x = fma(two_q, term[j], pc.dl[j]);
-      kp[j] = exp_tang(fma(dmul(x, x), pc.c1[j], pc.c0[j]));
+      const double xs = fma(pc.xa[j], term[j], pc.xb[j]);
+      kp[j] = exp_tang(fma(-xs, xs, pc.c0[j]));
     }
   }
 }

@@ -10,7 +10,7 @@ namespace pycd {
 
 // Device copy of a system descriptor plus the library-derived per-slot
 // tables kept in the KMC workspace: the exponent coefficients (c1, c0) and
-// the slot constants {dphi, t02q}, {de, lam} (two double2 per slot).
+// the slot constants {cq, xb}, {de, xa} (two double2 per slot).
 struct KmcSysDev {
   PycdKmcSystem pub;
   const double2* coef;
@@ -41,7 +41,9 @@ cudaError_t kmc_launch_cta(const KmcArgs& a, int W, int MAXP, int blocks,
                            cudaStream_t s, bool* found);
 cudaError_t kmc_preload_cta();
 int kmc_coef_launch(const PycdKmcSystem& s, double2* coef, cudaStream_t st);
-int kmc_slotc_launch(const PycdKmcSystem& s, double2* slotc, cudaStream_t st);
+// the slot constants; needs the system's coefficient table (coef) first
+int kmc_slotc_launch(const PycdKmcSystem& s, const double2* coef, double2* slotc,
+                     cudaStream_t st);
 int exp_probe_launch(const double* x, int64_t n, double* ours, double* ref,
                      cudaStream_t s);
 int philox_launch(uint64_t seed, uint64_t traj, int64_t step0, int64_t n,
