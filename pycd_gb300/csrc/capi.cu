@@ -268,14 +268,14 @@ int pycd_kmc_upload_systems(const PycdKmcSystem* systems, int32_t n_systems,
   cudaStream_t s = (cudaStream_t)stream;
   PYCD_CUDA(cudaMemcpyAsync(d_workspace, host.data(), host.size(),
                             cudaMemcpyHostToDevice, s));
+  int64_t max_slots = 0;
   for (int i = 0; i < n_systems; ++i) {
-    if (!systems[i].d_rate_coef) {
-      rc = kmc_coef_launch(systems[i], (double2*)dev[i].coef, s);
-      if (rc) return rc;
-    }
-    rc = kmc_slotc_launch(systems[i], dev[i].coef, (double2*)dev[i].slotc, s);
-    if (rc) return rc;
+    const int64_t m = systems[i].n_sites * (int64_t)systems[i].n_slots;
+    if (m > max_slots) max_slots = m;
   }
+  rc = kmc_derive_launch((const KmcSysDev*)((const char*)d_workspace + 256), n_systems,
+                         max_slots, s);
+  if (rc) return rc;
   PYCD_CUDA(cudaStreamSynchronize(s));
   rc = kmc_preload();
   if (rc) return rc;

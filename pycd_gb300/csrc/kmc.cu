@@ -9,45 +9,65 @@
 namespace pycd {
 
 // Per-slot exponent coefficients: c1 = -1/(4 lam kT), c0 = (V + shift)/kT + ln vn.
+__device__ __forceinline__ double2 rate_coef(const double* __restrict__ lam,
+                                             const double* __restrict__ vab,
+                                             const double* __restrict__ shift, int64_t i,
+                                             double kT, double vn) {
+  const double l = lam[i];
+  const double v = vab[i] + (shift ? shift[i] : 0.0);
+  return make_double2(-1.0 / (4.0 * l * kT), v / kT + log(vn));
+}
+
 __global__ void kmc_coef_kernel(const double* __restrict__ lam,
                                 const double* __restrict__ vab,
                                 const double* __restrict__ shift, int64_t n,
                                 double kT, double vn, double2* __restrict__ coef) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  const double l = lam[i];
-  const double v = vab[i] + (shift ? shift[i] : 0.0);
-  coef[i] = make_double2(-1.0 / (4.0 * l * kT), v / kT + log(vn));
+  coef[i] = rate_coef(lam, vab, shift, i, kT, vn);
 }
 
-// Per-slot constants of the rate that change only with the slot's own site
-// (core.py:2004-2026, 2041-2047), with n = nbr[o, s] and the slot's
-// exponent coefficients (c1, c0) = coef[slot]:
+// Per-slot tables of every system of a workspace, in one launch
+// (blockIdx.y = system).  The rate coefficients (c1, c0) (core.py:2041-2047)
+// are written for the systems that do not bring their own.  The slot
+// constants change only with the slot's own site (core.py:2004-2026), with
+// n = nbr[o, s]:
 //   cq = (phi_bg[n] - phi_bg[o]) + q (A[o,o] - A[o,n]),
 //   de = e_rel[n] - e_rel[o],   w = sqrt(-c1),
 //   xa = 2q w,   xb = (de + lam) w,
-// stored as {cq, xb}, {de, xa} and computed once per system.  The step then
-// forms x' = w (lam + dE0) = xa term + xb and c1 (lam + dE0)^2 + c0 =
-// c0 - x'^2.  A slot with an out-of-range neighbour gets zeros; the step
-// stops on that index before it uses them.
-__global__ void kmc_slotc_kernel(PycdKmcSystem s, const double2* __restrict__ coef,
-                                 double2* __restrict__ out) {
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+// stored as {cq, xb}, {de, xa}.  The step then forms x' = w (lam + dE0) =
+// xa term + xb and c1 (lam + dE0)^2 + c0 = c0 - x'^2.  A slot with an
+// out-of-range neighbour gets zeros; the step stops on that index before it
+// uses them.
+__global__ void kmc_derive_kernel(const KmcSysDev* __restrict__ systems, int sys0) {
+  const KmcSysDev& sd = systems[sys0 + blockIdx.y];
+  const PycdKmcSystem& s = sd.pub;
   const int64_t N = s.n_sites;
-  if (i >= N * s.n_slots) return;
-  const int64_t o = i / s.n_slots;
-  const int n = s.d_nbr[i];
-  double2 a = make_double2(0.0, 0.0), b = make_double2(0.0, 0.0);
-  if (n >= 0 && n < N) {
-    const double w = __dsqrt_rn(-coef[i].x);
-    const double dphi = dsub(s.d_phi_bg[n], s.d_phi_bg[o]);
-    const double t02q = dmul(s.carrier_charge, dsub(s.d_A[o * N + o], s.d_A[o * N + n]));
-    const double de = dsub(s.d_e_rel[n], s.d_e_rel[o]);
-    a = make_double2(dadd(dphi, t02q), dmul(dadd(de, s.d_lam[i]), w));
-    b = make_double2(de, dmul(dmul(2.0, s.carrier_charge), w));
+  const int64_t total = N * s.n_slots;
+  double2* out = (double2*)sd.slotc;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    double2 cf;
+    if (s.d_rate_coef) {
+      cf = sd.coef[i];
+    } else {
+      cf = rate_coef(s.d_lam, s.d_vab, s.d_field_shift, i, s.kT, s.vn);
+      ((double2*)sd.coef)[i] = cf;
+    }
+    const int64_t o = i / s.n_slots;
+    const int n = s.d_nbr[i];
+    double2 a = make_double2(0.0, 0.0), b = make_double2(0.0, 0.0);
+    if (n >= 0 && n < N) {
+      const double w = __dsqrt_rn(-cf.x);
+      const double dphi = dsub(s.d_phi_bg[n], s.d_phi_bg[o]);
+      const double t02q = dmul(s.carrier_charge, dsub(s.d_A[o * N + o], s.d_A[o * N + n]));
+      const double de = dsub(s.d_e_rel[n], s.d_e_rel[o]);
+      a = make_double2(dadd(dphi, t02q), dmul(dadd(de, s.d_lam[i]), w));
+      b = make_double2(de, dmul(dmul(2.0, s.carrier_charge), w));
+    }
+    out[2 * i] = a;
+    out[2 * i + 1] = b;
   }
-  out[2 * i] = a;
-  out[2 * i + 1] = b;
 }
 
 __global__ void exp_probe_kernel(const double* __restrict__ x, int64_t n,
@@ -201,12 +221,17 @@ int kmc_coef_launch(const PycdKmcSystem& s, double2* coef, cudaStream_t st) {
   return PYCD_OK;
 }
 
-int kmc_slotc_launch(const PycdKmcSystem& s, const double2* coef, double2* slotc,
-                     cudaStream_t st) {
-  const int64_t n = s.n_sites * (int64_t)s.n_slots;
-  kmc_slotc_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(s, coef, slotc);
-  cudaError_t e = cudaGetLastError();
-  if (e != cudaSuccess) return cuda_fail(e, "kmc_slotc_kernel", __FILE__, __LINE__);
+int kmc_derive_launch(const KmcSysDev* d_systems, int n_systems, int64_t max_slots,
+                      cudaStream_t st) {
+  int64_t bx = (max_slots + 255) / 256;
+  if (bx > 128) bx = 128;
+  if (bx < 1) bx = 1;
+  for (int s0 = 0; s0 < n_systems; s0 += 65535) {
+    const int ny = n_systems - s0 < 65535 ? n_systems - s0 : 65535;
+    kmc_derive_kernel<<<dim3((unsigned)bx, (unsigned)ny), 256, 0, st>>>(d_systems, s0);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(e, "kmc_derive_kernel", __FILE__, __LINE__);
+  }
   return PYCD_OK;
 }
 

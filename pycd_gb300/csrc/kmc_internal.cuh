@@ -41,9 +41,11 @@ cudaError_t kmc_launch_cta(const KmcArgs& a, int W, int MAXP, int blocks,
                            cudaStream_t s, bool* found);
 cudaError_t kmc_preload_cta();
 int kmc_coef_launch(const PycdKmcSystem& s, double2* coef, cudaStream_t st);
-// the slot constants; needs the system's coefficient table (coef) first
-int kmc_slotc_launch(const PycdKmcSystem& s, const double2* coef, double2* slotc,
-                     cudaStream_t st);
+// the per-slot tables (coefficients where not given, slot constants) of
+// every system in a device descriptor table, in one launch per 65,535
+// systems; max_slots = the largest n_sites * n_slots
+int kmc_derive_launch(const KmcSysDev* d_systems, int n_systems, int64_t max_slots,
+                      cudaStream_t st);
 int exp_probe_launch(const double* x, int64_t n, double* ours, double* ref,
                      cudaStream_t s);
 int philox_launch(uint64_t seed, uint64_t traj, int64_t step0, int64_t n,
