@@ -371,6 +371,11 @@ PYCD_API int pycd_philox_uniforms(uint64_t seed, uint64_t traj, int64_t step0,
 PYCD_API int pycd_debug_exp(const double* d_x, int64_t n, double* d_ours,
                             double* d_cuda, void* stream);
 
+/* The kernels' exp() table, as the library builds it on the host (no device
+ * needed): h_out[2 j] + h_out[2 j + 1] = 2^(j/4096), j < 4096 (8192
+ * doubles).  No counterpart in the reference.                              */
+PYCD_API int pycd_debug_exp_table(double* h_out);
+
 /* ---------------------------------------------------------------------------
  * Mean squared displacement: Analysis.compute_msd (PyCD/core.py:2974-3081)
  * on unwrapped trajectory rows already in device memory.

@@ -414,4 +414,11 @@ int pycd_debug_exp(const double* d_x, int64_t n, double* d_ours, double* d_cuda,
   return exp_probe_launch(d_x, n, d_ours, d_cuda, (cudaStream_t)stream);
 }
 
+int pycd_debug_exp_table(double* h_out) {
+  clear_error();
+  PYCD_REQUIRE(h_out, "bad arguments");
+  exp_table_host((double2*)h_out);
+  return PYCD_OK;
+}
+
 }  // extern "C"

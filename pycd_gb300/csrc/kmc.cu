@@ -3,10 +3,63 @@
 #include <cuda_runtime.h>
 #include <math.h>
 #include <stdint.h>
+#include <string.h>
+
+#include <cmath>
+#include <mutex>
 
 #include "kmc_device.cuh"
 
 namespace pycd {
+
+static double seed_bits(unsigned long long b) {
+  double d;
+  memcpy(&d, &b, sizeof d);
+  return d;
+}
+
+// 2^(j/4096) for j = 16 a + b as the double-double product of the seeds
+// 2^(a/256) and 2^(b/4096): ph + pl = h1 h2 exactly (FMA), plus the cross
+// terms; hi = RN(ph + c), lo = (ph - hi) + c (exact).  IEEE operations
+// only (host code is built without contraction), so every host gets the
+// same table; hi + lo is within ~2^-100 of 2^(j/4096).
+void exp_table_host(double2* out) {
+  for (int j = 0; j < 4096; ++j) {
+    const int a = j >> 4, b = j & 15;
+    const double h1 = seed_bits(kExpSeedHi256[a]), l1 = seed_bits(kExpSeedLo256[a]);
+    const double h2 = seed_bits(kExpSeedHi16[b]), l2 = seed_bits(kExpSeedLo16[b]);
+    const double ph = h1 * h2;
+    const double pl = std::fma(h1, h2, -ph);
+    const double c = std::fma(h1, l2, std::fma(l1, h2, pl));
+    const double hi = ph + c;
+    const double lo = (ph - hi) + c;
+    out[j] = make_double2(hi, lo);
+  }
+}
+
+// Fill the exp table of every KMC translation unit on the current device
+// (once per device).
+int kmc_exp_init() {
+  static std::mutex mu;
+  static bool done[64] = {false};
+  static double2 host[4096];
+  static bool built = false;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice", __FILE__, __LINE__);
+  std::lock_guard<std::mutex> lock(mu);
+  if (dev >= 0 && dev < 64 && done[dev]) return PYCD_OK;
+  if (!built) {
+    exp_table_host(host);
+    built = true;
+  }
+  e = exp_table_upload(host);
+  if (e == cudaSuccess) e = kmc_exp_upload_capped(host);
+  if (e == cudaSuccess) e = kmc_exp_upload_cta(host);
+  if (e != cudaSuccess) return cuda_fail(e, "exp table upload", __FILE__, __LINE__);
+  if (dev >= 0 && dev < 64) done[dev] = true;
+  return PYCD_OK;
+}
 
 // Per-slot exponent coefficients: c1 = -1/(4 lam kT), c0 = (V + shift)/kT + ln vn.
 __device__ __forceinline__ double2 rate_coef(const double* __restrict__ lam,
@@ -199,6 +252,8 @@ int kmc_launch(const KmcArgs& a, int max_np, int max_nc,
 }
 
 int kmc_preload() {
+  const int rc = kmc_exp_init();
+  if (rc) return rc;
   cudaFuncAttributes fa;
   cudaError_t e = cudaSuccess;
 #define PYCD_KMC_LOAD(g_, m_)                                                \
@@ -238,6 +293,8 @@ int kmc_derive_launch(const KmcSysDev* d_systems, int n_systems, int64_t max_slo
 int exp_probe_launch(const double* x, int64_t n, double* ours, double* ref,
                      cudaStream_t s) {
   if (n <= 0) return PYCD_OK;
+  const int rc = kmc_exp_init();
+  if (rc) return rc;
   exp_probe_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(x, n, ours, ref);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_fail(e, "exp_probe_kernel", __FILE__, __LINE__);

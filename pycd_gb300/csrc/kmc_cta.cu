@@ -30,4 +30,7 @@ cudaError_t kmc_preload_cta() {
   return e;
 }
 
+// this translation unit's copy of the exp table
+cudaError_t kmc_exp_upload_cta(const double2* h_tab) { return exp_table_upload(h_tab); }
+
 }  // namespace pycd

@@ -33,9 +33,8 @@
 //   The event is the first process whose cumulative rate exceeds u1 k_tot
 //   (core.py:2796-2800); t -= log(u2) / k_tot (core.py:2802-2803).
 // exp() is Tang's table-driven method (ACM TOMS 15(2), 1989): reduction by
-// ln2/256 with a 256-entry table of 2^(j/256) in two parts and a degree-4
-// polynomial on |r| <= ln2/512 (within 0.8 ulp; 2 FP64 instructions fewer
-// than a 32-entry table with a degree-6 polynomial).
+// ln2/4096 with a 4096-entry table of 2^(j/4096) in two parts and a degree-3
+// polynomial on |r| <= ln2/8192 (about 0.52 ulp; 9 FP64 instructions).
 #pragma once
 
 #include <cuda_runtime.h>
@@ -43,6 +42,7 @@
 #include <stdint.h>
 
 #include "common.cuh"
+#include "exp_seed.h"
 #include "kmc_internal.cuh"
 
 namespace pycd {
@@ -53,165 +53,34 @@ __device__ __forceinline__ double dmul(double a, double b) { return __dmul_rn(a,
 __device__ __forceinline__ double ddiv(double a, double b) { return __ddiv_rn(a, b); }
 
 // ---------------------------------------------------------------------------
-// exp(x), Tang's method
+// exp(x), Tang's method with a table of 2^(j/4096)
 // ---------------------------------------------------------------------------
-// 2^(j/256) = kExp2Hi[j] + kExp2Lo[j] (printed by exp_table.py)
-static __device__ const unsigned long long kExp2Hi[256] = {
-    0x3ff0000000000000ULL, 0x3ff00b1afa5abcbfULL, 0x3ff0163da9fb3335ULL, 0x3ff02168143b0281ULL,
-    0x3ff02c9a3e778061ULL, 0x3ff037d42e11bbccULL, 0x3ff04315e86e7f85ULL, 0x3ff04e5f72f654b1ULL,
-    0x3ff059b0d3158574ULL, 0x3ff0650a0e3c1f89ULL, 0x3ff0706b29ddf6deULL, 0x3ff07bd42b72a836ULL,
-    0x3ff0874518759bc8ULL, 0x3ff092bdf66607e0ULL, 0x3ff09e3ecac6f383ULL, 0x3ff0a9c79b1f3919ULL,
-    0x3ff0b5586cf9890fULL, 0x3ff0c0f145e46c85ULL, 0x3ff0cc922b7247f7ULL, 0x3ff0d83b23395decULL,
-    0x3ff0e3ec32d3d1a2ULL, 0x3ff0efa55fdfa9c5ULL, 0x3ff0fb66affed31bULL, 0x3ff1073028d7233eULL,
-    0x3ff11301d0125b51ULL, 0x3ff11edbab5e2ab6ULL, 0x3ff12abdc06c31ccULL, 0x3ff136a814f204abULL,
-    0x3ff1429aaea92de0ULL, 0x3ff14e95934f312eULL, 0x3ff15a98c8a58e51ULL, 0x3ff166a45471c3c2ULL,
-    0x3ff172b83c7d517bULL, 0x3ff17ed48695bbc0ULL, 0x3ff18af9388c8deaULL, 0x3ff1972658375d2fULL,
-    0x3ff1a35beb6fcb75ULL, 0x3ff1af99f8138a1cULL, 0x3ff1bbe084045cd4ULL, 0x3ff1c82f95281c6bULL,
-    0x3ff1d4873168b9aaULL, 0x3ff1e0e75eb44027ULL, 0x3ff1ed5022fcd91dULL, 0x3ff1f9c18438ce4dULL,
-    0x3ff2063b88628cd6ULL, 0x3ff212be3578a819ULL, 0x3ff21f49917ddc96ULL, 0x3ff22bdda27912d1ULL,
-    0x3ff2387a6e756238ULL, 0x3ff2451ffb82140aULL, 0x3ff251ce4fb2a63fULL, 0x3ff25e85711ece75ULL,
-    0x3ff26b4565e27cddULL, 0x3ff2780e341ddf29ULL, 0x3ff284dfe1f56381ULL, 0x3ff291ba7591bb70ULL,
-    0x3ff29e9df51fdee1ULL, 0x3ff2ab8a66d10f13ULL, 0x3ff2b87fd0dad990ULL, 0x3ff2c57e39771b2fULL,
-    0x3ff2d285a6e4030bULL, 0x3ff2df961f641589ULL, 0x3ff2ecafa93e2f56ULL, 0x3ff2f9d24abd886bULL,
-    0x3ff306fe0a31b715ULL, 0x3ff31432edeeb2fdULL, 0x3ff32170fc4cd831ULL, 0x3ff32eb83ba8ea32ULL,
-    0x3ff33c08b26416ffULL, 0x3ff3496266e3fa2dULL, 0x3ff356c55f929ff1ULL, 0x3ff36431a2de883bULL,
-    0x3ff371a7373aa9cbULL, 0x3ff37f26231e754aULL, 0x3ff38cae6d05d866ULL, 0x3ff39a401b7140efULL,
-    0x3ff3a7db34e59ff7ULL, 0x3ff3b57fbfec6cf4ULL, 0x3ff3c32dc313a8e5ULL, 0x3ff3d0e544ede173ULL,
-    0x3ff3dea64c123422ULL, 0x3ff3ec70df1c5175ULL, 0x3ff3fa4504ac801cULL, 0x3ff40822c367a024ULL,
-    0x3ff4160a21f72e2aULL, 0x3ff423fb2709468aULL, 0x3ff431f5d950a897ULL, 0x3ff43ffa3f84b9d4ULL,
-    0x3ff44e086061892dULL, 0x3ff45c2042a7d232ULL, 0x3ff46a41ed1d0057ULL, 0x3ff4786d668b3237ULL,
-    0x3ff486a2b5c13cd0ULL, 0x3ff494e1e192aed2ULL, 0x3ff4a32af0d7d3deULL, 0x3ff4b17dea6db7d7ULL,
-    0x3ff4bfdad5362a27ULL, 0x3ff4ce41b817c114ULL, 0x3ff4dcb299fddd0dULL, 0x3ff4eb2d81d8abffULL,
-    0x3ff4f9b2769d2ca7ULL, 0x3ff508417f4531eeULL, 0x3ff516daa2cf6642ULL, 0x3ff5257de83f4eefULL,
-    0x3ff5342b569d4f82ULL, 0x3ff542e2f4f6ad27ULL, 0x3ff551a4ca5d920fULL, 0x3ff56070dde910d2ULL,
-    0x3ff56f4736b527daULL, 0x3ff57e27dbe2c4cfULL, 0x3ff58d12d497c7fdULL, 0x3ff59c0827ff07ccULL,
-    0x3ff5ab07dd485429ULL, 0x3ff5ba11fba87a03ULL, 0x3ff5c9268a5946b7ULL, 0x3ff5d84590998b93ULL,
-    0x3ff5e76f15ad2148ULL, 0x3ff5f6a320dceb71ULL, 0x3ff605e1b976dc09ULL, 0x3ff6152ae6cdf6f4ULL,
-    0x3ff6247eb03a5585ULL, 0x3ff633dd1d1929fdULL, 0x3ff6434634ccc320ULL, 0x3ff652b9febc8fb7ULL,
-    0x3ff6623882552225ULL, 0x3ff671c1c70833f6ULL, 0x3ff68155d44ca973ULL, 0x3ff690f4b19e9538ULL,
-    0x3ff6a09e667f3bcdULL, 0x3ff6b052fa75173eULL, 0x3ff6c012750bdabfULL, 0x3ff6cfdcddd47645ULL,
-    0x3ff6dfb23c651a2fULL, 0x3ff6ef9298593ae5ULL, 0x3ff6ff7df9519484ULL, 0x3ff70f7466f42e87ULL,
-    0x3ff71f75e8ec5f74ULL, 0x3ff72f8286ead08aULL, 0x3ff73f9a48a58174ULL, 0x3ff74fbd35d7cbfdULL,
-    0x3ff75feb564267c9ULL, 0x3ff77024b1ab6e09ULL, 0x3ff780694fde5d3fULL, 0x3ff790b938ac1cf6ULL,
-    0x3ff7a11473eb0187ULL, 0x3ff7b17b0976cfdbULL, 0x3ff7c1ed0130c132ULL, 0x3ff7d26a62ff86f0ULL,
-    0x3ff7e2f336cf4e62ULL, 0x3ff7f3878491c491ULL, 0x3ff80427543e1a12ULL, 0x3ff814d2add106d9ULL,
-    0x3ff82589994cce13ULL, 0x3ff8364c1eb941f7ULL, 0x3ff8471a4623c7adULL, 0x3ff857f4179f5b21ULL,
-    0x3ff868d99b4492edULL, 0x3ff879cad931a436ULL, 0x3ff88ac7d98a6699ULL, 0x3ff89bd0a478580fULL,
-    0x3ff8ace5422aa0dbULL, 0x3ff8be05bad61778ULL, 0x3ff8cf3216b5448cULL, 0x3ff8e06a5e0866d9ULL,
-    0x3ff8f1ae99157736ULL, 0x3ff902fed0282c8aULL, 0x3ff9145b0b91ffc6ULL, 0x3ff925c353aa2fe2ULL,
-    0x3ff93737b0cdc5e5ULL, 0x3ff948b82b5f98e5ULL, 0x3ff95a44cbc8520fULL, 0x3ff96bdd9a7670b3ULL,
-    0x3ff97d829fde4e50ULL, 0x3ff98f33e47a22a2ULL, 0x3ff9a0f170ca07baULL, 0x3ff9b2bb4d53fe0dULL,
-    0x3ff9c49182a3f090ULL, 0x3ff9d674194bb8d5ULL, 0x3ff9e86319e32323ULL, 0x3ff9fa5e8d07f29eULL,
-    0x3ffa0c667b5de565ULL, 0x3ffa1e7aed8eb8bbULL, 0x3ffa309bec4a2d33ULL, 0x3ffa42c980460ad8ULL,
-    0x3ffa5503b23e255dULL, 0x3ffa674a8af46052ULL, 0x3ffa799e1330b358ULL, 0x3ffa8bfe53c12e59ULL,
-    0x3ffa9e6b5579fdbfULL, 0x3ffab0e521356ebaULL, 0x3ffac36bbfd3f37aULL, 0x3ffad5ff3a3c2774ULL,
-    0x3ffae89f995ad3adULL, 0x3ffafb4ce622f2ffULL, 0x3ffb0e07298db666ULL, 0x3ffb20ce6c9a8952ULL,
-    0x3ffb33a2b84f15fbULL, 0x3ffb468415b749b1ULL, 0x3ffb59728de5593aULL, 0x3ffb6c6e29f1c52aULL,
-    0x3ffb7f76f2fb5e47ULL, 0x3ffb928cf22749e4ULL, 0x3ffba5b030a1064aULL, 0x3ffbb8e0b79a6f1fULL,
-    0x3ffbcc1e904bc1d2ULL, 0x3ffbdf69c3f3a207ULL, 0x3ffbf2c25bd71e09ULL, 0x3ffc06286141b33dULL,
-    0x3ffc199bdd85529cULL, 0x3ffc2d1cd9fa652cULL, 0x3ffc40ab5fffd07aULL, 0x3ffc544778fafb22ULL,
-    0x3ffc67f12e57d14bULL, 0x3ffc7ba88988c933ULL, 0x3ffc8f6d9406e7b5ULL, 0x3ffca3405751c4dbULL,
-    0x3ffcb720dcef9069ULL, 0x3ffccb0f2e6d1675ULL, 0x3ffcdf0b555dc3faULL, 0x3ffcf3155b5bab74ULL,
-    0x3ffd072d4a07897cULL, 0x3ffd1b532b08c968ULL, 0x3ffd2f87080d89f2ULL, 0x3ffd43c8eacaa1d6ULL,
-    0x3ffd5818dcfba487ULL, 0x3ffd6c76e862e6d3ULL, 0x3ffd80e316c98398ULL, 0x3ffd955d71ff6075ULL,
-    0x3ffda9e603db3285ULL, 0x3ffdbe7cd63a8315ULL, 0x3ffdd321f301b460ULL, 0x3ffde7d5641c0658ULL,
-    0x3ffdfc97337b9b5fULL, 0x3ffe11676b197d17ULL, 0x3ffe264614f5a129ULL, 0x3ffe3b333b16ee12ULL,
-    0x3ffe502ee78b3ff6ULL, 0x3ffe653924676d76ULL, 0x3ffe7a51fbc74c83ULL, 0x3ffe8f7977cdb740ULL,
-    0x3ffea4afa2a490daULL, 0x3ffeb9f4867cca6eULL, 0x3ffecf482d8e67f1ULL, 0x3ffee4aaa2188510ULL,
-    0x3ffefa1bee615a27ULL, 0x3fff0f9c1cb6412aULL, 0x3fff252b376bba97ULL, 0x3fff3ac948dd7274ULL,
-    0x3fff50765b6e4540ULL, 0x3fff6632798844f8ULL, 0x3fff7bfdad9cbe14ULL, 0x3fff91d802243c89ULL,
-    0x3fffa7c1819e90d8ULL, 0x3fffbdba3692d514ULL, 0x3fffd3c22b8f71f1ULL, 0x3fffe9d96b2a23d9ULL,
-};
-static __device__ const unsigned long long kExp2Lo[256] = {
-    0x0000000000000000ULL, 0xbc84f6b2a7609f71ULL, 0x3c9b61299ab8cdb7ULL, 0xbc82bf310fc54eb6ULL,
-    0xbc719083535b085dULL, 0x3c656811eeade11aULL, 0xbc90a31c1977c96eULL, 0x3c84c3793aa0d08dULL,
-    0x3c8d73e2a475b465ULL, 0xbc95cb7b5799c397ULL, 0xbc8c91dfe2b13c27ULL, 0x3c83233454458700ULL,
-    0x3c6186be4bb284ffULL, 0xbc968063800a3fd1ULL, 0x3c91487818316136ULL, 0x3c85d16c873d1d38ULL,
-    0x3c98a62e4adc610bULL, 0x3c94f98906d21cefULL, 0x3c901edc16e24f71ULL, 0xbc9bc14de43f316aULL,
-    0x3c403a1727c57b53ULL, 0xbc949db9bc54021bULL, 0xbc6b9bedc44ebd7bULL, 0x3c8d46eb1692fdd5ULL,
-    0xbc96c51039449b3aULL, 0xbc9ca454f703fb72ULL, 0xbc51b514b36ca5c7ULL, 0xbc67108fba48dcf0ULL,
-    0xbc932fbf9af1369eULL, 0xbc8b91e839bf44abULL, 0x3c82406ab9eeab0aULL, 0x3c58f23b82ea1a32ULL,
-    0xbc819041b9d78a76ULL, 0x3c709e3fe2ac5a64ULL, 0xbc911023d1970f6cULL, 0x3c94aadd85f17e08ULL,
-    0x3c8e5b4c7b4968e4ULL, 0x3c97bf85a4b69280ULL, 0xbc995386352ef607ULL, 0x3c9009778010f8c9ULL,
-    0x3c9e016e00a2643cULL, 0xbc96fdd8088cb6deULL, 0xbc91df98027bb78cULL, 0xbc9bf524a097af5cULL,
-    0x3c8dc775814a8495ULL, 0x3c93592d2cfcaac9ULL, 0x3c82a97e9494a5eeULL, 0x3c8d34fb5577d69fULL,
-    0x3c99b07eb6c70573ULL, 0x3c8acfcc911ca996ULL, 0x3c8ac155bef4f4a4ULL, 0x3c93e1a24ac31b2cULL,
-    0x3c82bd339940e9d9ULL, 0x3c9e067c05f9e76cULL, 0xbc9a4c3a8c3f0d7eULL, 0xbc82cc7228401cbdULL,
-    0x3c8612e8afad1255ULL, 0xbc995743191690a7ULL, 0xbc410adcd6381aa4ULL, 0xbc950145a6eb5124ULL,
-    0x3c90024754db41d5ULL, 0x3c9d16cffbbce198ULL, 0x3c71ca0f45d52383ULL, 0xbc653c55532bda93ULL,
-    0x3c86f46ad23182e4ULL, 0x3c8959a3f3f3fcd1ULL, 0x3c8a9ce78e18047cULL, 0xbc9c45e83cb4f318ULL,
-    0x3c932721843659a6ULL, 0xbc835a75930881a4ULL, 0xbc8b5cee5c4e4628ULL, 0xbc8c3144a06cb85eULL,
-    0xbc963aeabf42eae2ULL, 0xbc99f5ca9eceb23cULL, 0xbc9e958d3c9904bdULL, 0xbc99a9a5fc8e2934ULL,
-    0xbc75e436d661f5e3ULL, 0x3c954c66e26fff18ULL, 0xbc9efff8375d29c3ULL, 0x3c7fe8d08c284c71ULL,
-    0x3c8ada0911f09ebcULL, 0xbc8af6637b8c9bcaULL, 0xbc97d023f956f9f3ULL, 0x3c8bddf8b6f4d048ULL,
-    0xbc5ef3691c309278ULL, 0xbc98462dc0b314ddULL, 0xbc81c7dde35f7999ULL, 0x3c8880be9704c003ULL,
-    0x3c489b7a04ef80d0ULL, 0xbc68641982fb1f8eULL, 0x3c9c944bd1648a76ULL, 0xbc9c20f0ed445733ULL,
-    0x3c73c1a3b69062f0ULL, 0xbc83b2895e499ea0ULL, 0x3c99cb62f3d1be56ULL, 0xbc8125b87f2897f0ULL,
-    0x3c7d4397afec42e2ULL, 0x3c905e29690abd5dULL, 0x3c98ecdbbc6a7833ULL, 0xbc95257d2e5d7a52ULL,
-    0xbc94b309d25957e3ULL, 0x3c7a249b49b7465fULL, 0xbc8f768569bd93efULL, 0xbc7c998d43efef71ULL,
-    0xbc807abe1db13cadULL, 0x3c87926d192d5f7eULL, 0xbc8d689cefede59bULL, 0xbc90fb6e168eebf0ULL,
-    0x3c99bb2c011d93adULL, 0xbc90b98c8a57b9c4ULL, 0x3c8295e15b9a1de8ULL, 0xbc97e2cee467e60fULL,
-    0x3c96324c054647adULL, 0xbc9b77a14c233e1aULL, 0x3c3c4b1b816986a2ULL, 0xbc9cd6a7a8b45643ULL,
-    0x3c9ba6f93080e65eULL, 0xbc89eadde3cdcf92ULL, 0xbc93e2429b56de47ULL, 0x3c9e4b3e4ab84c27ULL,
-    0xbc9383c17e40b497ULL, 0x3c984710beb964e5ULL, 0xbc8c483c759d8933ULL, 0xbc9ae3d5c9a73e09ULL,
-    0xbc9bb60987591c34ULL, 0xbc8e8732586c6134ULL, 0x3c6038ae44f73e65ULL, 0x3c8804bd9aeb445dULL,
-    0xbc9bdd3413b26456ULL, 0x3c7a38f52c9a9d0eULL, 0xbc72895667ff0b0dULL, 0x3c9c7aa9b6f17309ULL,
-    0xbc6bbe3a683c88abULL, 0xbc90b9749e1ac8b2ULL, 0xbc883c0f25860ef6ULL, 0x3c59d644d45aa65fULL,
-    0xbc816e4786887a99ULL, 0xbc920aa02cd62c72ULL, 0xbc90a8d96c65d53cULL, 0x3c9047fd618a6e1cULL,
-    0xbc90245957316dd3ULL, 0x3c9b7877169147f8ULL, 0x3c9866b80a02162dULL, 0x3c9349a862aadd3eULL,
-    0xbc841577ee04992fULL, 0xbc9bebb58468dc88ULL, 0x3c9f124cd1164dd6ULL, 0x3c91bddbfb72b8b4ULL,
-    0x3c705d02ba15797eULL, 0xbc807f11cf9311aeULL, 0xbc927c86626d972bULL, 0x3c9464370d151d4dULL,
-    0xbc9d4c1dd41532d8ULL, 0x3c999b9a31df2bd5ULL, 0xbc88d684a341cdfbULL, 0xbc5ba748f8b216d0ULL,
-    0xbc9fc6f89bd4f6baULL, 0x3c85d2d7d2db47bdULL, 0x3c9994c2f37cb53aULL, 0x3c9d53954475202bULL,
-    0x3c96e9f156864b27ULL, 0x3c9ecb5efc43446eULL, 0xbc70d55e32e9e3aaULL, 0xbc97114a6fc9b2e6ULL,
-    0x3c85cc13a2e3976cULL, 0x3c9592ca85fe3fd2ULL, 0xbc9dd6792e582524ULL, 0xbc83455fa639db7fULL,
-    0xbc675fc781b57ebcULL, 0xbc8dc3d6797d2d99ULL, 0xbc764b7c96a5f039ULL, 0xbc5ba5967f19c896ULL,
-    0xbc9d185b7c1b85d1ULL, 0x3c7cabdaa24c78edULL, 0xbc9173bd91cee632ULL, 0xbc9dd84e4df6d518ULL,
-    0x3c7c7c46b071f2beULL, 0xbc9516bea3dd8233ULL, 0x3c7824ca78e64c6eULL, 0xbc84a9ceaaf1faceULL,
-    0xbc9359495d1cd533ULL, 0x3c9c6618ee8be70eULL, 0x3c96305c7ddc36abULL, 0xbc9aa780589fb120ULL,
-    0xbc9d2f6edb8d41e1ULL, 0x3c650f5630670366ULL, 0x3c9bcb7ecac563c7ULL, 0xbc94f867b2ba15a9ULL,
-    0x3c90fac90ef7fd31ULL, 0x3c889c31dae94545ULL, 0xbc8f9234cae76cd0ULL, 0x3c97ef3bb6b1b8e5ULL,
-    0x3c97a1cd345dcc81ULL, 0xbc94b2fc0f315ecdULL, 0xbc9bdef54c80e425ULL, 0x3c94dd024a0756ccULL,
-    0xbc62805e3084d708ULL, 0xbc7f763de9df7c90ULL, 0xbc9c71dfbbba6de3ULL, 0x3c92a8f352883f6eULL,
-    0xbc75584f7e54ac3bULL, 0xbc9b721654cb65c6ULL, 0xbc9efcd30e54292eULL, 0xbc3f52d1c9696205ULL,
-    0x3c823dd07a2d9e84ULL, 0xbc3c262360ea5b52ULL, 0xbc9efdca3f6b9c73ULL, 0xbc8d8a5aa1fbca34ULL,
-    0x3c811065895048ddULL, 0xbc96e51617c8a5d7ULL, 0x3c9b4537e083c60aULL, 0x3c912f072493b5afULL,
-    0x3c92884dff483cadULL, 0xbc8e76bbbe255559ULL, 0x3c71acbc48805c44ULL, 0xbc87f2bed10d08f5ULL,
-    0x3c7503cbd1e949dbULL, 0xbc7d220f86009093ULL, 0xbc8dd83b53829d72ULL, 0xbc9a08e9b86dff57ULL,
-    0xbc9cbc3743797a9cULL, 0x3c955636219a36eeULL, 0xbc9d487b719d8578ULL, 0x3c93db53bf5a1614ULL,
-    0x3c82ed02d75b3707ULL, 0x3c5fe87a4a8165a0ULL, 0xbc911ec18beddfe8ULL, 0x3c9a052dbb9af6beULL,
-    0x3c9c2300696db532ULL, 0xbc9b76f1926b8be4ULL, 0x3c92da5778f018c3ULL, 0xbc9ca5528e79ba8fULL,
-    0xbc91a5cd4f184b5cULL, 0xbc72b529bd5c7f44ULL, 0xbc97b627817a1496ULL, 0xbc99f4a431fdc68bULL,
-    0x3c839e8980a9cc8fULL, 0xbc863ff87522b735ULL, 0x3c92d522ca0c8de2ULL, 0xbc91089480b054b1ULL,
-    0xbc9e9c23179c2893ULL, 0x3c94832f2293e4f2ULL, 0xbc9c93f3b411ad8cULL, 0x3c91c68da487568dULL,
-    0x3c9dc7f486a4b6b0ULL, 0xbc93220065181d45ULL, 0x3c93a1a5bf0d8e43ULL, 0xbc795a5a3ed837deULL,
-    0x3c99d3e12dd8a18bULL, 0x3c9fa37b3539343eULL, 0xbc9dbb12d006350aULL, 0xbc612ea8a779f689ULL,
-    0x3c874853f3a5931eULL, 0xbc79677315098eb6ULL, 0x3c62eb74966579e7ULL, 0x3c74a6037442fde3ULL,
-};
+// g_exp2_tab[j] = (hi, lo) with hi + lo = 2^(j/4096) to ~2^-100 relative,
+// hi = RN(2^(j/4096)) and |lo| < ulp(hi)/2.  Every translation unit that
+// includes this header has its own copy; the library fills each once per
+// device (exp_table_upload) before any kernel of the unit runs.
+static __device__ double2 g_exp2_tab[4096];
 
-// v = 2^(j/256) (1 + expm1(r)) in [2^-1/512, 2^(1+1/512)) for
-// x = (256m + j) ln2/256 + r
+static inline cudaError_t exp_table_upload(const double2* h_tab) {
+  return cudaMemcpyToSymbol(g_exp2_tab, h_tab, sizeof(double2) * 4096);
+}
+
+// v = 2^(j/4096) (1 + expm1(r)) in [2^-1/8192, 2^(1+1/8192)) for
+// x = (4096m + j) ln2/4096 + r
 __device__ __forceinline__ double exp_tang_core(double x, int& m) {
-  const double kInvL = 369.3299304675746;        // 256 / ln 2
-  const double kL1 = 0.002707606173999011;       // ln2/256 to 34 bits (N kL1 exact)
-  const double kL2 = 6.327543041662719e-14;      // ln2/256 - kL1
   const double kShift = 6755399441055744.0;      // 1.5 * 2^52
-  // N = round(x * 256/ln2) in the low word of t
-  const double t = fma(x, kInvL, kShift);
+  // N = round(x * 4096/ln2) in the low word of t
+  const double t = fma(x, PYCD_EXP_INVL, kShift);
   const int n = __double2loint(t);
   const double nd = dsub(t, kShift);
-  const double r = fma(-nd, kL2, fma(-nd, kL1, x));
-  const int j = n & 255;
-  m = (n - j) >> 8;
-  // p = expm1(r) on |r| <= ln2/512, Taylor to degree 4 (r^5/120 < 4e-17)
-  double p = fma(r, 1.0 / 24.0, 1.0 / 6.0);
-  p = fma(p, r, 0.5);
-  p = fma(dmul(p, r), r, r);
-  const double shi = __longlong_as_double((long long)kExp2Hi[j]);
-  const double slo = __longlong_as_double((long long)kExp2Lo[j]);
-  // 2^(j/256) (1 + p) = shi + (slo + (shi + slo) p), where shi + slo rounds
-  // to shi (|slo| < ulp(shi)/2 for every entry, by construction of the table)
-  return dadd(shi, fma(shi, p, slo));
+  const double r = fma(-nd, PYCD_EXP_L2, fma(-nd, PYCD_EXP_L1, x));
+  const int j = n & 4095;
+  m = (n - j) >> 12;
+  // p = expm1(r) on |r| <= ln2/8192 to degree 3 (r^4/24 < 2.2e-18)
+  const double p = fma(fma(r, 1.0 / 6.0, 0.5), dmul(r, r), r);
+  const double2 e = g_exp2_tab[j];
+  // 2^(j/4096) (1 + p) = hi + (lo + (hi + lo) p), where hi + lo rounds to hi
+  return dadd(e.x, fma(e.x, p, e.y));
 }
 
 static __device__ __noinline__ double exp_tang_wide(double x) {

@@ -46,6 +46,24 @@ def test_default_lanes_rule():
         default_lanes(16, 33, 1)
 
 
+def test_exp_table_is_correctly_rounded():
+    """The kernels' table of 2^(j/4096), built by the library on the host from
+    two seed tables: hi is 2^(j/4096) correctly rounded, hi + lo is within
+    2^-100 of it, and |lo| < ulp(hi)/2 (so hi + lo rounds to hi, which the
+    kernels' exp relies on)."""
+    mp = pytest.importorskip("mpmath")
+    import math
+    mp.mp.prec = 200
+    out = np.zeros(8192)
+    nat.check(nat.lib().pycd_debug_exp_table(out.ctypes.data_as(ctypes.c_void_p)))
+    hi, lo = out[0::2], out[1::2]
+    for j in range(4096):
+        exact = mp.mpf(2) ** (mp.mpf(j) / 4096)
+        assert hi[j] == float(exact), j
+        assert abs(mp.mpf(hi[j]) + mp.mpf(lo[j]) - exact) < exact * mp.mpf(2) ** -100, j
+        assert abs(lo[j]) < math.ulp(hi[j]) / 2 and hi[j] + lo[j] == hi[j], j
+
+
 def test_library_reports_missing_device_as_error():
     import torch
     if torch.cuda.is_available():
