@@ -131,8 +131,18 @@ def _material(params, lattice, types_, counts, frac):
     return Material(ReturnValues(**p))
 
 
-def corundum(cells=(3, 3, 3), neighbor_list=True):
+def corundum(cells=(3, 3, 3), neighbor_list=True, shells=None):
+    """The corundum Fe sublattice; `shells` replaces the two hop shells
+    (2.90, 2.97 A) by the given Fe-Fe distances (2.90, 2.971, 3.364, 3.705,
+    3.986 A hold 1, 3, 3, 6, 1 neighbours), each with lambda 0.9 eV and
+    V_ab 0.2 eV."""
     params = corundum_params()
+    if shells is not None:
+        n = len(shells)
+        params.update(neighbor_cutoff_dist={"Fe:Fe": [list(shells)]},
+                      neighbor_cutoff_dist_tol={"Fe:Fe": [[0.01] * n]},
+                      lambda_values={"Fe:Fe": [[0.9] * n]},
+                      v_ab={"Fe:Fe": [[0.2] * n]})
     mat = _material(params, CORUNDUM_LATTICE, ["Fe"], [12], corundum_frac())
     nb = Neighbors(mat, np.asarray(cells), np.array([1, 1, 1]))
     hop = nb.generate_neighbor_list(None, (3, 3, 3), save=False) \

@@ -339,3 +339,42 @@ def test_block_form_matches_oracle_with_32_carriers(cuda_ready):
                run.temp, u, run.time_interval, tables.n_path_steps)
     assert np.array_equal(o["proc"], b.step_proc[0, :m].cpu().numpy())
     assert np.abs(o["time"][1:] / b.step_time[0, :m].cpu().numpy() - 1).max() < TIME_RTOL
+
+
+def test_fourteen_slots_two_rebuild_rounds(cuda_ready):
+    """Five corundum hop shells give 14 hop slots per carrier; 12 carriers
+    give 168 processes.  The moved carrier's 15 rebuild jobs take two rounds
+    in the warp form's many-carrier rebuild and in the block form, whose
+    neighbour cache covers at most 4 slots (so it reads the neighbour table
+    here).  Events, times and sites must agree across the forms, and the
+    events with the oracle's."""
+    import torch
+    sysm = wl.corundum((3, 3, 3), shells=(2.90, 2.97, 3.364, 3.705, 3.986))
+    A = sysm.get_precomputed_array_device("fp64")
+    tables, run = wl.batched_tables(sysm, A, 12, [], 1.0, t_final=1e30, time_interval=1e27)
+    assert tables.n_slots == 14
+    T, n, seed = 4, 400, 515
+    rng = np.random.default_rng(17)
+    occ = np.stack([rng.choice(324, size=12, replace=False) for _ in range(T)])
+    results = []
+    for lanes in (32, 64, 128):
+        eng = KmcEngine(tables, launch={"lanes_per_traj": lanes})
+        b = KmcBatch(occ, step_capacity=n)
+        eng.advance(b, n, eng.rng_struct(seed=seed))
+        torch.cuda.synchronize()
+        assert (b.step.cpu().numpy() == n).all(), lanes
+        results.append((b.step_proc.cpu().numpy(), b.step_time.cpu().numpy(),
+                        b.occ.cpu().numpy()))
+    for r in results[1:]:
+        for x, y in zip(r, results[0]):
+            assert np.array_equal(x, y)
+    m = sysm.material
+    otab = ko.Tables(sysm.hop_neighbor_list, "Fe:Fe", np.zeros(324, int), 12, 0, 12,
+                     m.lambda_values["Fe:Fe"], m.v_ab["Fe:Fe"])
+    k = 300
+    u = np.array([v for s in range(k) for v in philox.step_uniforms(seed, 0, s)])
+    o = ko.run(A.cpu().numpy(), otab, list(occ[0]), np.zeros(324), -1.0, np.zeros(324),
+               m.vn, run.temp, u, run.time_interval, tables.n_path_steps)
+    assert o["steps"] == k
+    assert np.array_equal(o["proc"], results[0][0][0, :k])
+    assert np.abs(o["time"][1:] / results[0][1][0, :k] - 1).max() < TIME_RTOL
