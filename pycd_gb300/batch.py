@@ -16,7 +16,7 @@ the device, the whole job runs, and NumPy results come back.
 import numpy as np
 
 from . import _native as nat
-from .kmc import KmcBatch, KmcEngine, KmcTables
+from .kmc import KmcBatch, KmcEngine, KmcTables, default_lanes
 
 
 def _bucket_of(n_proc):
@@ -99,6 +99,33 @@ class BatchedKmc(object):
             out.append(bk.tuning["best"])
         self.graph = None
         return out
+
+    def adapt_shapes(self):
+        """Re-pick each bucket's launch shape for the trajectories still
+        running, by the launcher's default rule (wider, up to one block of 4
+        warps per trajectory, while the launch keeps <= 2 warps per SM
+        sub-partition).  A shape is only widened, so a full bucket keeps its
+        tuned shape; results do not depend on it.  Call between chunks (it
+        reads the statuses); the next chunk recaptures its graph if a shape
+        changed.  Returns the number of buckets whose shape changed."""
+        changed = 0
+        for bk in self.buckets:
+            running = int((bk.batch.status == nat.TRAJ_RUNNING).sum().item())
+            if running == 0:
+                continue
+            L = bk.engine.launch
+            cur = L.lanes_per_traj or default_lanes(L.max_processes, L.max_carriers,
+                                                    len(bk.idx))
+            lanes = default_lanes(L.max_processes, L.max_carriers, running)
+            if lanes > cur:
+                L.lanes_per_traj = lanes
+                if lanes > 32:
+                    L.warps_per_block = 0
+                    L.min_blocks_per_sm = 0
+                changed += 1
+        if changed:
+            self.graph = None
+        return changed
 
     def _launch_all(self):
         import torch

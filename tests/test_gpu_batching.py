@@ -23,6 +23,9 @@ def _tables(lattice, cells, n_carriers, dopants, precision="fp64"):
 
 
 def test_uneven_buckets_equal_alone_runs(cuda_ready):
+    """Trajectories of four systems in process-count buckets with autotuned
+    shapes, widened between chunks as they finish, equal the same
+    trajectories run alone."""
     import torch
     specs = [("corundum", (3, 3, 1), 1, [5]), ("monoclinic", (3, 3, 3), 3, []),
              ("corundum", (3, 3, 2), 6, [1, 2, 3]), ("monoclinic", (4, 4, 3), 12, [7])]
@@ -40,7 +43,14 @@ def test_uneven_buckets_equal_alone_runs(cuda_ready):
     bk = BatchedKmc(tables, np.stack(occ), sys_index=sys_index, seed=77,
                     chunk_steps=1000, step_limit=limits, autotune=True)
     assert len(bk.buckets) >= 3
-    bk.run(3000)
+    # chunk by chunk, re-picking the buckets' shapes for the trajectories
+    # still running (widening, up to the block forms): results must not move
+    changed = 0
+    for _ in range(3):
+        bk.step_chunk()
+        torch.cuda.synchronize()
+        changed += bk.adapt_shapes()
+    assert changed > 0
     torch.cuda.synchronize()
     assert (bk.gather("status").cpu().numpy() == nat.TRAJ_STEP_LIMIT).all()
     assert (bk.gather("step").cpu().numpy() == np.array(limits)).all()
