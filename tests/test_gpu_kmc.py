@@ -18,7 +18,7 @@ from pycd_gb300 import _native as nat
 from pycd_gb300 import constants as K
 from pycd_gb300 import workloads as wl
 from pycd_gb300.core import Run, System
-from pycd_gb300.kmc import KmcBatch, KmcEngine
+from pycd_gb300.kmc import KmcBatch, KmcEngine, KmcTables
 
 pytestmark = pytest.mark.gpu
 TIME_RTOL = 1e-12
@@ -378,3 +378,54 @@ def test_fourteen_slots_two_rebuild_rounds(cuda_ready):
     assert o["steps"] == k
     assert np.array_equal(o["proc"], results[0][0][0, :k])
     assert np.abs(o["time"][1:] / results[0][1][0, :k] - 1).max() < TIME_RTOL
+
+
+def test_field_drift_and_delg0_grid(cuda_ready):
+    """An electric field shifts each rate by 0.5 E.hop (core.py:2041-2047).
+    Events and the dG0 path grid (core.py:2806-2808) against the oracle; the
+    drift sums (hop x rate of each event, core.py:2821-2824), the grids and
+    the times equal across the warp and block forms."""
+    import torch
+    sysm = wl.corundum((3, 3, 3))
+    A = sysm.get_precomputed_array_device("fp64")
+    field = {"electric": {"active": 1, "dir": [1, 0, 0], "ld": 0, "mag": 5e-5}}
+    run = Run(sysm, None, 300, "full", "full", 1, 5e-11, 1e-13, np.array([2]),
+              {"electron": []}, {"class_index": {}, "doping": {}}, field,
+              {"num_dopants": [0]})
+    assert run.site_field_shift is not None and np.abs(run.site_field_shift).max() > 0
+    n_path = int(run.t_final / run.time_interval) + 1
+    q = run.base_charge_config()[:, 0].copy()
+    tables = KmcTables(A, run.site_nbr, run.site_hop, run.site_lam, run.site_vab,
+                       run.system_relative_energies, q, run.carrier_charge, 2,
+                       run.material.vn, run.temp, run.time_interval, n_path,
+                       field_shift=run.site_field_shift)
+    T, n, seed = 4, 400, 808
+    rng = np.random.default_rng(23)
+    occ = np.stack([rng.choice(324, size=2, replace=False) for _ in range(T)])
+    keys = ("step_proc", "step_time", "delg0_grid", "drift", "occ", "time")
+    results = []
+    for lanes in (8, 16, 64, 128):
+        eng = KmcEngine(tables, launch={"lanes_per_traj": lanes})
+        b = KmcBatch(occ, step_capacity=n, delg0_grid_rows=n_path, drift=True)
+        eng.advance(b, n, eng.rng_struct(seed=seed))
+        torch.cuda.synchronize()
+        assert (b.step.cpu().numpy() == n).all(), lanes
+        results.append({k: getattr(b, k).cpu().numpy() for k in keys})
+    for r in results[1:]:
+        for k in keys:
+            assert np.array_equal(r[k], results[0][k]), k
+    assert np.abs(results[0]["drift"]).max() > 0
+    m = sysm.material
+    otab = ko.Tables(sysm.hop_neighbor_list, "Fe:Fe", np.zeros(324, int), 12, 0, 12,
+                     m.lambda_values["Fe:Fe"], m.v_ab["Fe:Fe"], field=run.electric_field)
+    k = 300
+    u = np.array([v for s in range(k) for v in philox.step_uniforms(seed, 0, s)])
+    o = ko.run(A.cpu().numpy(), otab, list(occ[0]), q, run.carrier_charge,
+               run.system_relative_energies, m.vn, run.temp, u, run.time_interval, n_path)
+    assert o["steps"] == k
+    assert np.array_equal(o["proc"], results[0]["step_proc"][0, :k])
+    assert np.abs(o["time"][1:] / results[0]["step_time"][0, :k] - 1).max() < TIME_RTOL
+    rows = np.nonzero(o["delg0"])[0]
+    assert len(rows) > 3  # several grid crossings within the oracle's steps
+    got = results[0]["delg0_grid"][0, rows]
+    assert np.abs(got - o["delg0"][rows]).max() <= 1e-12 * np.abs(o["delg0"][rows]).max()
