@@ -290,6 +290,38 @@ def example(core, name, params, t_final):
     (HERE / f"{name.lower()}.json").write_text(json.dumps(cfg, indent=1))
 
 
+def every_step(core):
+    """examples/Hematite for its first ~2,000 steps with write_every_step = 1:
+    the reference's per-step unwrapped rows (core.py:2832-2846) and times,
+    from the shipped traj1 random state."""
+    import copy
+    name, params, t_final = "Hematite", HEMATITE, 6e-7
+    ex = REF / "examples" / name
+    poscar = (ex / "InputFiles" / "POSCAR").read_text()
+    tmp = tempfile.mkdtemp()
+    mat, nb = material_objects(core, params, poscar, [2, 2, 1], [1, 1, 1], tmp)
+    hop = np.load(ex / "InputFiles" / "hop_neighbor_list.npy", allow_pickle=True)[()]
+    pmiv = np.load(ex / "InputFiles" / "pairwise_min_image_vector_data.npy")
+    A_shipped = np.load(ex / "InputFiles" / "precomputed_array.npy")
+    system = make_system(core, mat, nb, hop, pmiv, params)
+    run_p = copy.deepcopy(dict(RUN_COMMON, t_final=t_final))
+    run_p["output_data"]["unwrapped_traj"]["write_every_step"] = 1
+    run = core.Run(system, A_shipped, run_p["temp"], run_p["ion_charge_type"],
+                   run_p["species_charge_type"], 1, t_final, run_p["time_interval"],
+                   np.asarray(run_p["species_count"]), run_p["initial_occupancy"],
+                   run_p["relative_energies"], run_p["external_field"], run_p["doping"])
+    d = Path(tempfile.mkdtemp())
+    shutil.copy(ex / "traj1" / "initial_rnd_state.dump", d / "initial_rnd_state.dump")
+    run.do_kmc_steps(d, run_p["output_data"], run_p["random_seed"], "parallel")
+    u = np.load(d / "unwrapped_traj.npy")
+    t = np.load(d / "time_data.npy")
+    print(f"{name} every step: {len(t) - 1} steps, {len(u)} rows")
+    np.savez_compressed(HERE / "hematite_every_step.npz", unwrapped=u, time=t)
+    cfg = {"t_final": t_final, "n_steps": int(len(t) - 1), "rows": int(len(u)),
+           "output_data": run_p["output_data"], "unwrapped_sha256": sha(u)}
+    (HERE / "hematite_every_step.json").write_text(json.dumps(cfg, indent=1))
+
+
 # ---------------------------------------------------------------- injected run
 class Injected:
     """random-module stand-in: random() pops injected uniforms, sample()
@@ -626,6 +658,8 @@ def main(parts):
         msd(core)
     if "hematite" in parts:
         example(core, "Hematite", HEMATITE, 1e-4)
+    if "every_step" in parts:
+        every_step(core)
     if "bvo" in parts:
         example(core, "BVO", BVO, 1e-3)
     if "corundum324" in parts:
@@ -635,5 +669,5 @@ def main(parts):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1:] or ["hematite", "bvo", "corundum324", "corundum3600", "msd",
-                          "ewald_params"])
+    main(sys.argv[1:] or ["hematite", "every_step", "bvo", "corundum324", "corundum3600",
+                          "msd", "ewald_params"])

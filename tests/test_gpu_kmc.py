@@ -24,14 +24,14 @@ pytestmark = pytest.mark.gpu
 TIME_RTOL = 1e-12
 
 
-def _example_run(name):
+def _example_run(name, t_final=None):
     cfg, arr = gio.load(name)
     mat, nb = gio.material(cfg)
     p, r = cfg["params"], cfg["run"]
     sysm = System(mat, nb, gio.hop_list(cfg, arr), arr["pmiv"], p["alpha"],
                   p["r_cut"], p["k_cut"])
     run = Run(sysm, arr["A"], r["temp"], r["ion_charge_type"],
-              r["species_charge_type"], 1, r["t_final"], r["time_interval"],
+              r["species_charge_type"], 1, t_final or r["t_final"], r["time_interval"],
               np.asarray(r["species_count"]), r["initial_occupancy"],
               r["relative_energies"], r["external_field"], r["doping"])
     return cfg, arr, run
@@ -54,6 +54,24 @@ def test_do_kmc_steps_reproduces_shipped_trajectory(cuda_ready, name):
     assert np.abs(ts[1:] / arr["time"][1:] - 1).max() < TIME_RTOL
     assert abs(t[-1] / arr["time_last"][0] - 1) < TIME_RTOL
     assert (d / "Run.log").exists()
+
+
+def test_do_kmc_steps_write_every_step_matches_reference(cuda_ready):
+    """write_every_step = 1 (core.py:2832-2846): the per-step unwrapped rows
+    of the reference's own run of examples/Hematite (~2,000 steps from the
+    shipped random state), bit for bit, and its times."""
+    ref, fix = gio.load("hematite_every_step")
+    cfg, arr, run = _example_run("hematite", t_final=ref["t_final"])
+    d = Path(tempfile.mkdtemp())
+    st = cfg["rnd_state"]
+    with open(d / "initial_rnd_state.dump", "wb") as fh:
+        pickle.dump((st[0], tuple(st[1]), st[2]), fh)
+    run.do_kmc_steps(d, ref["output_data"], cfg["run"]["random_seed"], "parallel")
+    u = np.load(d / "unwrapped_traj.npy")
+    t = np.load(d / "time_data.npy")
+    assert len(t) == ref["n_steps"] + 1
+    assert np.array_equal(u, fix["unwrapped"])
+    assert np.abs(t[1:] / fix["time"][1:] - 1).max() < TIME_RTOL
 
 
 def _corundum324_engine(cfg, arr):
