@@ -322,6 +322,60 @@ def every_step(core):
     (HERE / "hematite_every_step.json").write_text(json.dumps(cfg, indent=1))
 
 
+BVO_DOPING = {"num_dopants": [2, 0], "doping_element_map": ["V:W", "V:Mo"],
+              "insertion_type": ["manual", "manual"],
+              "charge": {"full": {"W": 6.0, "Mo": 6.0}},
+              "site_charge_initiation": ["yes", "no"], "min_shell_separation": [0, 0],
+              "max_attempts": 1}
+
+
+def bvo_doped(core):
+    """examples/BVO with two W dopants (charge 6 on V sites) from a manual
+    site_indices.npy with shell-indexed site energies (shells 0, 1, 2), the
+    electron starting on a dopant site (site_charge_initiation 'yes', drawn
+    by rnd.sample from the shipped traj1 random state).  The reference's
+    do_kmc_steps: unwrapped rows, times, occupancy list and its doped site
+    energies (core.py:2723-2772, 2478-2528)."""
+    import copy
+    name, params, t_final = "BVO", BVO, 4e-5
+    ex = REF / "examples" / name
+    poscar = (ex / "InputFiles" / "POSCAR").read_text()
+    tmp = tempfile.mkdtemp()
+    mat, nb = material_objects(core, params, poscar, [2, 2, 1], [1, 1, 1], tmp)
+    hop = np.load(ex / "InputFiles" / "hop_neighbor_list.npy", allow_pickle=True)[()]
+    pmiv = np.load(ex / "InputFiles" / "pairwise_min_image_vector_data.npy")
+    A_shipped = np.load(ex / "InputFiles" / "precomputed_array.npy")
+    system = make_system(core, mat, nb, hop, pmiv, params)
+    # V sites: the hop neighbours of the V:V list; two dopants and a few shells
+    v_sites = sorted({int(i) for obj in hop["V:V"][0]
+                      for row in obj.neighbor_system_element_indices for i in row})
+    d1, d2 = v_sites[1], v_sites[6]
+    near = [i for i in v_sites if i not in (d1, d2)]
+    site_indices = np.array([[d1, 0, 0, 0], [d2, 0, 0, 0],
+                             [near[0], 0, 0, 1], [near[2], 0, 0, 1],
+                             [near[4], 0, 0, 2], [near[7], 0, 0, 2]], dtype=int)
+    run_p = copy.deepcopy(dict(RUN_COMMON, t_final=t_final, doping=BVO_DOPING))
+    run = core.Run(system, A_shipped, run_p["temp"], run_p["ion_charge_type"],
+                   run_p["species_charge_type"], 1, t_final, run_p["time_interval"],
+                   np.asarray(run_p["species_count"]), run_p["initial_occupancy"],
+                   run_p["relative_energies"], run_p["external_field"], run_p["doping"])
+    d = Path(tempfile.mkdtemp())
+    shutil.copy(ex / "traj1" / "initial_rnd_state.dump", d / "initial_rnd_state.dump")
+    np.save(d / "site_indices.npy", site_indices)
+    run.do_kmc_steps(d, run_p["output_data"], run_p["random_seed"], "parallel")
+    u = np.load(d / "unwrapped_traj.npy")
+    t = np.load(d / "time_data.npy")
+    occ = np.load(d / "occupancy.npy")
+    print(f"{name} doped: {len(t) - 1} steps, first site {occ[0].tolist()}, "
+          f"dopants {d1}, {d2}")
+    np.savez_compressed(HERE / "bvo_doped.npz", unwrapped=u, time=t, occupancy=occ,
+                        site_indices=site_indices,
+                        system_relative_energies=np.asarray(run.system_relative_energies))
+    cfg = {"t_final": t_final, "n_steps": int(len(t) - 1), "doping": run_p["doping"],
+           "output_data": run_p["output_data"], "unwrapped_sha256": sha(u)}
+    (HERE / "bvo_doped.json").write_text(json.dumps(cfg, indent=1))
+
+
 # ---------------------------------------------------------------- injected run
 class Injected:
     """random-module stand-in: random() pops injected uniforms, sample()
@@ -662,6 +716,8 @@ def main(parts):
         every_step(core)
     if "bvo" in parts:
         example(core, "BVO", BVO, 1e-3)
+    if "bvo_doped" in parts:
+        bvo_doped(core)
     if "corundum324" in parts:
         corundum324(core)
     if "corundum3600" in parts:
@@ -669,5 +725,5 @@ def main(parts):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1:] or ["hematite", "every_step", "bvo", "corundum324", "corundum3600",
-                          "msd", "ewald_params"])
+    main(sys.argv[1:] or ["hematite", "every_step", "bvo", "bvo_doped", "corundum324",
+                          "corundum3600", "msd", "ewald_params"])

@@ -24,7 +24,7 @@ pytestmark = pytest.mark.gpu
 TIME_RTOL = 1e-12
 
 
-def _example_run(name, t_final=None):
+def _example_run(name, t_final=None, doping=None):
     cfg, arr = gio.load(name)
     mat, nb = gio.material(cfg)
     p, r = cfg["params"], cfg["run"]
@@ -33,7 +33,7 @@ def _example_run(name, t_final=None):
     run = Run(sysm, arr["A"], r["temp"], r["ion_charge_type"],
               r["species_charge_type"], 1, t_final or r["t_final"], r["time_interval"],
               np.asarray(r["species_count"]), r["initial_occupancy"],
-              r["relative_energies"], r["external_field"], r["doping"])
+              r["relative_energies"], r["external_field"], doping or r["doping"])
     return cfg, arr, run
 
 
@@ -67,6 +67,29 @@ def test_do_kmc_steps_write_every_step_matches_reference(cuda_ready):
     with open(d / "initial_rnd_state.dump", "wb") as fh:
         pickle.dump((st[0], tuple(st[1]), st[2]), fh)
     run.do_kmc_steps(d, ref["output_data"], cfg["run"]["random_seed"], "parallel")
+    u = np.load(d / "unwrapped_traj.npy")
+    t = np.load(d / "time_data.npy")
+    assert len(t) == ref["n_steps"] + 1
+    assert np.array_equal(u, fix["unwrapped"])
+    assert np.abs(t[1:] / fix["time"][1:] - 1).max() < TIME_RTOL
+
+
+def test_do_kmc_steps_doped_bvo_matches_reference(cuda_ready):
+    """examples/BVO with two W dopants (charge 6) and shell-indexed site
+    energies read from site_indices.npy, the electron starting on a dopant
+    site (MT19937 rnd.sample): the doped site energies, the occupancy list,
+    the unwrapped rows and the times of the reference's own run."""
+    ref, fix = gio.load("bvo_doped")
+    cfg, arr, run = _example_run("bvo", t_final=ref["t_final"], doping=ref["doping"])
+    d = Path(tempfile.mkdtemp())
+    st = cfg["rnd_state"]
+    with open(d / "initial_rnd_state.dump", "wb") as fh:
+        pickle.dump((st[0], tuple(st[1]), st[2]), fh)
+    np.save(d / "site_indices.npy", fix["site_indices"])
+    run.do_kmc_steps(d, ref["output_data"], cfg["run"]["random_seed"], "parallel")
+    assert np.array_equal(np.asarray(run.system_relative_energies),
+                          fix["system_relative_energies"])
+    assert np.array_equal(np.load(d / "occupancy.npy"), fix["occupancy"])
     u = np.load(d / "unwrapped_traj.npy")
     t = np.load(d / "time_data.npy")
     assert len(t) == ref["n_steps"] + 1
