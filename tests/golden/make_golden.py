@@ -322,6 +322,39 @@ def every_step(core):
     (HERE / "hematite_every_step.json").write_text(json.dumps(cfg, indent=1))
 
 
+def hematite_outputs(core):
+    """examples/Hematite for its first ~2,000 steps with the energy and dG0
+    path grids written (core.py:2806-2808, 2848-2861, 2863-2906), from the
+    shipped traj1 random state."""
+    import copy
+    name, params, t_final = "Hematite", HEMATITE, 6e-7
+    ex = REF / "examples" / name
+    poscar = (ex / "InputFiles" / "POSCAR").read_text()
+    tmp = tempfile.mkdtemp()
+    mat, nb = material_objects(core, params, poscar, [2, 2, 1], [1, 1, 1], tmp)
+    hop = np.load(ex / "InputFiles" / "hop_neighbor_list.npy", allow_pickle=True)[()]
+    pmiv = np.load(ex / "InputFiles" / "pairwise_min_image_vector_data.npy")
+    A_shipped = np.load(ex / "InputFiles" / "precomputed_array.npy")
+    system = make_system(core, mat, nb, hop, pmiv, params)
+    run_p = copy.deepcopy(dict(RUN_COMMON, t_final=t_final))
+    run_p["output_data"]["energy"]["write"] = 1
+    run_p["output_data"]["delg_0"]["write"] = 1
+    run = core.Run(system, A_shipped, run_p["temp"], run_p["ion_charge_type"],
+                   run_p["species_charge_type"], 1, t_final, run_p["time_interval"],
+                   np.asarray(run_p["species_count"]), run_p["initial_occupancy"],
+                   run_p["relative_energies"], run_p["external_field"], run_p["doping"])
+    d = Path(tempfile.mkdtemp())
+    shutil.copy(ex / "traj1" / "initial_rnd_state.dump", d / "initial_rnd_state.dump")
+    run.do_kmc_steps(d, run_p["output_data"], run_p["random_seed"], "parallel")
+    out = {k: np.load(d / run_p["output_data"][k]["file_name"])
+           for k in ("unwrapped_traj", "time", "energy", "delg_0")}
+    print(f"{name} outputs: {len(out['time']) - 1} steps, energy rows {len(out['energy'])}")
+    np.savez_compressed(HERE / "hematite_outputs.npz", **out)
+    cfg = {"t_final": t_final, "n_steps": int(len(out["time"]) - 1),
+           "output_data": run_p["output_data"]}
+    (HERE / "hematite_outputs.json").write_text(json.dumps(cfg, indent=1))
+
+
 BVO_DOPING = {"num_dopants": [2, 0], "doping_element_map": ["V:W", "V:Mo"],
               "insertion_type": ["manual", "manual"],
               "charge": {"full": {"W": 6.0, "Mo": 6.0}},
@@ -714,6 +747,8 @@ def main(parts):
         example(core, "Hematite", HEMATITE, 1e-4)
     if "every_step" in parts:
         every_step(core)
+    if "hematite_outputs" in parts:
+        hematite_outputs(core)
     if "bvo" in parts:
         example(core, "BVO", BVO, 1e-3)
     if "bvo_doped" in parts:
@@ -725,5 +760,5 @@ def main(parts):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1:] or ["hematite", "every_step", "bvo", "bvo_doped", "corundum324",
-                          "corundum3600", "msd", "ewald_params"])
+    main(sys.argv[1:] or ["hematite", "every_step", "hematite_outputs", "bvo", "bvo_doped",
+                          "corundum324", "corundum3600", "msd", "ewald_params"])

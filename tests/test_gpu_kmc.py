@@ -97,6 +97,29 @@ def test_do_kmc_steps_doped_bvo_matches_reference(cuda_ready):
     assert np.abs(t[1:] / fix["time"][1:] - 1).max() < TIME_RTOL
 
 
+def test_do_kmc_steps_energy_and_delg0_grids_match_reference(cuda_ready):
+    """examples/Hematite, ~2,000 steps with the energy and dG0 path grids
+    written: rows and events bit for bit; energies within 1e-12 relative;
+    dG0 (a difference of ~1 Ha potentials, ~1e-8 Ha here) within 1e-14 Ha."""
+    ref, fix = gio.load("hematite_outputs")
+    cfg, arr, run = _example_run("hematite", t_final=ref["t_final"])
+    d = Path(tempfile.mkdtemp())
+    st = cfg["rnd_state"]
+    with open(d / "initial_rnd_state.dump", "wb") as fh:
+        pickle.dump((st[0], tuple(st[1]), st[2]), fh)
+    od = ref["output_data"]
+    run.do_kmc_steps(d, od, cfg["run"]["random_seed"], "parallel")
+    got = {k: np.load(d / od[k]["file_name"])
+           for k in ("unwrapped_traj", "time", "energy", "delg_0")}
+    assert len(got["time"]) == ref["n_steps"] + 1
+    assert np.array_equal(got["unwrapped_traj"], fix["unwrapped_traj"])
+    assert np.abs(got["time"][1:] / fix["time"][1:] - 1).max() < TIME_RTOL
+    e, er = got["energy"], fix["energy"]
+    assert e.shape == er.shape and np.abs(e - er).max() <= 1e-12 * np.abs(er).max()
+    g, gr = got["delg_0"], fix["delg_0"]
+    assert g.shape == gr.shape and np.abs(g - gr).max() <= 1e-14
+
+
 def _corundum324_engine(cfg, arr):
     import torch
     mat, nb = gio.material(cfg)
