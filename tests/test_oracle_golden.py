@@ -88,6 +88,39 @@ def test_oracle_kmc_reproduces_shipped_trajectory(name):
     assert np.abs(t[1:] / ref[1:] - 1).max() < 1e-12
 
 
+def test_oracle_kmc_reproduces_reference_doped_bvo():
+    """The reference's doped BVO run (two W dopants of charge 6, shell
+    energies from site_indices.npy, the electron drawn onto a dopant site by
+    rnd.sample, core.py:2478-2528, 2723-2772): the oracle, given the
+    reference's doped site energies, reproduces its occupancy list and its
+    unwrapped rows bit for bit and its times within 1e-12."""
+    cfg, arr = gio.load("bvo")
+    ref, fix = gio.load("bvo_doped")
+    mat, nb = gio.material(cfg)
+    tables, ei = _example_tables(cfg, arr, mat, nb)
+    run = cfg["run"]
+    st = cfg["rnd_state"]
+    random.setstate((st[0], tuple(st[1]), st[2]))
+    si = fix["site_indices"]
+    dopants = [int(x) for x in si[si[:, 3] == 0, 0]]
+    occ = random.sample(dopants, 1)  # site_charge_initiation 'yes'
+    n = ref["n_steps"]
+    u = np.array([random.random() for _ in range(2 * n + 2)])
+    n_cells = int(nb.num_cells)
+    q = np.tile(np.array([mat.charge_types["full"][mat.element_types[e]]
+                          for e in mat.element_type_index_list]), n_cells).astype(float)
+    q[dopants] = ref["doping"]["charge"]["full"]["W"]
+    dt = run["time_interval"] * K.SEC2AUTIME
+    n_path = int(ref["t_final"] * K.SEC2AUTIME / dt) + 1
+    out = ko.run(arr["A"], tables, occ, q, -1.0, fix["system_relative_energies"], mat.vn,
+                 run["temp"] * K.K2AUTEMP, u, dt, n_path)
+    assert out["stop"] == "done" and out["steps"] == n
+    assert np.array_equal(np.asarray(out["sites"])[:, 0], fix["occupancy"][1:, 0])
+    assert fix["occupancy"][0, 0] == occ[0]
+    assert np.array_equal(out["unwrapped"], fix["unwrapped"])
+    assert np.abs(out["time"][1:] / fix["time"][1:] - 1).max() < 1e-12
+
+
 def test_oracle_kmc_matches_reference_events_corundum324():
     cfg, arr = gio.load("corundum324")
     mat, nb = gio.material(cfg)
