@@ -615,21 +615,32 @@ __device__ void advance_trajectory(const KmcArgs& a, int64_t t, int g,
   double* csum = st.d_csum ? st.d_csum + t * (int64_t)st.csum_stride : nullptr;
   const int half = st.csum_stride / 2;
 
-  int occ = 0;
-  double disp0 = 0.0, disp1 = 0.0, disp2 = 0.0;
-  double row0 = 0.0, row1 = 0.0, row2 = 0.0;
-  const bool owns_carrier = g < NC;
-  if (owns_carrier) {
-    occ = st.d_occ[t * MC + g];
-    const double* dp = st.d_disp + (t * MC + g) * 3;
-    disp0 = dp[0]; disp1 = dp[1]; disp2 = dp[2];
-    const double* lr = st.d_last_row + (t * MC + g) * 3;
-    row0 = lr[0]; row1 = lr[1]; row2 = lr[2];
+  // The carriers' displacements since the last path row (slot 3c + k:
+  // component k of carrier c), their path-row values and the energy (slot
+  // 3 NC) are spread over the lanes: lane g holds slots g + G r, r < 4
+  // (3 NC + 1 <= 4 G).  A step's additions (the moved carrier's three
+  // components and the energy) then take ceil((3 NC + 1) / G) FP64
+  // instructions instead of four.  Every value gets the same additions in
+  // the same order; a slot a step does not touch adds +0, which is exact
+  // (none of these sums is -0).
+  constexpr int kSlotRegs = 4;
+  const int n_disp = 3 * NC;
+  const int n_regs = (n_disp + 1 + G - 1) / G;
+  const int64_t sbase = t * 3 * (int64_t)MC;
+  int occ = (g < NC) ? st.d_occ[t * MC + g] : 0;
+  double dacc[kSlotRegs], racc[kSlotRegs];
+  {
+    const double e0 = st.d_energy ? st.d_energy[t] : 0.0;
+#pragma unroll
+    for (int r = 0; r < kSlotRegs; ++r) {
+      const int j = g + G * r;
+      dacc[r] = (j < n_disp) ? st.d_disp[sbase + j] : (j == n_disp ? e0 : 0.0);
+      racc[r] = (j < n_disp) ? st.d_last_row[sbase + j] : 0.0;
+    }
   }
   double sim_time = st.d_time[t];
   int64_t step = st.d_step[t];
   int64_t start_path = st.d_path_index[t];
-  double energy = st.d_energy ? st.d_energy[t] : 0.0;
   int64_t ucur = st.d_u_cursor ? st.d_u_cursor[t] : 0;
   const int64_t step_limit = st.d_step_limit ? st.d_step_limit[t] : INT64_MAX;
   const double* ubase = a.rng.d_uniforms
@@ -783,21 +794,29 @@ __device__ void advance_trajectory(const KmcArgs& a, int64_t t, int g,
     }
 
     // ---- state update (core.py:2810-2830) -----------------------------
-    if (g == c_sel) {
-      occ = n_sel;
+    {
       const double* hv = sy.d_hop + ((int64_t)o_sel * S + s_sel) * 3;
       const double h0 = __ldg(hv), h1 = __ldg(hv + 1), h2 = __ldg(hv + 2);
-      disp0 = dadd(disp0, h0);
-      disp1 = dadd(disp1, h1);
-      disp2 = dadd(disp2, h2);
-      if (a.out.d_drift) {
-        double* dr = a.out.d_drift + ((int64_t)t * MC + g) * 3;
-        dr[0] = dadd(dr[0], dmul(h0, k_sel));
-        dr[1] = dadd(dr[1], dmul(h1, k_sel));
-        dr[2] = dadd(dr[2], dmul(h2, k_sel));
+      if (g == c_sel) {
+        occ = n_sel;
+        if (a.out.d_drift) {
+          double* dr = a.out.d_drift + ((int64_t)t * MC + g) * 3;
+          dr[0] = dadd(dr[0], dmul(h0, k_sel));
+          dr[1] = dadd(dr[1], dmul(h1, k_sel));
+          dr[2] = dadd(dr[2], dmul(h2, k_sel));
+        }
+      }
+      const int j0 = 3 * c_sel;
+#pragma unroll
+      for (int r = 0; r < kSlotRegs; ++r) {
+        if (r < n_regs) {
+          const int j = g + G * r;
+          const double v = (j == j0) ? h0 : (j == j0 + 1) ? h1 : (j == j0 + 2) ? h2
+                         : (j == n_disp) ? de_sel : 0.0;
+          dacc[r] = dadd(dacc[r], v);
+        }
       }
     }
-    energy = dadd(energy, de_sel);
     if (g == 0 && a.out.d_step_time) {
       const int64_t col = step - a.out.step_offset;
       if (col >= 0 && col < a.out.step_capacity) {
@@ -829,21 +848,24 @@ __device__ void advance_trajectory(const KmcArgs& a, int64_t t, int g,
     // ---- path-grid rows (core.py:2847-2861) ---------------------------
     if (end_path >= start_path + 1) {
       if (end_path >= n_path) end_path = n_path;
-      if (owns_carrier) {
-        row0 = dadd(row0, disp0);
-        row1 = dadd(row1, disp1);
-        row2 = dadd(row2, disp2);
-        if (unw) {
-          for (int64_t r = start_path; r < end_path; ++r) {
-            double* rp = unw + r * row_len + 3 * g;
-            rp[0] = row0; rp[1] = row1; rp[2] = row2;
-          }
+#pragma unroll
+      for (int q = 0; q < kSlotRegs; ++q) {
+        const int j = g + G * q;
+        if (q < n_regs && j < n_disp) {
+          racc[q] = dadd(racc[q], dacc[q]);
+          dacc[q] = 0.0;
+          if (unw)
+            for (int64_t r = start_path; r < end_path; ++r) unw[r * row_len + j] = racc[q];
         }
-        disp0 = disp1 = disp2 = 0.0;
       }
       if (a.out.d_energy_grid) {
+        double en = 0.0;
+#pragma unroll
+        for (int q = 0; q < kSlotRegs; ++q)
+          if (q == n_disp / G) en = dacc[q];
+        en = gshfl<G>(gmask, en, n_disp % G);
         double* eg = a.out.d_energy_grid + (int64_t)t * n_path;
-        for (int64_t r = start_path + g; r < end_path; r += G) eg[r] = energy;
+        for (int64_t r = start_path + g; r < end_path; r += G) eg[r] = en;
       }
       start_path = end_path;
       t_guard = dmul(dmul((double)(start_path + 1), dt_grid), 1.0 - 0x1p-40);
@@ -861,18 +883,21 @@ __device__ void advance_trajectory(const KmcArgs& a, int64_t t, int g,
       if (pc.valid[j]) { csum[p] = pc.P[j]; csum[half + p] = pc.Q[j]; }
     }
   }
-  if (owns_carrier) {
-    st.d_occ[t * MC + g] = occ;
-    double* dp = st.d_disp + (t * MC + g) * 3;
-    dp[0] = disp0; dp[1] = disp1; dp[2] = disp2;
-    double* lr = st.d_last_row + (t * MC + g) * 3;
-    lr[0] = row0; lr[1] = row1; lr[2] = row2;
+  if (g < NC) st.d_occ[t * MC + g] = occ;
+#pragma unroll
+  for (int q = 0; q < kSlotRegs; ++q) {
+    const int j = g + G * q;
+    if (j < n_disp) {
+      st.d_disp[sbase + j] = dacc[q];
+      st.d_last_row[sbase + j] = racc[q];
+    } else if (j == n_disp && st.d_energy) {
+      st.d_energy[t] = dacc[q];
+    }
   }
   if (g == 0) {
     st.d_time[t] = sim_time;
     st.d_step[t] = step;
     st.d_path_index[t] = start_path;
-    if (st.d_energy) st.d_energy[t] = energy;
     if (st.d_u_cursor) st.d_u_cursor[t] = ucur;
     st.d_status[t] = status;
   }
