@@ -204,7 +204,9 @@ __device__ void advance_trajectory_cta(const KmcArgs& a, int64_t t, CtaShared& s
   double t_guard = dmul(dmul((double)(start_path + 1), dt_grid), 1.0 - 0x1p-40);
   TimeChain<32> tc;
   tc.reset(t_guard, sim_time);
-  const bool exact_each_step = a.out.d_step_time != nullptr;
+  // per-step log: warp 0 stores each step's time when its chain flushes
+  double* tlog = (w == 0 && a.out.d_step_time)
+                     ? a.out.d_step_time + (int64_t)t * a.out.step_capacity : nullptr;
   double pre_u1 = 0.0, pre_lu2 = 0.0;
   int64_t pre_base = -33;
 
@@ -358,8 +360,8 @@ __device__ void advance_trajectory_cta(const KmcArgs& a, int64_t t, CtaShared& s
     if (sel >= NP) { status = PYCD_TRAJ_NO_EVENT; break; }
 
     // ---- residence time (every warp, identical values) -------------------
-    const bool exact = tc.push(l, ktot, lu2, exact_each_step);
-    if (exact) tc.flush(l, full, sim_time);
+    const bool exact = tc.push(l, ktot, lu2, false, step - a.out.step_offset);
+    if (exact) tc.flush(l, full, sim_time, tlog, a.out.step_capacity);
     int64_t end_path = start_path - 1;
     if (exact && !nonneg_gt(t_guard, sim_time)) {
       const double tq = ddiv(sim_time, dt_grid);
@@ -389,12 +391,10 @@ __device__ void advance_trajectory_cta(const KmcArgs& a, int64_t t, CtaShared& s
       }
     }
     energy = dadd(energy, de_sel);
-    if (g == 0 && a.out.d_step_time) {
+    if (g == 0 && a.out.d_step_proc) {
       const int64_t col = step - a.out.step_offset;
-      if (col >= 0 && col < a.out.step_capacity) {
-        a.out.d_step_time[(int64_t)t * a.out.step_capacity + col] = sim_time;
+      if (col >= 0 && col < a.out.step_capacity)
         a.out.d_step_proc[(int64_t)t * a.out.step_capacity + col] = sel;
-      }
     }
     ++step;
     if (ubase) ucur += 2;
@@ -449,7 +449,7 @@ __device__ void advance_trajectory_cta(const KmcArgs& a, int64_t t, CtaShared& s
     if (end_path >= n_path) { status = PYCD_TRAJ_DONE; break; }
     if (exact) tc.reset(t_guard, sim_time);
   }
-  if (tc.npend > 0) tc.flush(l, full, sim_time);
+  if (tc.npend > 0) tc.flush(l, full, sim_time, tlog, a.out.step_capacity);
 
   if (csum) {
 #pragma unroll

@@ -543,6 +543,7 @@ __device__ __forceinline__ float f32_below(double x) {
 template <int G>
 struct TimeChain {
   double kt = 1.0, nlu2 = 0.0;  // this lane's pending step: k_tot, log(u2)
+  int64_t col = -1;             // and its column in a per-step time log
   int npend = 0;
   float bound = 0.0f, slack = -1.0f;
 
@@ -558,9 +559,11 @@ struct TimeChain {
     const double gap = dsub(dsub(t_guard, t), m);
     if (__double_as_longlong(gap) > 0) slack = f32_below(gap);
   }
-  // record this step; true when the exact time is needed now
-  __device__ __forceinline__ bool push(int g, double ktot, double lu2, bool force) {
-    if (g == npend) { kt = ktot; nlu2 = lu2; }
+  // record this step (c: its column in a per-step time log); true when the
+  // exact time is needed now
+  __device__ __forceinline__ bool push(int g, double ktot, double lu2, bool force,
+                                       int64_t c) {
+    if (g == npend) { kt = ktot; nlu2 = lu2; col = c; }
     ++npend;
     // -lu2 / ktot <= above(-lu2) / below(ktot), rounded up, with room for
     // the rounding of the double quotient
@@ -569,13 +572,22 @@ struct TimeChain {
     bound = __fadd_ru(bound, inc);
     return force || npend == G || !(bound < slack);
   }
-  __device__ __forceinline__ void flush(int g, unsigned gmask, double& t) {
+  // apply the pending steps in step order; with a log row, lane j stores
+  // the time after its step (the reference's value at that step) in its
+  // column, when the column is inside [0, cap)
+  __device__ __forceinline__ void flush(int g, unsigned gmask, double& t,
+                                        double* log_row = nullptr, int64_t cap = 0) {
     const double q = (g < npend) ? ddiv(nlu2, kt) : 0.0;
+    double mine = 0.0;
 #pragma unroll
     for (int j = 0; j < G; ++j) {
       const double qj = gshfl<G>(gmask, q, j);
-      if (j < npend) t = dsub(t, qj);
+      if (j < npend) {
+        t = dsub(t, qj);
+        if (g == j) mine = t;
+      }
     }
+    if (log_row && g < npend && col >= 0 && col < cap) log_row[col] = mine;
     npend = 0;
   }
 };
@@ -660,8 +672,10 @@ __device__ void advance_trajectory(const KmcArgs& a, int64_t t, int g,
   double t_guard = dmul(dmul((double)(start_path + 1), dt_grid), 1.0 - 0x1p-40);
   TimeChain<G> tc;
   tc.reset(t_guard, sim_time);
-  // per-step times are an output: keep the chain exact every step
-  const bool exact_each_step = a.out.d_step_time != nullptr;
+  // per-step log: the event is stored at its step, its time when the chain
+  // is next made exact (the flush stores each pending step's time)
+  double* tlog = a.out.d_step_time
+                     ? a.out.d_step_time + (int64_t)t * a.out.step_capacity : nullptr;
 
   // uniforms of steps pre_base + g, prepared G at a time
   double pre_u1 = 0.0, pre_lu2 = 0.0;
@@ -762,8 +776,8 @@ __device__ void advance_trajectory(const KmcArgs& a, int64_t t, int g,
     if (sel >= NP) { status = PYCD_TRAJ_NO_EVENT; break; }
 
     // ---- residence time (core.py:2802-2804) ---------------------------
-    const bool exact = tc.push(g, ktot, lu2, exact_each_step);
-    if (exact) tc.flush(g, gmask, sim_time);
+    const bool exact = tc.push(g, ktot, lu2, false, step - a.out.step_offset);
+    if (exact) tc.flush(g, gmask, sim_time, tlog, a.out.step_capacity);
     int64_t end_path = start_path - 1;
     // without a flush sim_time < t_guard is guaranteed by the bound
     if (exact && !nonneg_gt(t_guard, sim_time)) {  // sim_time >= t_guard, both >= +0
@@ -817,12 +831,10 @@ __device__ void advance_trajectory(const KmcArgs& a, int64_t t, int g,
         }
       }
     }
-    if (g == 0 && a.out.d_step_time) {
+    if (g == 0 && a.out.d_step_proc) {
       const int64_t col = step - a.out.step_offset;
-      if (col >= 0 && col < a.out.step_capacity) {
-        a.out.d_step_time[(int64_t)t * a.out.step_capacity + col] = sim_time;
+      if (col >= 0 && col < a.out.step_capacity)
         a.out.d_step_proc[(int64_t)t * a.out.step_capacity + col] = sel;
-      }
     }
     ++step;
     if (ubase) ucur += 2;
@@ -873,7 +885,7 @@ __device__ void advance_trajectory(const KmcArgs& a, int64_t t, int g,
     if (end_path >= n_path) { status = PYCD_TRAJ_DONE; break; }
     if (exact) tc.reset(t_guard, sim_time);
   }
-  if (tc.npend > 0) tc.flush(g, gmask, sim_time);
+  if (tc.npend > 0) tc.flush(g, gmask, sim_time, tlog, a.out.step_capacity);
 
   // ---- write the state back ---------------------------------------------
   if (csum) {

@@ -315,11 +315,11 @@ def test_event_stream_independent_of_launch_shape(cuda_ready):
 
 
 def test_deferred_times_equal_exact_chain_across_shapes(cuda_ready):
-    """Without per-step time output the kernel defers the residence-time
-    divisions (bounded in FP32, exact FP64 chain at grid crossings and every
-    G steps).  On a fine time grid (a crossing every ~50 steps) the rows,
-    energies, final times and sites must equal the every-step exact chain
-    bit for bit, for every launch shape."""
+    """The kernel defers the residence-time divisions (bounded in FP32, the
+    exact FP64 chain at possible grid crossings and every G steps; a per-step
+    time log is filled at each flush).  On a fine time grid (a crossing every
+    ~50 steps) the rows, energies, final times and sites must be equal bit
+    for bit for every launch shape, with and without a per-step log."""
     import torch
     cfg, arr = gio.load("corundum324")
     mat, nb = gio.material(cfg)
