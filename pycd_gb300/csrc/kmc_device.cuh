@@ -6,8 +6,9 @@
 // (G = 1..32, a power of two); a warp holds 32/G trajectories.  Process p of
 // a trajectory is (carrier c = p / S, slot s = p % S), the reference's order
 // (core.py:1946-1987).  Lane g owns the contiguous processes
-// p = g*MAXP + j (j < MAXP) and carrier g (its site, its displacement
-// accumulator and its path-row values); G*MAXP >= n_carriers * S.
+// p = g*MAXP + j (j < MAXP) and carrier g's site; G*MAXP >= n_carriers * S.
+// The carriers' displacement and path-row values and the energy are spread
+// over the lanes by slot (component k of carrier c is slot 3c + k).
 //
 // Arithmetic.  GB300 issues ~2 DFMA/clk/SM: one FP64 unit per SM
 // sub-partition, which a warp's FP64 instruction holds for 64 cycles
