@@ -121,6 +121,46 @@ def test_oracle_kmc_reproduces_reference_doped_bvo():
     assert np.abs(out["time"][1:] / fix["time"][1:] - 1).max() < 1e-12
 
 
+def test_oracle_energy_and_delg0_grids_match_reference_hematite():
+    """The reference's Hematite run with the energy and dG0 path grids
+    written (initial energy core.py:2663-2667; grids 2806-2808, 2848-2861):
+    the oracle reproduces its rows bit for bit, its energies within 1e-12
+    relative and its dG0 within 1e-14 Ha."""
+    cfg, arr = gio.load("hematite")
+    ref, fix = gio.load("hematite_outputs")
+    mat, nb = gio.material(cfg)
+    tables, ei = _example_tables(cfg, arr, mat, nb)
+    run = cfg["run"]
+    st = cfg["rnd_state"]
+    random.setstate((st[0], tuple(st[1]), st[2]))
+    n_cells = int(nb.num_cells)
+    tpc = mat.total_elements_per_unit_cell
+    head = mat.n_elements_per_unit_cell[:ei].sum()
+    sites = sorted(int(head + e + c * tpc) for c in range(n_cells)
+                   for e in range(mat.n_elements_per_unit_cell[ei]))
+    occ = random.sample(sites, 1)
+    n = ref["n_steps"]
+    u = np.array([random.random() for _ in range(2 * n + 2)])
+    q = np.tile(np.array([mat.charge_types["full"][mat.element_types[e]]
+                          for e in mat.element_type_index_list]), n_cells).astype(float)
+    # initial energy as the reference forms it: neutralising background plus
+    # the pair sum over the charges with the carrier
+    g = _geom(cfg, mat)
+    qc = q.reshape(-1, 1).copy()
+    qc[occ[0]] += -1.0
+    ewald_neut = -(np.pi * 1.0 ** 2 / (2 * g["vol"] * g["alpha"]))
+    energy0 = ewald_neut + np.sum(np.multiply(np.multiply(qc.transpose(), qc), arr["A"]))
+    dt = run["time_interval"] * K.SEC2AUTIME
+    n_path = int(ref["t_final"] * K.SEC2AUTIME / dt) + 1
+    out = ko.run(arr["A"], tables, occ, q, -1.0, np.zeros(nb.num_system_elements), mat.vn,
+                 run["temp"] * K.K2AUTEMP, u, dt, n_path, energy0=energy0)
+    assert out["stop"] == "done" and out["steps"] == n
+    assert np.array_equal(out["unwrapped"], fix["unwrapped_traj"])
+    e, er = out["energy"], fix["energy"]
+    assert np.abs(e - er).max() <= 1e-12 * np.abs(er).max()
+    assert np.abs(out["delg0"] - fix["delg_0"]).max() <= 1e-14
+
+
 def test_oracle_kmc_matches_reference_events_corundum324():
     cfg, arr = gio.load("corundum324")
     mat, nb = gio.material(cfg)
