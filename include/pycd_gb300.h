@@ -24,8 +24,13 @@
  *     Launches are asynchronous on that stream unless stated otherwise.
  *   - Units are Hartree atomic units (bohr, Hartree, a.u. time), as in PyCD.
  *   - Thread safety: distinct calls on distinct streams and buffers are
- *     independent; the library keeps no global mutable state except the
- *     per-thread error string.
+ *     independent.  Global state: the per-thread error string; per device,
+ *     the exp tables of the KMC kernels (filled once, then read-only) and
+ *     the fixed scratch array of pycd_ewald_build_noalloc, which every call
+ *     of that entry point shares (overlapping calls race).  Per-device state
+ *     is kept for device ordinals below 64.  The library is not usable
+ *     across a cudaDeviceReset: the reset reloads its device arrays while
+ *     the host-side records of them stay.
  */
 #ifndef PYCD_GB300_H
 #define PYCD_GB300_H
@@ -156,8 +161,9 @@ PYCD_API int pycd_ewald_build(const PycdEwaldDesc* desc, int mode, double* d_out
  * the GPU's memory.  The scratch (per-k constants and N x 2K feature rows,
  * 8 * (5K + N * 2K) bytes rounded up) lives in a fixed 32 MiB device array
  * inside the library, reserved on every GPU that loads it until the process
- * exits; larger (N, K) are rejected with PYCD_ERR_WORKSPACE.  The caller
- * still passes the descriptor's input buffers and d_out.
+ * exits; larger (N, K) are rejected with PYCD_ERR_WORKSPACE.  K counts only
+ * when desc->parts includes the Fourier part.  The caller still passes the
+ * descriptor's input buffers and d_out.
  *   - The first call on a device resolves the array's device address with
  *     that device current; make that first call before any stream capture.
  *   - Every call uses the same array: calls whose work overlaps on the GPU

@@ -126,7 +126,9 @@ class System(EwaldParameterSearch):
         'simulation_cell') first runs get_ewald_parameters, whose energy scans
         run on the GPU, and may move dst_path as the reference does.  The
         report keeps the reference's lines (alpha on line 4, which
-        material_run reads) and adds the k-vector count and build mode."""
+        material_run reads) and adds the k-vector count and build mode.
+        ``return_k_vector_data`` also writes the per-k energy log
+        (k_vector_data_report)."""
         import torch
         a2b = constants.ANG2BOHR
         if self._user_specified():
@@ -182,9 +184,38 @@ class System(EwaldParameterSearch):
                   f"build: {info['mode']} on the GPU\n\n"]
         if dst_path is not None:
             Path(dst_path).mkdir(parents=True, exist_ok=True)
+            if return_k_vector_data:
+                self.k_vector_data_report(dst_path, alpha, k_cut)
             generate_report(self.start_time, Path(dst_path), "precomputed_array",
                             1, "".join(lines))
         return (A, dst_path)
+
+    def k_vector_data_report(self, dst_path, alpha, k_cut):
+        """The ``return_k_vector_data`` branch of get_precomputed_array
+        (PyCD/core.py:1626-1653, pot_k_ewald_with_k_vector_data at
+        core.py:880-911): the energy contribution of every half-space
+        k-vector of the k_max box for the 'full' lattice charges (zero for
+        those outside k_cut), sorted in decreasing order into
+        ``k_vector_energy_contribution_within_user_specified_k_cut.log``.
+        Each contribution is one device pass over the pairs per k-vector
+        (``pycd_ewald_kvector_energies``).  Returns (k-vectors, contributions)
+        in the reference's unsorted k order."""
+        from .ewald import half_space_k_vectors, k_max_for
+        kv, keep = half_space_k_vectors(self.reciprocal_lattice_matrix,
+                                        k_max_for(self, k_cut), k_cut)
+        contrib = np.zeros(len(kv))
+        if keep.any():
+            contrib[keep] = self._energy_evaluator("full").k_vectors(alpha, kv[keep])
+        order = np.argsort(contrib)[::-1]
+        eh = constants.EV2HARTREE
+        lines = ["k-vectors sorted in the decreasing order of their energy contributions\n"]
+        lines += [f"{k[0]:4d} {k[1]:4d} {k[2]:4d}: {e / eh:.3e} eV\n"
+                  for k, e in zip(kv[order].tolist(), contrib[order])]
+        generate_report(self.start_time, Path(dst_path),
+                        "k_vector_energy_contribution_within_user_specified_k_cut", 0,
+                        "".join(lines))
+        print("Finished k-vector analysis")
+        return kv, contrib
 
 
 class Run(object):

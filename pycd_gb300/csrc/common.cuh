@@ -21,6 +21,11 @@ void clear_error();
 // Map a CUDA error to PYCD_ERR_CUDA with context text.
 int cuda_fail(cudaError_t e, const char* what, const char* file, int line);
 
+// Per-device state (the exp tables, the fixed no-alloc scratch address) is
+// kept for device ordinals below this bound; higher ordinals are rejected
+// with PYCD_ERR_INVALID_ARG by every entry point that needs such state.
+constexpr int kMaxDevices = 64;
+
 }  // namespace pycd
 
 #define PYCD_CUDA(call)                                                    \

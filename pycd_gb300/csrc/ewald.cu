@@ -510,7 +510,15 @@ int ewald_build(const PycdEwaldDesc* d, int mode, double* out, void* ws,
     inv.m[c] = d->sim_cell_inv[c];
   }
   const double coeff = 2.0 * M_PI / d->volume;
-  cudaEvent_t e0 = nullptr, e1 = nullptr, e2 = nullptr;
+  // timing events, released on every return path
+  struct Events {
+    cudaEvent_t e[3] = {nullptr, nullptr, nullptr};
+    ~Events() {
+      for (cudaEvent_t ev : e)
+        if (ev) cudaEventDestroy(ev);
+    }
+  } ev;
+  cudaEvent_t &e0 = ev.e[0], &e1 = ev.e[1], &e2 = ev.e[2];
   const bool timing = real_ms || fourier_ms;
   if (timing) {
     PYCD_CUDA(cudaEventCreate(&e0));
@@ -577,9 +585,6 @@ int ewald_build(const PycdEwaldDesc* d, int mode, double* out, void* ws,
     PYCD_CUDA(cudaEventElapsedTime(&b, e1, e2));
     if (real_ms) *real_ms = a;
     if (fourier_ms) *fourier_ms = b;
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
-    cudaEventDestroy(e2);
   }
   return PYCD_OK;
 }
@@ -600,8 +605,9 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratch
 
 // Host code cannot use &g_noalloc_scratch as a device address (it names a
 // host-side stand-in), so the address is resolved once per device with that
-// device current and cached here.
-constexpr int kMaxDevices = 64;
+// device current and cached here.  A cudaDeviceReset reloads the module and
+// may move the array, leaving the cached address stale: the library is not
+// usable across a device reset.
 static void* g_noalloc_ptr[kMaxDevices] = {nullptr};
 static std::mutex g_noalloc_mutex;
 
@@ -713,12 +719,17 @@ extern "C" int pycd_ewald_build_noalloc(const PycdEwaldDesc* desc, double* d_out
   PYCD_REQUIRE(d_out != nullptr, "d_out is NULL");
   int rc = ewald_validate(desc, PYCD_EWALD_FP64_GEMM);
   if (rc) return rc;
-  const size_t need = ewald_workspace_bytes(desc, PYCD_EWALD_FP64_GEMM);
+  // a build without the Fourier part uses no k-vectors and needs scratch
+  // for none of them
+  PycdEwaldDesc eff = *desc;
+  const int parts = eff.parts ? eff.parts : PYCD_EWALD_PART_ALL;
+  if (!(parts & PYCD_EWALD_PART_FOURIER)) eff.n_kvec = 0;
+  const size_t need = ewald_workspace_bytes(&eff, PYCD_EWALD_FP64_GEMM);
   if (need > kNoAllocScratchBytes) {
     set_error("pycd_ewald_build_noalloc: N=%lld with K=%lld needs %zu bytes of "
               "scratch; the fixed scratch holds %zu bytes (use pycd_ewald_build "
               "with a workspace)",
-              (long long)desc->n_sites, (long long)desc->n_kvec, need,
+              (long long)eff.n_sites, (long long)eff.n_kvec, need,
               kNoAllocScratchBytes);
     return PYCD_ERR_WORKSPACE;
   }
@@ -728,6 +739,6 @@ extern "C" int pycd_ewald_build_noalloc(const PycdEwaldDesc* desc, double* d_out
   // Nothing in the scratch needs clearing: each call writes every byte it
   // later reads (per-k constants, then all feature rows including padding)
   // before reading it.
-  return ewald_build(desc, PYCD_EWALD_FP64_GEMM, d_out, scratch,
+  return ewald_build(&eff, PYCD_EWALD_FP64_GEMM, d_out, scratch,
                      kNoAllocScratchBytes, (cudaStream_t)stream, nullptr, nullptr);
 }

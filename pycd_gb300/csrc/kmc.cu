@@ -38,17 +38,20 @@ void exp_table_host(double2* out) {
 }
 
 // Fill the exp table of every KMC translation unit on the current device
-// (once per device).
+// (once per device; device ordinals >= kMaxDevices are rejected).  A
+// cudaDeviceReset zeroes the tables without clearing this record: the
+// library is not usable across a device reset.
 int kmc_exp_init() {
   static std::mutex mu;
-  static bool done[64] = {false};
+  static bool done[kMaxDevices] = {false};
   static double2 host[4096];
   static bool built = false;
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice", __FILE__, __LINE__);
+  PYCD_REQUIRE(dev >= 0 && dev < kMaxDevices, "device ordinal %d out of range", dev);
   std::lock_guard<std::mutex> lock(mu);
-  if (dev >= 0 && dev < 64 && done[dev]) return PYCD_OK;
+  if (done[dev]) return PYCD_OK;
   if (!built) {
     exp_table_host(host);
     built = true;
@@ -57,7 +60,7 @@ int kmc_exp_init() {
   if (e == cudaSuccess) e = kmc_exp_upload_capped(host);
   if (e == cudaSuccess) e = kmc_exp_upload_cta(host);
   if (e != cudaSuccess) return cuda_fail(e, "exp table upload", __FILE__, __LINE__);
-  if (dev >= 0 && dev < 64) done[dev] = true;
+  done[dev] = true;
   return PYCD_OK;
 }
 

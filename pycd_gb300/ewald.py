@@ -21,14 +21,16 @@ def k_max_for(system, k_cut):
     return np.ceil(k_cut / system.reciprocal_lattice_vector_length).astype(int)
 
 
-def effective_k_vectors(recip, k_max, k_cut):
-    """Half-space integer k list kept by the reference, in its order.
+def half_space_k_vectors(recip, k_max, k_cut):
+    """(k, keep): every half-space integer k-vector of the k_max box in the
+    reference's order (get_effective_k_vectors, PyCD/core.py:816-838) and the
+    mask of those with k^2 < k_cut^2 (core.py:868).
 
     The grid [-k_max, k_max]^3 in C order with the first member of every +-m
-    pair kept is exactly the set of points before the origin; the filter is
-    k^2 < k_cut^2 with k = m . recip.  k^2 is compared vectorised and every
-    vector within rounding of the cut is re-evaluated with the reference's
-    per-vector ``np.dot`` so the kept set is the reference's.
+    pair kept is exactly the set of points before the origin.  k^2 is
+    compared vectorised and every vector within rounding of the cut is
+    re-evaluated with the reference's per-vector ``np.dot`` so the kept set
+    is the reference's.
     """
     k_max = np.asarray(k_max, dtype=int)
     g = np.mgrid[-k_max[0]:k_max[0] + 1, -k_max[1]:k_max[1] + 1,
@@ -42,7 +44,14 @@ def effective_k_vectors(recip, k_max, k_cut):
     for i in np.nonzero(near)[0]:
         kk = np.dot(half[i], recip)
         keep[i] = np.dot(kk, kk) < kc2
-    return np.ascontiguousarray(half[keep].astype(np.int32))
+    return np.ascontiguousarray(half.astype(np.int32)), keep
+
+
+def effective_k_vectors(recip, k_max, k_cut):
+    """Half-space integer k list kept by the reference, in its order: the
+    k-vectors of ``half_space_k_vectors`` inside the cut."""
+    half, keep = half_space_k_vectors(recip, k_max, k_cut)
+    return np.ascontiguousarray(half[keep])
 
 
 def pmiv_is_lattice_consistent(system, pmiv, tol=1e-8):

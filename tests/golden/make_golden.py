@@ -1,9 +1,9 @@
 """Generate the golden fixtures under tests/golden/ from the reference PyCD.
 
-Run in a container where the reference checkout exists (default
-/root/reference, or $PYCD_REFERENCE):
+Run where a checkout of the reference exists, with $PYCD_REFERENCE naming
+its root directory (the one holding PyCD/ and examples/):
 
-    python tests/golden/make_golden.py
+    PYCD_REFERENCE=<reference checkout> python tests/golden/make_golden.py [parts]
 
 The reference is imported with test-only shims (stub matplotlib / yaml
 modules, ``np.in1d = np.isin``, a ragged-list ``asarray`` for multi-element
@@ -31,6 +31,13 @@ produced by the reference's code or ships with it:
       shipped pmiv) and the 'converge' k_cut scan of the unit cell (its pmiv
       from the reference): the choices, the report lines after the timing
       lines, and the k_cut convergence / k-vector contribution logs.
+  kvector_data.json
+      get_precomputed_array(dst, 0, 1) of the reference on the Hematite
+      example (2x2x1, shipped pmiv, its own alpha / r_cut / k_cut): the
+      k_vector_energy_contribution_within_user_specified_k_cut.log it writes
+      (every half-space k-vector of the k_max box, sorted by decreasing
+      energy contribution, zero outside k_cut) and the k_max / k-vector
+      count lines of precomputed_array.log.
   msd.json/.npz
       Analysis.compute_msd of the reference on the shipped Hematite
       trajectory (examples/Hematite/traj1, with the example's MSD parameters)
@@ -52,7 +59,7 @@ import numpy as np
 
 HERE = Path(__file__).resolve().parent
 REPO = HERE.parent.parent
-REF = Path(os.environ.get("PYCD_REFERENCE", "/root/reference"))
+REF = Path(os.environ["PYCD_REFERENCE"]) if os.environ.get("PYCD_REFERENCE") else None
 
 
 # ---------------------------------------------------------------- shims
@@ -737,8 +744,45 @@ def ewald_params(core):
     (HERE / "ewald_params.json").write_text(json.dumps(cfg, indent=1))
 
 
+def kvector_data(core):
+    """get_precomputed_array(dst, compute_energy_contributions=0,
+    return_k_vector_data=1) of the reference (core.py:1611-1679) on the
+    Hematite example: the sorted per-k energy contributions it logs and the
+    array it returns (checked against the shipped one)."""
+    name, params = "Hematite", HEMATITE
+    ex = REF / "examples" / name
+    poscar = (ex / "InputFiles" / "POSCAR").read_text()
+    tmp = tempfile.mkdtemp()
+    mat, nb = material_objects(core, params, poscar, [2, 2, 1], [1, 1, 1], tmp)
+    hop = np.load(ex / "InputFiles" / "hop_neighbor_list.npy", allow_pickle=True)[()]
+    pmiv = np.load(ex / "InputFiles" / "pairwise_min_image_vector_data.npy")
+    A_shipped = np.load(ex / "InputFiles" / "precomputed_array.npy")
+    system = make_system(core, mat, nb, hop, pmiv, params)
+    dst = Path(tmp) / "InputFiles"
+    dst.mkdir(parents=True, exist_ok=True)
+    t0 = time.time()
+    A, _ = system.get_precomputed_array(dst, 0, 1)
+    dt = time.time() - t0
+    err = float(np.abs(A - A_shipped).max())
+    print(f"kvector_data: {dt:.1f} s, array vs shipped max |dA| = {err:.3e} Ha")
+    assert err < 1e-15
+    log = (dst / "k_vector_energy_contribution_within_user_specified_k_cut.log").read_text()
+    report = (dst / "precomputed_array.log").read_text().split("Time elapsed")[0]
+    tail = [l + "\n" for l in report.splitlines()
+            if l.startswith(("k_max:", "number of k-vectors:"))]
+    cfg = {"system_size": [2, 2, 1],
+           "params": {k: params[k] for k in ("alpha", "r_cut", "k_cut")},
+           "kvector_log": log, "report_lines": tail, "reference_seconds": dt,
+           "array_vs_shipped_max_abs_ha": err}
+    (HERE / "kvector_data.json").write_text(json.dumps(cfg, indent=1))
+
+
 def main(parts):
+    if REF is None:
+        raise SystemExit("set PYCD_REFERENCE to the root of a reference checkout")
     core = install_shims()
+    if "kvector_data" in parts:
+        kvector_data(core)
     if "ewald_params" in parts:
         ewald_params(core)
     if "msd" in parts:
@@ -761,4 +805,4 @@ def main(parts):
 
 if __name__ == "__main__":
     main(sys.argv[1:] or ["hematite", "every_step", "hematite_outputs", "bvo", "bvo_doped",
-                          "corundum324", "corundum3600", "msd", "ewald_params"])
+                          "corundum324", "corundum3600", "msd", "ewald_params", "kvector_data"])

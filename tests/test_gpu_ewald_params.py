@@ -9,6 +9,7 @@ import numpy as np
 import pytest
 
 import golden_io as gio
+from pycd_gb300 import constants as K
 from pycd_gb300.core import System
 
 pytestmark = pytest.mark.gpu
@@ -140,3 +141,26 @@ def test_fourier_energy_from_per_k_cache_equals_build(cuda_ready):
         via_cache = ev.fourier(sysm.alpha, k_cut)
         via_build = ev._energy(sysm.alpha, 0.0, k_cut, 2)
         assert abs(via_cache - via_build) <= 1e-12 * max(abs(via_build), 1e-300)
+
+
+def test_return_k_vector_data_matches_reference(cuda_ready, tmp_path):
+    """get_precomputed_array(dst, 0, 1) on the Hematite example writes the
+    reference's k_vector_energy_contribution_within_user_specified_k_cut.log
+    (PyCD/core.py:1626-1653): the same k-vectors with the same contributions
+    (ties compared as a set), sorted in decreasing order, and returns the
+    shipped array."""
+    ref = json.loads((gio.GOLDEN / "kvector_data.json").read_text())
+    cfg, arr = gio.load("hematite")
+    mat, nb = gio.material(cfg)
+    p = ref["params"]
+    sysm = System(mat, nb, gio.hop_list(cfg, arr), arr["pmiv"], p["alpha"], p["r_cut"],
+                  p["k_cut"])
+    dst = tmp_path / "InputFiles"
+    A, _ = sysm.get_precomputed_array(dst, 0, 1)
+    assert np.abs(A - arr["A"]).max() < 1e-10 * K.EV2HARTREE  # 1e-10 eV
+    got = (dst / "k_vector_energy_contribution_within_user_specified_k_cut.log").read_text()
+    assert "Time elapsed" not in got
+    _same_contributions(got, ref["kvector_log"])
+    log = (dst / "precomputed_array.log").read_text()
+    for line in ref["report_lines"]:
+        assert line in log

@@ -125,6 +125,31 @@ def test_k_vectors_match_oracle(name):
     assert np.array_equal(np.frombuffer(buf, np.int32).reshape(-1, 3), ours)
 
 
+def test_half_space_k_vectors_match_reference_k_vector_log():
+    """The k-vectors listed by the reference's return_k_vector_data report
+    (every half-space vector of the k_max box, those outside k_cut at zero)
+    are the half-space list of pycd_gb300.ewald, and those with a non-zero
+    contribution lie inside the cut."""
+    import json
+    cfg, arr = gio.load("hematite")
+    ref = json.loads((gio.GOLDEN / "kvector_data.json").read_text())
+    mat, nb = gio.material(cfg)
+    p = ref["params"]
+    sysm = System(mat, nb, gio.hop_list(cfg, arr), arr["pmiv"], p["alpha"], p["r_cut"],
+                  p["k_cut"])
+    kmax = ew.k_max_for(sysm, sysm.k_cut)
+    kv, keep = ew.half_space_k_vectors(sysm.reciprocal_lattice_matrix, kmax, sysm.k_cut)
+    rows = {}
+    for line in ref["kvector_log"].splitlines()[1:]:
+        k, e = line.split(":")
+        rows[tuple(int(v) for v in k.split())] = float(e.split()[0])
+    assert len(rows) == len(kv) == len(set(map(tuple, kv.tolist())))
+    assert set(rows) == set(map(tuple, kv.tolist()))
+    inside = set(map(tuple, kv[keep].tolist()))
+    assert all(k in inside for k, e in rows.items() if e != 0.0)
+    assert ref["report_lines"][0] == f"k_max: [{kmax[0]}, {kmax[1]}, {kmax[2]}]\n"
+
+
 def test_corundum324_uses_feature_contraction():
     cfg, arr = gio.load("corundum324")
     mat, nb = gio.material(cfg)
