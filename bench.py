@@ -37,6 +37,14 @@ CHUNK = 10000
 B_STEP = 8 * N_CARRIERS * (Z + 1) * (N_CARRIERS + N_DOPANTS) + 16 * N_CARRIERS * (Z + 1)
 T_FINAL, DT = 1e30, 1e27  # time grid wide enough that no trajectory ends by time
 SEED = 20251203
+# FP64 thread instructions per KMC step of kmc_advance_kernel<8, 2, 1> on this
+# workload (ncu: smsp__sass_thread_inst_executed_op_{dadd,dfma,dmul}_pred_on
+# summed, divided by the launch's KMC steps)
+FP64_INSTR_PER_STEP = 424
+# DRAM bytes per KMC step of the same kernel (ncu: dram__bytes_read.sum +
+# dram__bytes_write.sum of one 10,000-step chunk launch of this workload,
+# 7,648,000 + 0 bytes, divided by its 4.096e7 KMC steps)
+DRAM_BYTES_PER_STEP = 7648000 / 40960000
 
 
 def peaks():
@@ -93,6 +101,27 @@ class ClockSampler(object):
         return {"sm_mhz": float(np.median(sm)) if sm else None,
                 "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
                 "samples": len(self.rows)}
+
+
+def fp64_peak_tflops(n=4096, reps=3):
+    """Measured FP64 peak of this GPU: cuBLAS DGEMM n^3 (2 n^3 flops), best of
+    `reps` after a warm-up, timed with CUDA events."""
+    import torch
+    a = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    b = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    torch.matmul(a, b)
+    torch.cuda.synchronize()
+    best = None
+    for _ in range(reps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.matmul(a, b)
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        best = ms if best is None else min(best, ms)
+    del a, b
+    return 2.0 * n ** 3 / (best / 1e3) / 1e12
 
 
 def build_workload(rank=0, n_traj=N_TRAJ):
@@ -272,72 +301,89 @@ def cpu_fourier_ns_per_entry_k(system, rows=48, n_k=24):
     return dt / (rows * n * len(kv))
 
 
+def ewald_split_record(n, kk, kc, modes=("fp64", "bf16x3", "tf32x3"), cpu=True):
+    """One (N, K) point of the split-precision build: FP64 feature build and
+    the BF16x3 / TF32x3 tcgen05 builds timed end to end (best of 3 after a
+    warm-up), their max / RMS error in eV against the FP64 array, and the
+    error of the hop energy dE0 over sampled 16-carrier, 16-dopant
+    configurations as a fraction of kT (300 K)."""
+    import torch
+    from pycd_gb300 import constants as K
+    from pycd_gb300 import ewald as ew
+    from pycd_gb300 import workloads as wl
+    peaks_file = ROOT / "MEASURED_PEAKS.json"
+    bf16_peak = json.loads(peaks_file.read_text())["bf16_tflops"] if peaks_file.exists() else 1900.0
+    cells = EWALD_SIZES[n][0]
+    system = wl.monoclinic(cells, kc, neighbor_list=True)
+    run1 = wl.run_for(system, 1)
+    kT, nbr = run1.temp, run1.site_nbr
+    line = {"workload": "ewald-split", "n_sites": n, "cells": list(cells),
+            "k_cut_per_angstrom": kc, "k_target": kk}
+    times = {}
+    ref = None
+    for mode in modes:
+        reps = 1 if mode == "fp64" else 3
+        system.get_precomputed_array_device(mode)  # warm-up / workspace
+        torch.cuda.synchronize()
+        best = None
+        for _ in range(reps):
+            t0 = time.perf_counter()
+            A = system.get_precomputed_array_device(mode)
+            torch.cuda.synchronize()
+            dt = time.perf_counter() - t0
+            best = dt if best is None else min(best, dt)
+        info = system.last_build_info
+        times[mode] = {"build_ms": 1e3 * best, "fourier_ms": info["fourier_ms"],
+                       "real_ms": info["real_ms"]}
+        line["n_kvec"] = info["n_kvec"]
+        if mode == "fp64":
+            ref = A
+        elif ref is not None:
+            err = (A - ref).abs()
+            times[mode]["max_err_ev"] = err.max().item() / K.EV2HARTREE
+            times[mode]["rms_err_ev"] = err.square().mean().sqrt().item() / K.EV2HARTREE
+            del err
+            de_max, de_rms = ew.hop_energy_error(ref, A, nbr, 16, 16, samples=2048, seed=1)
+            times[mode]["dE_max_err_over_kT"] = de_max / kT
+            times[mode]["dE_rms_err_over_kT"] = de_rms / kT
+        if mode != "fp64":
+            del A
+    kn = line["n_kvec"]
+    flops = 4.0 * n * n * kn  # N x 2K by 2K x N
+    for mode in modes:
+        t = times[mode]
+        t["algorithmic_tflops"] = flops / (t["fourier_ms"] / 1e3) / 1e12
+        if mode != "fp64":
+            if "fp64" in times:
+                t["speedup_vs_fp64"] = times["fp64"]["build_ms"] / t["build_ms"]
+            t["tensor_peak_tflops"] = bf16_peak if mode == "bf16x3" else bf16_peak / 2
+    line["modes"] = times
+    line["algorithmic_flops"] = "4 N^2 K (N x 2K features times their transpose)"
+    del ref
+    torch.cuda.empty_cache()
+    if cpu:
+        ns = cpu_fourier_ns_per_entry_k(system)
+        line["cpu_reference_fourier"] = {
+            "s_per_entry_k": ns, "extrapolated_build_s": ns * n * n * kn,
+            "cores": 1, "kind": "port",
+            "sample": "48 rows x all N columns x 24 k-vectors of pot_k_ewald"}
+    return line
+
+
 def ewald_split_bench(args):
     """Split-precision (BF16x3 / TF32x3 tcgen05) vs FP64 GPU Ewald build on
     the monoclinic supercells; one JSON line per (N, K)."""
     import torch
     from pycd_gb300 import _native as nat
-    from pycd_gb300 import constants as K
-    from pycd_gb300 import workloads as wl
     torch.cuda.set_device(0)
     nat.require_device()
-    peaks_file = ROOT / "MEASURED_PEAKS.json"
-    bf16_peak = json.loads(peaks_file.read_text())["bf16_tflops"] if peaks_file.exists() else 1900.0
     sizes = [int(s) for s in args.sizes.split(",")] if args.sizes else sorted(EWALD_SIZES)
     ks = [int(k) for k in args.kvecs.split(",")] if args.kvecs else [4096, 8192, 16384]
     for n in sizes:
-        cells, kcuts = EWALD_SIZES[n]
-        for kk, kc in zip((4096, 8192, 16384), kcuts):
-            if kk not in ks:
-                continue
-            system = wl.monoclinic(cells, kc)
-            line = {"workload": "ewald-split", "n_sites": n, "cells": list(cells),
-                    "k_cut_per_angstrom": kc}
-            times = {}
-            arrays = {}
-            for mode in ("fp64", "bf16x3", "tf32x3"):
-                reps = 1 if mode == "fp64" else 3
-                system.get_precomputed_array_device(mode)  # warm-up / workspace
-                torch.cuda.synchronize()
-                best = None
-                for _ in range(reps):
-                    t0 = time.perf_counter()
-                    A = system.get_precomputed_array_device(mode)
-                    torch.cuda.synchronize()
-                    dt = time.perf_counter() - t0
-                    best = dt if best is None else min(best, dt)
-                info = system.last_build_info
-                times[mode] = {"build_s": best, "fourier_ms": info["fourier_ms"],
-                               "real_ms": info["real_ms"]}
-                line["n_kvec"] = info["n_kvec"]
-                if mode == "fp64":
-                    arrays["fp64"] = A
-                else:
-                    err = (A - arrays["fp64"]).abs()
-                    times[mode]["max_err_ev"] = err.max().item() / K.EV2HARTREE
-                    times[mode]["rms_err_ev"] = (err.square().mean().sqrt().item()
-                                                 / K.EV2HARTREE)
-                    del err
-                del A
-            kn = line["n_kvec"]
-            flops = 4.0 * n * n * kn  # N x 2K by 2K x N
-            for mode in ("bf16x3", "tf32x3"):
-                t = times[mode]
-                t["speedup_vs_fp64"] = times["fp64"]["build_s"] / t["build_s"]
-                t["algorithmic_tflops"] = flops / (t["fourier_ms"] / 1e3) / 1e12
-                peak = bf16_peak if mode == "bf16x3" else bf16_peak / 2
-                t["tensor_peak_tflops"] = peak
-            times["fp64"]["algorithmic_tflops"] = flops / (times["fp64"]["fourier_ms"] / 1e3) / 1e12
-            line["modes"] = times
-            del arrays["fp64"]
-            torch.cuda.empty_cache()
-            if not args.no_cpu_baseline:
-                ns = cpu_fourier_ns_per_entry_k(system)
-                line["cpu_reference_fourier"] = {
-                    "s_per_entry_k": ns, "extrapolated_build_s": ns * n * n * kn,
-                    "cores": 1, "kind": "port",
-                    "sample": "48 rows x all N columns x 24 k-vectors of pot_k_ewald"}
-            print(json.dumps(line), flush=True)
+        for kk, kc in zip((4096, 8192, 16384), EWALD_SIZES[n][1]):
+            if kk in ks:
+                print(json.dumps(ewald_split_record(n, kk, kc, cpu=not args.no_cpu_baseline)),
+                      flush=True)
 
 
 def _lattice_tables(cache, lattice, cells, precision):
@@ -446,7 +492,7 @@ def uneven_bench(args):
     print(json.dumps(line), flush=True)
 
 
-def serving_bench(args):
+def serving_record(args):
     """Poisson arrivals (200 jobs/s) of single-trajectory KMC jobs over both
     lattices; continuous batching; p50/p99 latency and aggregate steps/s;
     a sample of jobs re-run alone must give identical results."""
@@ -454,8 +500,6 @@ def serving_bench(args):
     from pycd_gb300 import _native as nat
     from pycd_gb300.batch import BatchedKmc
     from pycd_gb300.serving import KmcServer, poisson_jobs
-    torch.cuda.set_device(0)
-    nat.require_device()
     jobs = poisson_jobs(args.jobs, rate=200.0, seed=11, max_steps=args.max_job_steps)
     server = KmcServer(budget_bytes=150e9, chunk_steps=args.chunk, precision="bf16x3",
                        seed=SEED)
@@ -477,7 +521,8 @@ def serving_bench(args):
     # alone vs in the mix
     rng = np.random.default_rng(3)
     same = []
-    for j in rng.choice(server.done, size=min(6, len(server.done)), replace=False):
+    served = [j for j in server.done if j["status"] == nat.TRAJ_STEP_LIMIT]
+    for j in rng.choice(served, size=min(6, len(served)), replace=False):
         lat = server.cache.get(j["lattice"], j["cells"])
         n = lat["n_sites"]
         q = np.zeros(n)
@@ -494,11 +539,21 @@ def serving_bench(args):
                          and alone.batch.time.item() == j["time"]
                          and np.array_equal(disp.reshape(-1, 3), j["displacement"])))
     line = {"workload": "serving", "metric": "KMC job latency p50/p99 and steps/s",
-            "arrival_rate_jobs_per_s": 200.0, "jobs": len(jobs),
+            "arrival_rate_jobs_per_s": 200.0, "jobs": len(jobs), "arrival_seed": 11,
             "lattice_cache_warm_s": warm_s, **stats,
             "alone_equals_mix": same, "chunk_steps": args.chunk,
             "clocks": clocks.summary()}
-    print(json.dumps(line), flush=True)
+    del server
+    torch.cuda.empty_cache()
+    return line
+
+
+def serving_bench(args):
+    import torch
+    from pycd_gb300 import _native as nat
+    torch.cuda.set_device(0)
+    nat.require_device()
+    print(json.dumps(serving_record(args)), flush=True)
 
 
 def heavy_bench(args):
@@ -726,6 +781,69 @@ def plain_bench(args):
                          "reference loop"}}), flush=True)
 
 
+OUTPUT_DATA = {"unwrapped_traj": {"file_name": "unwrapped_traj.npy", "write": 1,
+                                  "write_every_step": 0},
+               "time": {"file_name": "time_data.npy", "write": 1},
+               "wrapped_traj": {"file_name": "wrapped_traj.npy", "write": 0},
+               "energy": {"file_name": "energy_traj.npy", "write": 0},
+               "delg_0": {"file_name": "delG0_traj.npy", "write": 0},
+               "potential": {"file_name": "potential_traj.npy", "write": 0}}
+
+
+def dropin_bench(args):
+    """Run.do_kmc_steps, the drop-in call, on the plain configuration's
+    lattice (corundum 3x3x3 = 324 sites, one electron drawn by the Run's
+    MT19937 stream, FP64 array, time grid 1e-11 s up to 2e-9 s, about
+    5e4 steps per trajectory): n_traj trajectories in one call, where they
+    advance together, against one call per trajectory (the reference's
+    one-after-another order), wall time of the whole call with set-up and
+    file writes.  Both write the same files."""
+    import shutil
+    import tempfile
+    import torch
+    from pycd_gb300 import _native as nat
+    from pycd_gb300 import workloads as wl
+    nat.require_device()
+    system = wl.corundum((3, 3, 3))
+    A, _ = system.get_precomputed_array(None, precision="fp64")
+    rows = []
+    for n_traj in (1, 8, 64):
+        d = Path(tempfile.mkdtemp(prefix="pycd_dropin_"))
+        run = wl.run_for(system, 1, t_final=2e-9, time_interval=1e-11, n_traj=n_traj,
+                         precomputed_array=A)
+        run.do_kmc_steps(d, OUTPUT_DATA, 11, "serial")  # untimed: loads the kernels
+        shutil.rmtree(d)
+        d = Path(tempfile.mkdtemp(prefix="pycd_dropin_"))
+        t0 = time.perf_counter()
+        run.do_kmc_steps(d, OUTPUT_DATA, 11, "serial")
+        torch.cuda.synchronize()
+        together = time.perf_counter() - t0
+        steps = int(sum(len(s) for s in run.last_run_steps))
+        t_each = 0.0
+        same = True
+        for i in range(n_traj):
+            one = wl.run_for(system, 1, t_final=2e-9, time_interval=1e-11, n_traj=1,
+                             precomputed_array=A)
+            e = Path(tempfile.mkdtemp(prefix="pycd_dropin_"))
+            shutil.copy(d / f"traj{i + 1}" / "initial_rnd_state.dump", e)
+            t0 = time.perf_counter()
+            one.do_kmc_steps(e, OUTPUT_DATA, 11, "parallel")
+            torch.cuda.synchronize()
+            t_each += time.perf_counter() - t0
+            for name in ("unwrapped_traj.npy", "time_data.npy"):
+                same &= (d / f"traj{i + 1}" / name).read_bytes() == (e / name).read_bytes()
+            shutil.rmtree(e)
+        shutil.rmtree(d)
+        rows.append({"n_traj": n_traj, "steps": steps, "one_call_s": together,
+                     "one_call_steps_per_s": steps / together,
+                     "call_per_trajectory_s": t_each,
+                     "call_per_trajectory_steps_per_s": steps / t_each,
+                     "speedup": t_each / together, "files_identical": bool(same)})
+    print(json.dumps({"workload": "dropin", "metric": "Run.do_kmc_steps wall time",
+                      "config": "corundum 3x3x3 (324 sites), 1 electron, t_final 2e-9 s, "
+                                "dt 1e-11 s, FP64 array", "rows": rows}), flush=True)
+
+
 def ewald_params_bench(args):
     """Ewald parameter selection (get_ewald_parameters) on the Hematite
     example lattice with device energy scans: the cases of the fixtures in
@@ -773,7 +891,7 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--workload", default="batched",
                     choices=["batched", "plain", "ewald-split", "uneven", "serving",
-                             "msd", "ewald-params", "heavy"])
+                             "msd", "ewald-params", "heavy", "dropin"])
     ap.add_argument("--heavy-steps", type=int, default=2000)
     ap.add_argument("--jobs", type=int, default=2000)
     ap.add_argument("--max-job-steps", type=int, default=1_000_000)
@@ -787,6 +905,10 @@ def main():
     ap.add_argument("--chunk", type=int, default=CHUNK)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-serving", action="store_true",
+                    help="leave the serving record out of the default line")
+    ap.add_argument("--no-ewald", action="store_true",
+                    help="leave the split-precision build record out of the default line")
     ap.add_argument("--lanes", type=int, default=0)
     ap.add_argument("--warps", type=int, default=0)
     ap.add_argument("--min-blocks", type=int, default=0,
@@ -808,6 +930,8 @@ def main():
         return ewald_params_bench(args)
     if args.workload == "heavy":
         return heavy_bench(args)
+    if args.workload == "dropin":
+        return dropin_bench(args)
 
     import torch
     import torch.distributed as dist
@@ -895,11 +1019,26 @@ def main():
 
     hbm, peak_kind = peaks()
     launch_ms = float(np.mean(kernel_ms))
-    bytes_per_launch = B_STEP * steps_done / max(1, args.steps)
+    steps_per_launch = steps_done / max(1, args.steps)
+    bytes_per_launch = B_STEP * steps_per_launch
     achieved = bytes_per_launch / (launch_ms / 1e3) / 1e9
+    # the binding resource: FP64 issue.  One DFMA, DADD or DMUL thread
+    # instruction takes one FP64 lane slot; the peak slot rate is half the
+    # measured DGEMM flop rate (2 flops per DFMA slot).
+    fp64_tf = fp64_peak_tflops()
+    fp64_peak_instr = fp64_tf * 1e12 / 2.0
+    fp64_achieved = FP64_INSTR_PER_STEP * steps_per_launch / (launch_ms / 1e3)
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_baseline_1core(system, run, dopants, occ)
+    extra = {}
+    if rank == 0 and not args.no_ewald:
+        n, kk = 8192, 4096
+        extra["ewald_split"] = ewald_split_record(n, kk, EWALD_SIZES[n][1][0], cpu=False)
+    if rank == 0 and not args.no_serving:
+        del bk
+        torch.cuda.empty_cache()
+        extra["serving"] = serving_record(args)
     if rank == 0:
         line = {
             "metric": "KMC steps/s (batched uniform, 3,600 sites, 4 e- + 4 dopants)",
@@ -918,11 +1057,21 @@ def main():
             "launch_shape": tuned,
             "status_counts": status,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm,
-                         "unit": "GB/s", "frac": achieved / hbm, "traffic": None,
+                         "unit": "GB/s", "frac": achieved / hbm,
+                         "traffic": DRAM_BYTES_PER_STEP * steps_per_launch,
+                         "traffic_source": "ncu dram bytes per KMC step of one chunk "
+                                           "launch, scaled by this launch's steps",
                          "peak_kind": peak_kind,
-                         "bytes_per_step": B_STEP, "launch_ms": launch_ms},
+                         "bytes_per_step": B_STEP, "launch_ms": launch_ms,
+                         "fp64_issue": {
+                             "instr_per_step": FP64_INSTR_PER_STEP,
+                             "achieved": fp64_achieved, "peak": fp64_peak_instr,
+                             "unit": "FP64 thread instr/s",
+                             "frac": fp64_achieved / fp64_peak_instr,
+                             "peak_kind": "measured: cuBLAS DGEMM 4096^3 this run, "
+                                          f"{fp64_tf:.3f} TFLOP/s / 2 flops per DFMA"}},
             "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": args.steps,
-            "clocks": clocks.summary()}
+            "clocks": clocks.summary(), **extra}
         print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()

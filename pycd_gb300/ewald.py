@@ -183,3 +183,43 @@ def make_desc(system, alpha, r_cut, k_cut, pmiv=None, kvecs=None):
     desc.dielectric = float(system.material.dielectric_constant)
     keep = [cart, d_kv] + ([d_pmiv] if d_pmiv is not None else [])
     return desc, keep, k_max
+
+
+def hop_energy_error(A_ref, A, nbr, n_carriers, n_dopants, samples=4096, seed=0,
+                     carrier_charge=-1.0, dopant_charge=1.0):
+    """Error of the hop energy dE0 (PyCD/core.py:2004-2026) computed from the
+    array ``A`` instead of ``A_ref`` (both CUDA (N, N) float64), over
+    ``samples`` seeded charge configurations of ``n_carriers`` carriers and
+    ``n_dopants`` fixed dopants on distinct sites, each with one hop of a
+    carrier from its site o to a neighbour n = nbr[o, s] (``nbr``: (N, S)
+    int array, -1 for no neighbour):
+
+        dE0 = 2 q_s [sum_j q_j (A[n, j] - A[o, j]) + q_s (A[o, o] - A[o, n])]
+              + E_rel[n] - E_rel[o]
+
+    with q holding every charge before the move.  E_rel cancels.  Returns
+    (max, rms) of |dE0(A) - dE0(A_ref)| in Hartree."""
+    import torch
+    nbr = np.asarray(nbr)
+    n = nbr.shape[0]
+    rng = np.random.default_rng(seed)
+    m = n_carriers + n_dopants
+    sites = np.stack([rng.choice(n, size=m, replace=False) for _ in range(samples)])
+    q = np.concatenate([np.full(n_carriers, carrier_charge),
+                        np.full(n_dopants, dopant_charge)])
+    o = sites[np.arange(samples), rng.integers(0, n_carriers, samples)]
+    slots = nbr[o]
+    pick = np.array([rng.choice(np.nonzero(r >= 0)[0]) for r in slots])
+    dst = slots[np.arange(samples), pick]
+    dev = A.device
+    t = lambda a: torch.as_tensor(a, device=dev)
+    S, O, D, Q = t(sites), t(o), t(dst), t(q)
+
+    def de(M):
+        rows_n = M[D[:, None], S]          # A[n, j] at the charged sites
+        rows_o = M[O[:, None], S]
+        term = (Q[None, :] * (rows_n - rows_o)).sum(1)
+        return 2 * carrier_charge * (term + carrier_charge * (M[O, O] - M[O, D]))
+
+    err = (de(A) - de(A_ref)).abs()
+    return float(err.max().item()), float(err.square().mean().sqrt().item())

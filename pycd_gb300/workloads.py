@@ -162,10 +162,12 @@ def monoclinic(cells, k_cut, neighbor_list=False):
                   params["k_cut"])
 
 
-def run_for(system, n_carriers, t_final=1e-6, time_interval=1e-9, temp=300):
+def run_for(system, n_carriers, t_final=1e-6, time_interval=1e-9, temp=300,
+            n_traj=1, precomputed_array=None):
     """A Run of `n_carriers` electrons (explicit occupancy is set per
-    trajectory by the caller)."""
-    return Run(system, None, temp, "full", "full", 1, t_final, time_interval,
+    trajectory by the caller, or drawn by the Run from its MT19937 stream)."""
+    return Run(system, precomputed_array, temp, "full", "full", n_traj, t_final,
+               time_interval,
                np.array([n_carriers]), {"electron": []},
                {"class_index": {}, "doping": {}},
                {"electric": {"active": 0, "dir": [1, 0, 0], "ld": 0, "mag": 0.0}},

@@ -92,3 +92,42 @@ def test_server_results_equal_alone_runs(cuda_ready):
         assert alone.batch.time.item() == j["time"]
         disp = (alone.batch.last_row + alone.batch.disp).cpu().numpy()[0, :3 * nc]
         assert np.array_equal(disp.reshape(nc, 3), j["displacement"])
+
+
+def _diffusivity(bk, n_traj, n_carriers):
+    """D = <|dr|^2> / (6 t) per carrier at the end of each trajectory; the
+    mean and its standard error over carriers."""
+    disp = (bk.batch.last_row + bk.batch.disp).cpu().numpy()[:, :3 * n_carriers]
+    r2 = (disp.reshape(n_traj, n_carriers, 3) ** 2).sum(-1)
+    d = (r2 / (6.0 * bk.batch.time.cpu().numpy()[:, None])).ravel()
+    return float(d.mean()), float(d.std(ddof=1) / np.sqrt(len(d)))
+
+
+@pytest.mark.parametrize("lattice,target", [("corundum", 6000), ("monoclinic", 8192)])
+def test_split_array_diffusivity_matches_fp64(cuda_ready, lattice, target):
+    """Above 5,000 sites: 256 trajectories of 4 electrons, 1e5 steps each, on
+    the FP64 array and on the BF16x3 split-precision array (independent
+    Philox streams).  The diffusivities agree within statistical error
+    (|z| < 4 on the carriers' standard errors)."""
+    import torch
+    cells = wl.supercell_for(lattice, target)
+    system = wl.system_for(lattice, cells)
+    n = system.neighbors.num_system_elements
+    assert n > 5000
+    res = {}
+    for seed, prec in ((101, "fp64"), (202, "bf16x3")):
+        A = system.get_precomputed_array_device(prec)
+        tab, _ = wl.batched_tables(system, A, 4, [], 1.0, 1e30, 1e27)
+        rng = np.random.default_rng(seed)
+        occ = np.stack([rng.choice(n, 4, replace=False) for _ in range(256)]).astype(np.int32)
+        bk = BatchedKmc(tab, occ, seed=seed, chunk_steps=25000, step_limit=100000)
+        bk.run(100000)
+        torch.cuda.synchronize()
+        assert (bk.batch.step.cpu().numpy() == 100000).all()
+        res[prec] = _diffusivity(bk, 256, 4)
+        del bk, tab, A
+    (d64, s64), (ds, ss) = res["fp64"], res["bf16x3"]
+    z = abs(d64 - ds) / np.hypot(s64, ss)
+    print(f"{lattice} N={n}: D_fp64 {d64:.4e} +- {s64:.1e}, D_split {ds:.4e} +- {ss:.1e}, "
+          f"|z| = {z:.2f}")
+    assert z < 4.0

@@ -119,3 +119,50 @@ def test_split_precision_monoclinic_8192(cuda_ready, precision):
                          sysm.alpha, sysm.r_cut, sysm.k_cut, m.dielectric_constant,
                          rows=rows)
     assert np.abs(ref.cpu().numpy()[rows] - orc).max() < TOL_HA
+
+
+# split-precision builds at the largest k list (N = 8,192, K = 16,382) and
+# the next supercell (N = 16,384, K = 4,096)
+LARGE = [((16, 16, 8), 1.4516, 16382), ((16, 16, 16), 0.7244, 4096)]
+
+
+@pytest.mark.parametrize("cells,k_cut,n_kvec", LARGE)
+def test_split_precision_large_against_oracle_rows(cuda_ready, cells, k_cut, n_kvec):
+    """BF16x3 and TF32x3 builds: every entry within 1e-6 eV of the FP64
+    feature build, and sampled rows (tile edges 127/128/255/256, the middle,
+    the last tile and random rows) within 1e-6 eV of the oracle's FP64
+    translation-class evaluation of the reference's formula; the FP64 build's
+    rows within 1e-10 eV of the oracle.  The hop-energy error over sampled
+    16-carrier, 16-dopant configurations stays far below kT (300 K)."""
+    import torch
+    from pycd_gb300 import ewald as ew
+    sysm = wl.monoclinic(cells, k_cut, neighbor_list=True)
+    n = sysm.neighbors.num_system_elements
+    m = sysm.material
+    rng = np.random.default_rng(n)
+    rows = np.array(sorted({0, 1, 127, 128, 129, 255, 256, n // 2 - 1, n // 2,
+                            n - 129, n - 128, n - 1} | set(rng.choice(n, 8).tolist())))
+    orc = eo.class_array(m.cartesian_unit_cell_coords, m.lattice_matrix, cells,
+                         sysm.alpha, sysm.r_cut, sysm.k_cut, m.dielectric_constant,
+                         rows=rows)
+    ref = sysm.get_precomputed_array_device("fp64")
+    assert sysm.last_build_info["n_kvec"] == n_kvec
+    assert np.abs(ref[torch.as_tensor(rows, device=ref.device)].cpu().numpy()
+                  - orc).max() < TOL_HA
+    run = wl.run_for(sysm, 1)
+    kT = run.temp  # Hartree
+    for precision in ("bf16x3", "tf32x3"):
+        A = sysm.get_precomputed_array_device(precision)
+        assert sysm.last_build_info["mode"] == precision
+        got = A[torch.as_tensor(rows, device=A.device)].cpu().numpy()
+        assert np.isfinite(got).all()
+        err_rows = np.abs(got - orc).max()
+        assert err_rows < SPLIT_TOL_HA, (precision, err_rows / K.EV2HARTREE)
+        err_all = (A - ref).abs().max().item()
+        assert err_all < SPLIT_TOL_HA, (precision, err_all / K.EV2HARTREE)
+        de_max, _ = ew.hop_energy_error(ref, A, run.site_nbr, 16, 16, samples=2048,
+                                        seed=1)
+        assert de_max < 1e-3 * kT, (precision, de_max / kT)
+        del A
+    del ref
+    torch.cuda.empty_cache()
