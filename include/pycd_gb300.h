@@ -42,7 +42,7 @@
 extern "C" {
 #endif
 
-#define PYCD_ABI_VERSION 2
+#define PYCD_ABI_VERSION 3
 
 #if defined(__GNUC__)
 #define PYCD_API __attribute__((visibility("default")))
@@ -68,7 +68,10 @@ typedef enum PycdTrajStatus {
   PYCD_TRAJ_STALLED = 3,       /* k_total == 0 or not finite (core.py:2800)  */
   PYCD_TRAJ_BAD_INDEX = 4,     /* neighbour / site index out of range        */
   PYCD_TRAJ_NO_EVENT = 5,      /* u1 at or above the last cumulative rate    */
-  PYCD_TRAJ_STEP_LIMIT = 6     /* reached its d_step_limit                   */
+  PYCD_TRAJ_STEP_LIMIT = 6,    /* reached its d_step_limit                   */
+  PYCD_TRAJ_CANCELLED = 7,     /* its d_cancel flag was set (see PycdKmcState) */
+  PYCD_TRAJ_TIMEOUT = 8        /* ran past time_limit_ns in one launch;
+                                * resumable: set the status back to RUNNING  */
 } PycdTrajStatus;
 
 /* ------------------------------------------------------------------------ */
@@ -265,6 +268,23 @@ typedef struct PycdKmcState {
   double* d_csum;
   int32_t csum_stride;
   int32_t csum_refresh;
+  /* Cooperative stop, checked by every running trajectory once every
+   * poll_interval of its steps (and before its first step of a launch).
+   * The reference's loop has no such control (core.py:2787); it serves
+   * callers that must end or bound long launches.
+   *   d_cancel: T flags or NULL; d_cancel[t] != 0 stops trajectory t with
+   *     PYCD_TRAJ_CANCELLED.  It may point into host-mapped pinned memory,
+   *     so that the host can raise a flag while a launch runs.
+   *   time_limit_ns: > 0 stops a trajectory that has advanced for longer
+   *     than this within one launch (GPU global timer) with
+   *     PYCD_TRAJ_TIMEOUT; 0 = no limit.
+   *   poll_interval: steps between checks, a power of two; 0 = 256.
+   * A stopped trajectory's state is complete up to its last step: a
+   * TIMEOUT trajectory set back to PYCD_TRAJ_RUNNING continues with the
+   * same events it would have had without the stop.                        */
+  const volatile int32_t* d_cancel;
+  int64_t time_limit_ns;
+  int32_t poll_interval;
 } PycdKmcState;
 
 /* Optional per-trajectory outputs.  Each pointer may be NULL.               */

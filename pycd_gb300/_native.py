@@ -20,6 +20,9 @@ ERR_NO_DEVICE = -5
 ERR_WORKSPACE = -6
 
 # trajectory status (PycdTrajStatus)
+# ABI version of include/pycd_gb300.h that these ctypes structs mirror
+ABI_VERSION = 3
+
 TRAJ_RUNNING = 0
 TRAJ_DONE = 1
 TRAJ_NEED_UNIFORMS = 2
@@ -27,6 +30,8 @@ TRAJ_STALLED = 3
 TRAJ_BAD_INDEX = 4
 TRAJ_NO_EVENT = 5
 TRAJ_STEP_LIMIT = 6
+TRAJ_CANCELLED = 7
+TRAJ_TIMEOUT = 8
 
 # Ewald modes (PycdEwaldMode)
 EWALD_FP64_DIRECT = 0
@@ -80,7 +85,9 @@ class KmcState(C.Structure):
                 ("d_last_row", C.c_void_p), ("d_energy", C.c_void_p),
                 ("d_status", C.c_void_p), ("d_u_cursor", C.c_void_p),
                 ("d_step_limit", C.c_void_p), ("d_csum", C.c_void_p),
-                ("csum_stride", C.c_int32), ("csum_refresh", C.c_int32)]
+                ("csum_stride", C.c_int32), ("csum_refresh", C.c_int32),
+                ("d_cancel", C.c_void_p), ("time_limit_ns", C.c_int64),
+                ("poll_interval", C.c_int32)]
 
 
 class KmcOutputs(C.Structure):
@@ -175,6 +182,10 @@ def lib():
             fn = getattr(handle, name)
             fn.restype = res
             fn.argtypes = args
+        if handle.pycd_abi_version() != ABI_VERSION:
+            raise NativeError(ERR_INVALID_ARG,
+                              "%s has ABI version %d, this package needs %d: rebuild it"
+                              % (LIB_PATH, handle.pycd_abi_version(), ABI_VERSION))
         _lib = handle
     return _lib
 

@@ -230,6 +230,9 @@ static int validate_state(const PycdKmcState* st, const PycdKmcOutputs* out,
   PYCD_REQUIRE(!st->d_csum || (st->csum_refresh > 0 &&
                                (st->csum_refresh & (st->csum_refresh - 1)) == 0),
                "csum_refresh must be a positive power of two");
+  PYCD_REQUIRE(st->poll_interval >= 0 && (st->poll_interval & (st->poll_interval - 1)) == 0,
+               "poll_interval must be 0 or a power of two");
+  PYCD_REQUIRE(st->time_limit_ns >= 0, "time_limit_ns must be >= 0");
   return PYCD_OK;
 }
 

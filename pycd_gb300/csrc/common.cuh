@@ -54,6 +54,25 @@ struct Philox4 {
   uint32_t v[4];
 };
 
+// GPU global nanosecond timer
+__device__ __forceinline__ uint64_t global_timer_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Cooperative stop of trajectory t (PycdKmcState.d_cancel / time_limit_ns):
+// the status to stop with, or 0 to go on.  t_start: the global timer when
+// the trajectory began this launch.
+__device__ __forceinline__ int32_t kmc_stop_request(const PycdKmcState& st, int64_t t,
+                                                    uint64_t t_start) {
+  if (st.d_cancel && st.d_cancel[t] != 0) return PYCD_TRAJ_CANCELLED;
+  if (st.time_limit_ns > 0 &&
+      (int64_t)(global_timer_ns() - t_start) > st.time_limit_ns)
+    return PYCD_TRAJ_TIMEOUT;
+  return 0;
+}
+
 __host__ __device__ __forceinline__ void philox_mulhilo(uint32_t a, uint32_t b,
                                                         uint32_t& hi,
                                                         uint32_t& lo) {

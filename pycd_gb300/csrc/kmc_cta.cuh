@@ -32,7 +32,8 @@ constexpr int kNbrCache = 4;
 struct CtaShared {
   double wsum[4];
   double de_sel, k_sel;
-  int sel, n_sel, o_sel, pad;
+  int sel, n_sel, o_sel;
+  int stop;  // cooperative stop status for this step (0 = go on), from thread 0
   int nb[kNbrCache];  // neighbours of n_sel (from the selected process' cache)
   // rebuilt processes of the moved carrier: job i < S is slot i, job S its Q
   double jp[kCtaMaxJobs], jcq[kCtaMaxJobs], jxb[kCtaMaxJobs], jde[kCtaMaxJobs];
@@ -209,6 +210,11 @@ __device__ void advance_trajectory_cta(const KmcArgs& a, int64_t t, CtaShared& s
                      ? a.out.d_step_time + (int64_t)t * a.out.step_capacity : nullptr;
   double pre_u1 = 0.0, pre_lu2 = 0.0;
   int64_t pre_base = -33;
+  // cooperative stop: thread 0 checks every `poll` steps; the block reads
+  // its verdict after the step's first barrier
+  const bool polling = st.d_cancel != nullptr || st.time_limit_ns > 0;
+  const int64_t poll = st.poll_interval > 0 ? st.poll_interval : 256;
+  const uint64_t t_start = polling ? global_timer_ns() : 0;
 
   ProcCache<MAXP> pc;
   bool bad = setup_processes<32, MAXP>(sy, coef, slotc, g, full, occ, pc);
@@ -274,7 +280,10 @@ __device__ void advance_trajectory_cta(const KmcArgs& a, int64_t t, CtaShared& s
     for (int v = 0; v < 5; ++v)
       lvl[v + 1] = dadd(lvl[v], __shfl_xor_sync(full, lvl[v], 1 << v));
     if (l == 0) sh.wsum[w] = lvl[5];
+    if (g == 0)
+      sh.stop = (polling && (it & (poll - 1)) == 0) ? kmc_stop_request(st, t, t_start) : 0;
     __syncthreads();
+    if (sh.stop) { status = sh.stop; break; }
     double ws[W];
 #pragma unroll
     for (int i = 0; i < W; ++i) ws[i] = sh.wsum[i];

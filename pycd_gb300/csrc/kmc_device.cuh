@@ -681,6 +681,10 @@ __device__ void advance_trajectory(const KmcArgs& a, int64_t t, int g,
   // uniforms of steps pre_base + g, prepared G at a time
   double pre_u1 = 0.0, pre_lu2 = 0.0;
   int64_t pre_base = -(int64_t)G - 1;
+  // cooperative stop: lane 0 of the group checks every `poll` steps
+  const bool polling = st.d_cancel != nullptr || st.time_limit_ns > 0;
+  const int64_t poll = st.poll_interval > 0 ? st.poll_interval : 256;
+  const uint64_t t_start = polling ? global_timer_ns() : 0;
 
   // ---- process cache: geometry, constants, carrier sums ----------------
   ProcCache<MAXP> pc;
@@ -701,6 +705,11 @@ __device__ void advance_trajectory(const KmcArgs& a, int64_t t, int g,
 
   for (int64_t it = 0; it < a.max_steps; ++it) {
     if (step >= step_limit) { status = PYCD_TRAJ_STEP_LIMIT; break; }
+    if (polling && (it & (poll - 1)) == 0) {
+      int32_t stop = (g == 0) ? kmc_stop_request(st, t, t_start) : 0;
+      stop = gshfl<G>(gmask, stop, 0);
+      if (stop) { status = stop; break; }
+    }
     // ---- uniforms (core.py:2799, 2802) --------------------------------
     if (ubase && ucur + 2 > a.rng.u_count) { status = PYCD_TRAJ_NEED_UNIFORMS; break; }
     const int64_t since = step - pre_base;

@@ -140,7 +140,7 @@ class KmcBatch(object):
     def __init__(self, occupancy, sys_index=None, max_carriers=None,
                  energy0=None, unwrapped_rows=None, step_capacity=0,
                  energy_grid_rows=None, delg0_grid_rows=None, drift=False,
-                 step_limit=None, max_processes=256):
+                 step_limit=None, max_processes=256, cancellable=False):
         import torch
         dev = _dev()
         occ = np.asarray(occupancy, dtype=np.int32)
@@ -185,6 +185,20 @@ class KmcBatch(object):
         self.csum_stride = 2 * int(max_processes)
         self.csum = z64(T, self.csum_stride)
         self.csum_refresh = self.CSUM_REFRESH
+        # cooperative stop: per-trajectory flags in pinned host memory that
+        # the kernels read while they run (request_stop), and a per-launch
+        # time limit (0 = none), both checked every poll_interval steps
+        self.cancel = (torch.zeros(T, dtype=torch.int32, pin_memory=True)
+                       if cancellable else None)
+        self.time_limit_ns = 0
+        self.poll_interval = 0
+
+    def request_stop(self, t, flag=True):
+        """Ask trajectory t to stop with TRAJ_CANCELLED at its next poll,
+        also while a launch runs (or clear the request)."""
+        if self.cancel is None:
+            raise ValueError("this batch was made without cancellable=True")
+        self.cancel[int(t)] = 1 if flag else 0
 
     def state_struct(self):
         s = nat.KmcState()
@@ -204,6 +218,9 @@ class KmcBatch(object):
         s.d_csum = self.csum.data_ptr()
         s.csum_stride = self.csum_stride
         s.csum_refresh = self.csum_refresh
+        s.d_cancel = nat.ptr(self.cancel)
+        s.time_limit_ns = int(self.time_limit_ns)
+        s.poll_interval = int(self.poll_interval)
         return s
 
     def outputs_struct(self):

@@ -493,3 +493,87 @@ def test_field_drift_and_delg0_grid(cuda_ready):
     assert len(rows) > 3  # several grid crossings within the oracle's steps
     got = results[0]["delg0_grid"][0, rows]
     assert np.abs(got - o["delg0"][rows]).max() <= 1e-12 * np.abs(o["delg0"][rows]).max()
+
+
+def _state(b):
+    return {k: getattr(b, k).cpu().numpy().copy()
+            for k in ("occ", "time", "step", "disp", "last_row", "energy", "csum")}
+
+
+@pytest.mark.parametrize("lanes", [8, 64])
+def test_time_limit_stops_and_resumes_with_the_same_events(cuda_ready, lanes):
+    """A per-launch time limit stops every trajectory with TRAJ_TIMEOUT
+    before its step budget; relaunching the stopped trajectories (status set
+    back to RUNNING) until the budget is done gives the state of one
+    uninterrupted launch bit for bit, in the warp form (8 lanes) and the
+    block form (64 lanes)."""
+    import torch
+    sysm, tables, run, cfg, arr = _corundum3600()
+    T, n = 32, 60000
+    rng = np.random.default_rng(11)
+    occ = np.stack([rng.choice(3600, size=4, replace=False) for _ in range(T)])
+    eng = KmcEngine(tables, launch={"lanes_per_traj": lanes})
+    ref = KmcBatch(occ, step_limit=n)
+    eng.advance(ref, n, eng.rng_struct(seed=5))
+    torch.cuda.synchronize()
+    b = KmcBatch(occ, step_limit=n)
+    b.time_limit_ns = 2_000_000  # 2 ms per launch
+    b.poll_interval = 64
+    launches, stopped = 0, 0
+    while True:
+        eng.advance(b, n, eng.rng_struct(seed=5))
+        torch.cuda.synchronize()
+        launches += 1
+        st = b.status.cpu().numpy()
+        stopped += int((st == nat.TRAJ_TIMEOUT).sum())
+        if not (st == nat.TRAJ_TIMEOUT).any():
+            break
+        b.status[torch.as_tensor(st == nat.TRAJ_TIMEOUT, device=b.status.device)] = \
+            nat.TRAJ_RUNNING
+        assert launches < 10000
+    assert launches > 1 and stopped > 0
+    assert (b.step.cpu().numpy() == n).all()
+    got, want = _state(b), _state(ref)
+    for k in want:
+        assert np.array_equal(got[k], want[k]), k
+
+
+@pytest.mark.parametrize("lanes", [8, 64])
+def test_cancel_flag_stops_one_trajectory_during_a_launch(cuda_ready, lanes):
+    """The host raises one trajectory's cancel flag (pinned host memory)
+    while a long launch runs: that trajectory stops with TRAJ_CANCELLED
+    part-way, the others finish their budget, and the cancelled one's state
+    equals the same trajectory advanced alone by the same number of steps."""
+    import time
+    import torch
+    sysm, tables, run, cfg, arr = _corundum3600()
+    T, n, victim = 16, 400000, 5
+    rng = np.random.default_rng(12)
+    occ = np.stack([rng.choice(3600, size=4, replace=False) for _ in range(T)])
+    eng = KmcEngine(tables, launch={"lanes_per_traj": lanes})
+    warm = KmcBatch(occ, step_limit=100)  # kernel loaded before the timed launch
+    eng.advance(warm, 100, eng.rng_struct(seed=9))
+    torch.cuda.synchronize()
+    b = KmcBatch(occ, step_limit=n, cancellable=True)
+    b.poll_interval = 128
+    eng.advance(b, n, eng.rng_struct(seed=9))
+    time.sleep(0.05)
+    b.request_stop(victim)
+    torch.cuda.synchronize()
+    st, steps = b.status.cpu().numpy(), b.step.cpu().numpy()
+    assert st[victim] == nat.TRAJ_CANCELLED
+    assert 0 < steps[victim] < n
+    others = np.arange(T) != victim
+    assert (steps[others] == n).all()
+    alone = KmcBatch(occ[victim:victim + 1], step_limit=int(steps[victim]))
+    eng.advance(alone, n, eng.rng_struct(seed=9, traj_offset=victim))
+    torch.cuda.synchronize()
+    got, want = _state(b), _state(alone)
+    for k in ("occ", "time", "step", "disp", "last_row", "energy"):
+        assert np.array_equal(got[k][victim], want[k][0]), k
+    # a cleared flag lets the trajectory go on
+    b.request_stop(victim, False)
+    b.status[victim] = nat.TRAJ_RUNNING
+    eng.advance(b, n, eng.rng_struct(seed=9))
+    torch.cuda.synchronize()
+    assert b.step[victim].item() == n

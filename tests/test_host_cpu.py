@@ -25,7 +25,7 @@ def test_library_exports_every_declared_symbol():
     for name in declared:
         assert hasattr(lib, name), name
         assert name in nat.exported_symbols(), name
-    assert lib.pycd_abi_version() == 2
+    assert lib.pycd_abi_version() == 3
 
 
 def test_default_lanes_rule():
