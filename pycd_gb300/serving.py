@@ -26,6 +26,10 @@ from . import _native as nat
 from .kmc import KmcBatch, KmcEngine, default_lanes
 
 
+# status of a job whose lattice alone is larger than the HBM budget
+REJECTED = -1
+
+
 def _pow2(v):
     p = 1
     while p < v:
@@ -44,9 +48,18 @@ class LatticeCache(object):
         self.entries = {}
         self.clock = 0
         self.builds = 0
+        self.evictions = 0
+        self.deferrals = 0        # get() calls the budget could not serve yet
+        self.peak_bytes = 0.0     # largest bytes_in_use() after any build
 
     def bytes_in_use(self):
         return sum(e["bytes"] for e in self.entries.values())
+
+    def fits(self, lattice, cells):
+        """Whether the lattice could ever be held within the budget."""
+        per = 12 if lattice == "corundum" else 4
+        n = per * int(np.prod(cells))
+        return self.footprint(n, 4) <= self.budget
 
     def footprint(self, n_sites, n_slots):
         # array + neighbour/hop/lambda/V/coefficient tables + per-job potentials
@@ -58,6 +71,7 @@ class LatticeCache(object):
             if not idle:
                 return False
             del self.entries[min(idle)[1]]
+            self.evictions += 1
         return True
 
     def get(self, lattice, cells):
@@ -74,6 +88,7 @@ class LatticeCache(object):
         n = per * int(np.prod(cells))
         need = self.footprint(n, 4)
         if not self._evict(need):
+            self.deferrals += 1
             return None
         system = wl.system_for(lattice, cells)
         A = system.get_precomputed_array_device(self.precision)
@@ -85,6 +100,7 @@ class LatticeCache(object):
              "used": self.clock}
         self.entries[key] = e
         self.builds += 1
+        self.peak_bytes = max(self.peak_bytes, self.bytes_in_use())
         return e
 
 
@@ -93,14 +109,16 @@ class _Bucket(object):
     system table, engine, stream and completion event.  A bucket is touched
     by the host (retire, admit, table upload) only between its chunks."""
 
-    def __init__(self, np_bound, nc_bound, capacity, max_carriers):
+    def __init__(self, np_bound, nc_bound, capacity, max_carriers, long_jobs=False):
         import torch
         self.np_bound, self.nc_bound = np_bound, nc_bound
+        self.long_jobs = long_jobs
         self.capacity = capacity
         self.batch = KmcBatch(np.zeros((capacity, max_carriers), np.int32),
                               sys_index=np.zeros(capacity, np.int32),
                               max_carriers=max_carriers,
-                              step_limit=np.zeros(capacity, np.int64))
+                              step_limit=np.zeros(capacity, np.int64),
+                              cancellable=True)
         self.batch.status.fill_(nat.TRAJ_DONE)  # free slots are never advanced
         self.ids = torch.zeros(capacity, dtype=torch.int64, device="cuda")
         self.free = list(range(capacity - 1, -1, -1))
@@ -145,13 +163,20 @@ class KmcServer(object):
     its next chunk is launched on its own stream, while the other buckets keep
     running.  No bucket waits for another."""
 
+    # a job whose steps x carriers reach this is "long": it goes to a bucket
+    # of long jobs of its class, whose few trajectories get the wider (block)
+    # launch forms, the fastest per step; the longest jobs set the latency
+    # tail, so they are served first in per-step speed
+    LONG_WORK = 1.6e7
+
     def __init__(self, budget_bytes=150e9, chunk_steps=5000, slots_per_bucket=1024,
-                 precision="bf16x3", seed=0, max_carriers=32):
+                 precision="bf16x3", seed=0, max_carriers=32, long_work=LONG_WORK):
         self.cache = LatticeCache(budget_bytes, precision)
         self.chunk_steps = int(chunk_steps)
         self.slots = int(slots_per_bucket)
         self.seed = int(seed)
         self.max_carriers = int(max_carriers)
+        self.long_work = float(long_work) if long_work else float("inf")
         self.buckets = {}
         self.pending = []
         self.waiting = {}         # bucket key -> prepared jobs waiting for a slot
@@ -170,17 +195,30 @@ class KmcServer(object):
     def now(self):
         return time.perf_counter() - self.t0
 
-    def _bucket(self, n_proc, n_car):
-        key = (_pow2(n_proc), _pow2(n_car))
+    def _bucket(self, n_proc, n_car, long_jobs=False):
+        key = (_pow2(n_proc), _pow2(n_car), bool(long_jobs))
         b = self.buckets.get(key)
         if b is None:
-            b = _Bucket(key[0], key[1], self.slots, self.max_carriers)
+            b = _Bucket(key[0], key[1], self.slots, self.max_carriers, key[2])
             self.buckets[key] = b
         return b
 
+    def _finish_unadmitted(self, job, status):
+        """A job that leaves before it had a slot (cancelled or rejected)."""
+        t = self.now()
+        job.update(status=status, finished=t, latency=t - job["arrival"], steps_done=0,
+                   time=0.0, occupancy=None, displacement=None)
+        for k in ("bucket", "lattice_entry", "tab"):
+            job.pop(k, None)
+        self.done.append(job)
+
     def _prepare(self, job):
         """Lattice and job tables of an arrived job; False when the HBM
-        budget cannot hold its lattice now."""
+        budget cannot hold its lattice now.  A job whose lattice alone
+        exceeds the budget is rejected (status REJECTED)."""
+        if not self.cache.fits(job["lattice"], job["cells"]):
+            self._finish_unadmitted(job, REJECTED)
+            return True
         lat = self.cache.get(job["lattice"], job["cells"])
         if lat is None:
             return False
@@ -191,7 +229,8 @@ class KmcServer(object):
         q = np.zeros(n)
         q[dopants] = 1.0
         tab = lat["tables"].with_charges(q, job["carriers"])
-        b = self._bucket(job["carriers"] * tab.n_slots, job["carriers"])
+        long_job = job["steps"] * job["carriers"] >= self.long_work
+        b = self._bucket(job["carriers"] * tab.n_slots, job["carriers"], long_job)
         lat["refs"] += 1
         job.update(lattice_entry=lat, bucket=b, tab=tab, carrier_sites=carriers,
                    dopant_sites=dopants)
@@ -234,6 +273,8 @@ class KmcServer(object):
         bt.disp[idx] = 0.0
         bt.last_row[idx] = 0.0
         bt.status[idx] = nat.TRAJ_RUNNING
+        for j in new:  # the bucket is idle: no kernel reads these flags now
+            bt.request_stop(j["slot"], False)
 
     def _launch(self, b):
         """Next chunk of idle bucket b on its stream (after the host-side
@@ -243,6 +284,7 @@ class KmcServer(object):
         if b.dirty:
             b.upload()
         # launch shape for the jobs now in the bucket, not its slot count
+        # (a bucket of long jobs holds few, which widens it to block forms)
         b.engine.launch.lanes_per_traj = default_lanes(b.np_bound, b.nc_bound,
                                                        max(1, len(b.jobs)))
         b.engine.advance(b.batch, self.chunk_for(b),
@@ -263,6 +305,31 @@ class KmcServer(object):
                 self._retire(b, slot, job, int(st[slot]), t_ret)
                 out.append(job)
         return out
+
+    def cancel(self, job_id):
+        """Cancel a job.  A job on the GPU stops at its next poll (the
+        kernel reads its slot's flag in pinned host memory while the chunk
+        runs) and retires with TRAJ_CANCELLED and its state so far; a job
+        not yet admitted leaves at once with no steps.  Returns False for
+        an unknown or finished job."""
+        for j in self.pending:
+            if j["id"] == job_id:
+                self.pending.remove(j)
+                self._finish_unadmitted(j, nat.TRAJ_CANCELLED)
+                return True
+        for queue in self.waiting.values():
+            for j in queue:
+                if j["id"] == job_id:
+                    queue.remove(j)
+                    j["lattice_entry"]["refs"] -= 1
+                    self._finish_unadmitted(j, nat.TRAJ_CANCELLED)
+                    return True
+        for b in self.buckets.values():
+            for slot, j in b.jobs.items():
+                if j["id"] == job_id:
+                    b.batch.request_stop(slot)
+                    return True
+        return False
 
     def step(self):
         """One scheduling pass: prepare arrived jobs, then for every bucket
@@ -340,13 +407,21 @@ class KmcServer(object):
                 b.event.synchronize()
                 b.running = False
         wall = self.now()
-        lat = np.array([j["latency"] for j in self.done]) if self.done else np.zeros(1)
+        served = [j for j in self.done if j["status"] not in (REJECTED, nat.TRAJ_CANCELLED)]
+        lat = np.array([j["latency"] for j in served]) if served else np.zeros(1)
         return {"jobs": len(self.done), "wall_s": wall, "steps": steps,
                 "steps_per_s": steps / wall if wall else 0.0,
                 "latency_p50_s": float(np.percentile(lat, 50)),
                 "latency_p99_s": float(np.percentile(lat, 99)),
                 "lattice_builds": self.cache.builds,
-                "unfinished": len(self.pending) + sum(len(b.jobs) for b in self.buckets.values())}
+                "lattice_evictions": self.cache.evictions,
+                "admission_deferrals": self.cache.deferrals,
+                "peak_lattice_bytes": self.cache.peak_bytes,
+                "long_job_buckets": sum(1 for b in self.buckets.values() if b.long_jobs),
+                "cancelled": sum(1 for j in self.done if j["status"] == nat.TRAJ_CANCELLED),
+                "rejected": sum(1 for j in self.done if j["status"] == REJECTED),
+                "unfinished": len(self.pending) + sum(len(q) for q in self.waiting.values())
+                + sum(len(b.jobs) for b in self.buckets.values())}
 
 
 def poisson_jobs(n_jobs, rate=200.0, seed=0, median_sites=2000, min_sites=300,

@@ -131,3 +131,89 @@ def test_split_array_diffusivity_matches_fp64(cuda_ready, lattice, target):
     print(f"{lattice} N={n}: D_fp64 {d64:.4e} +- {s64:.1e}, D_split {ds:.4e} +- {ss:.1e}, "
           f"|z| = {z:.2f}")
     assert z < 4.0
+
+
+def _alone_equals_mix(server, jobs, seed):
+    import torch
+    for j in jobs:
+        lat = server.cache.get(j["lattice"], j["cells"])
+        q = np.zeros(lat["n_sites"])
+        q[j["dopant_sites"]] = 1.0
+        tab = lat["tables"].with_charges(q, j["carriers"])
+        alone = BatchedKmc(tab, np.asarray(j["carrier_sites"])[None, :], seed=seed,
+                           chunk_steps=j["steps"], step_limit=j["steps"],
+                           traj_offset=j["id"], use_graph=False)
+        alone.run(j["steps"])
+        torch.cuda.synchronize()
+        nc = j["carriers"]
+        assert np.array_equal(alone.batch.occ.cpu().numpy()[0, :nc], j["occupancy"])
+        assert alone.batch.time.item() == j["time"]
+
+
+def test_server_under_hbm_pressure_evicts_and_defers(cuda_ready):
+    """An HBM budget that holds the largest lattice but never all of them:
+    the lattice cache evicts idle lattices (least recently used) and defers
+    jobs whose lattice does not fit yet; every job finishes, the cache never
+    holds more than the budget, and results equal the jobs run alone."""
+    from pycd_gb300.serving import KmcServer, LatticeCache, poisson_jobs
+    jobs = poisson_jobs(40, rate=400.0, seed=21, median_sites=800, max_sites=3000,
+                        max_carriers=6, min_steps=1000, max_steps=6000, size_grid=12)
+    probe = LatticeCache(1e30)
+    fps = sorted({probe.footprint((12 if j["lattice"] == "corundum" else 4)
+                                  * int(np.prod(j["cells"])), 4)
+                  for j in jobs})
+    assert len(fps) >= 4
+    budget = fps[-1] + 0.5 * fps[-2]
+    server = KmcServer(budget_bytes=budget, chunk_steps=1000, slots_per_bucket=8, seed=3)
+    stats = server.run([dict(j) for j in jobs], max_seconds=300)
+    assert stats["jobs"] == 40 and stats["unfinished"] == 0 and stats["rejected"] == 0
+    assert stats["lattice_evictions"] > 0 and stats["admission_deferrals"] > 0
+    assert server.cache.peak_bytes <= budget
+    assert all(j["status"] == nat.TRAJ_STEP_LIMIT for j in server.done)
+    _alone_equals_mix(server, server.done[:4] + server.done[-2:], seed=3)
+
+
+def test_server_rejects_a_lattice_larger_than_the_budget(cuda_ready):
+    from pycd_gb300.serving import KmcServer, poisson_jobs
+    jobs = poisson_jobs(3, rate=100.0, seed=2, median_sites=400, max_sites=800,
+                        max_carriers=2, min_steps=500, max_steps=800)
+    server = KmcServer(budget_bytes=1e5, chunk_steps=500, slots_per_bucket=4, seed=1)
+    stats = server.run([dict(j) for j in jobs], max_seconds=60)
+    assert stats["rejected"] == 3 and stats["unfinished"] == 0
+
+
+def test_server_cancels_a_running_and_a_pending_job(cuda_ready):
+    """A long job is cancelled while its chunk runs on the GPU: it stops
+    within a poll interval, retires with TRAJ_CANCELLED and its partial
+    state, and its bucket's other jobs finish as if alone.  A job that has
+    not arrived yet is cancelled with no steps."""
+    import time
+    from pycd_gb300.serving import KmcServer, poisson_jobs
+    jobs = poisson_jobs(12, rate=200.0, seed=8, median_sites=400, max_sites=1000,
+                        max_carriers=4, min_steps=2000, max_steps=4000)
+    jobs[2]["steps"] = 50_000_000
+    jobs[11]["arrival"] = 30.0
+    server = KmcServer(budget_bytes=20e9, chunk_steps=1_000_000, slots_per_bucket=16,
+                       seed=4, long_work=0)
+    for j in jobs:
+        server.submit(dict(j))
+    server.start()
+    assert server.cancel(11)
+    t_cancel = None
+    while server.busy() and server.now() < 120:
+        server.step()
+        running = any(j["id"] == 2 for b in server.buckets.values() for j in b.jobs.values()
+                      if b.running)
+        if t_cancel is None and running and server.now() > 1.0:
+            assert server.cancel(2)
+            t_cancel = server.now()
+        time.sleep(0.001)
+    assert t_cancel is not None and not server.busy()
+    done = {j["id"]: j for j in server.done}
+    assert done[11]["status"] == nat.TRAJ_CANCELLED and done[11]["steps_done"] == 0
+    assert done[2]["status"] == nat.TRAJ_CANCELLED
+    assert 0 < done[2]["steps_done"] < 50_000_000
+    assert done[2]["finished"] - t_cancel < 2.0
+    rest = [j for i, j in done.items() if i not in (2, 11)]
+    assert len(rest) == 10 and all(j["status"] == nat.TRAJ_STEP_LIMIT for j in rest)
+    _alone_equals_mix(server, rest[:4], seed=4)
