@@ -26,6 +26,43 @@ def _numeric(v):
     return not isinstance(v, str) and bool(np.isreal(v))
 
 
+class _Mt19937Stream(object):
+    """The values ``random.random()`` would return from one CPython MT19937
+    state, drawn in blocks: NumPy's MT19937 gives the same 32-bit outputs,
+    combined as CPython's 53-bit ``random()`` ((a >> 5) 2^26 + (b >> 6)) / 2^53.
+    ``state()`` is the CPython state after the values marked ``used``."""
+
+    def __init__(self, state):
+        self.bg = np.random.MT19937()
+        self.bg.state = {"bit_generator": "MT19937",
+                         "state": {"key": np.asarray(state[1][:624], np.uint32),
+                                   "pos": int(state[1][624])}}
+        self.gauss = state[2]
+        self.block_start = self.bg.state
+        self.consumed = 0  # values used since block_start
+
+    def fill(self, out):
+        """Write the next len(out) values into `out`; they become the block
+        that ``used`` counts from."""
+        self.block_start = self.bg.state
+        self.consumed = 0
+        raw = self.bg.random_raw(2 * len(out))
+        a = (raw[0::2] >> np.uint64(5)).astype(np.float64)
+        b = (raw[1::2] >> np.uint64(6)).astype(np.float64)
+        out[:] = (a * 67108864.0 + b) / 9007199254740992.0
+
+    def used(self, n):
+        self.consumed += int(n)
+
+    def state(self):
+        bg = np.random.MT19937()
+        bg.state = self.block_start
+        if self.consumed:
+            bg.random_raw(2 * self.consumed)
+        st = bg.state["state"]
+        return (3, tuple(int(x) for x in st["key"]) + (int(st["pos"]),), self.gauss)
+
+
 class System(EwaldParameterSearch):
     """Ewald geometry and parameters (PyCD/core.py:671-797); the automatic
     parameter choices of PyCD/core.py:913-1592 come from EwaldParameterSearch."""
@@ -516,9 +553,28 @@ class Run(object):
             num_path, field_shift=self.site_field_shift)
 
     # -- the KMC loop -------------------------------------------------------
+    # device memory for one group of trajectories advanced together (path
+    # grids, per-step logs, uniforms); larger runs go in several groups
+    GROUP_BYTES = 2 << 30
+
+    def _group_size(self, num_path, outputs):
+        per = (8 * num_path * 3 * self.total_species * (1 + outputs)
+               + 28 * self.UNIFORM_BLOCK + 4096)
+        return max(1, int(self.GROUP_BYTES // per))
+
     def do_kmc_steps(self, dst_path, output_data, random_seed, compute_mode):
         """Run every trajectory on the GPU and write the reference's files
-        (core.py:2863-2906) with the same 'ab' append semantics."""
+        (core.py:2863-2906) with the same 'ab' append semantics.
+
+        The reference runs its trajectories one after another
+        (core.py:2668); here all n_traj trajectories of the call advance
+        together in one batch, each on its own MT19937 stream restored from
+        its initial_rnd_state.dump (core.py:2694-2695) and drawn in blocks of
+        UNIFORM_BLOCK steps.  A trajectory's events, times and files are the
+        same as when it runs alone.  A trajectory that stops on a zero or
+        non-finite k_total raises NativeError after the files of the
+        trajectories before it are written, where the reference raises its
+        IndexError."""
         import torch
         from .kmc import KmcBatch, KmcEngine
         nat.require_device()
@@ -540,6 +596,10 @@ class Run(object):
         drift = np.zeros((self.n_traj, self.total_species, 3)) \
             if self.electric_field_active else None
         self.last_run_steps = []
+        # per-trajectory set-up in the reference's order: MT state, doping,
+        # initial occupancy (which may draw from the stream), energy
+        trajs = []
+        shared_tables = None
         for ti in range(self.n_traj):
             traj_dir = (dst_path / f"traj{ti + 1}") if compute_mode != "parallel" \
                 else dst_path
@@ -548,75 +608,143 @@ class Run(object):
                 rnd.setstate(pickle.load(fh))
             dopants = self._load_doping(traj_dir)
             occ = self.generate_initial_occupancy(dopants)
-            occupancy_list = [list(occ)] if self.doping_active else None
             q = self.charge_config(occ, dopants)
             qq = np.multiply(q.transpose(), q)
             energy0 = ewald_neut + np.sum(np.multiply(qq, self.precomputed_array))
-            tables = self.device_tables(A_dev, dopants)
-            batch = KmcBatch(np.asarray(occ)[None, :], energy0=[energy0],
-                             unwrapped_rows=num_path,
-                             step_capacity=self.UNIFORM_BLOCK,
-                             energy_grid_rows=num_path if want("energy") else None,
-                             delg0_grid_rows=num_path if want("delg_0") else None,
-                             drift=self.electric_field_active)
-            engine = KmcEngine(tables)
-            times, procs = [], []
-            ubuf = torch.empty((1, 2 * self.UNIFORM_BLOCK), dtype=torch.float64,
-                               device="cuda")
-            while True:
-                u = np.fromiter((rnd.random() for _ in range(2 * self.UNIFORM_BLOCK)),
-                                dtype=np.float64, count=2 * self.UNIFORM_BLOCK)
-                ubuf.copy_(torch.from_numpy(u)[None, :])
-                batch.u_cursor.zero_()
-                batch.step_offset = int(batch.step.item())
-                engine.advance(batch, self.UNIFORM_BLOCK,
-                               engine.rng_struct(ubuf))
-                torch.cuda.synchronize()
-                n_done = int(batch.step.item()) - batch.step_offset
-                times.append(batch.step_time[0, :n_done].cpu().numpy().copy())
-                procs.append(batch.step_proc[0, :n_done].cpu().numpy().copy())
-                status = int(batch.status.item())
-                if status in (nat.TRAJ_RUNNING, nat.TRAJ_NEED_UNIFORMS):
-                    # the block of uniforms is used up: draw the next one
-                    batch.status.zero_()
-                    continue
-                if status == nat.TRAJ_DONE:
-                    break
-                raise nat.NativeError(
-                    nat.ERR_STALLED if status == nat.TRAJ_STALLED else nat.ERR_BAD_INDEX,
-                    "trajectory %d stopped with status %d after %d steps "
-                    "(k_total zero/not finite, or no event selected)"
-                    % (ti + 1, status, int(batch.step.item())))
-            step_proc = np.concatenate(procs) if procs else np.zeros(0, np.int32)
-            self.last_run_steps.append(step_proc)
-            time_data = np.concatenate([[0.0]] + times)
             if self.doping_active:
-                occupancy_list.extend(self._replay_occupancy(occ, step_proc)[1:])
-            if every_step:
-                unwrapped = self._every_step_rows(occ, step_proc)
+                tables = self.device_tables(A_dev, dopants)
             else:
-                unwrapped = batch.unwrapped[0, :, :3 * self.total_species].cpu().numpy()
-            if drift is not None:
-                drift[ti] = batch.drift[0, :self.total_species].cpu().numpy()
-            arrays = {"unwrapped_traj": unwrapped, "time": time_data,
-                      "wrapped_traj": np.zeros((num_path, self.total_species * 3)),
-                      "potential": np.zeros((num_path, self.total_species))}
-            if want("energy"):
-                arrays["energy"] = batch.energy_grid[0].cpu().numpy()
-            if want("delg_0"):
-                arrays["delg_0"] = batch.delg0_grid[0].cpu().numpy()
-            for kind, attrs in output_data.items():
-                if attrs.get("write") and kind in arrays:
-                    with open(traj_dir / attrs["file_name"], "ab") as fh:
-                        np.save(fh, arrays[kind])
-            if self.doping_active:
-                np.save(traj_dir / "occupancy.npy",
-                        np.asarray(occupancy_list, dtype=int))
+                if shared_tables is None:
+                    shared_tables = self.device_tables(A_dev, dopants)
+                tables = shared_tables
+            trajs.append({"dir": traj_dir, "occ": list(occ), "energy0": energy0,
+                          "tables": tables, "stream": _Mt19937Stream(rnd.getstate()),
+                          "occupancy_list": [list(occ)] if self.doping_active else None})
+        outputs = int(bool(want("energy"))) + int(bool(want("delg_0")))
+        g = self._group_size(num_path, outputs)
+        failure = None
+        for g0 in range(0, self.n_traj, g):
+            group = trajs[g0:g0 + g]
+            results = self._advance_group(group, num_path, want)
+            for off, (tr, res) in enumerate(zip(group, results)):
+                ti = g0 + off
+                if res["error"] is not None:
+                    failure = (ti, res["error"])
+                    break
+                step_proc = res["step_proc"]
+                self.last_run_steps.append(step_proc)
+                occ = tr["occ"]
+                if self.doping_active:
+                    tr["occupancy_list"].extend(self._replay_occupancy(occ, step_proc)[1:])
+                unwrapped = (self._every_step_rows(occ, step_proc) if every_step
+                             else res["unwrapped"])
+                if drift is not None:
+                    drift[ti] = res["drift"]
+                arrays = {"unwrapped_traj": unwrapped, "time": res["time"],
+                          "wrapped_traj": np.zeros((num_path, self.total_species * 3)),
+                          "potential": np.zeros((num_path, self.total_species))}
+                if want("energy"):
+                    arrays["energy"] = res["energy"]
+                if want("delg_0"):
+                    arrays["delg_0"] = res["delg_0"]
+                for kind, attrs in output_data.items():
+                    if attrs.get("write") and kind in arrays:
+                        with open(tr["dir"] / attrs["file_name"], "ab") as fh:
+                            np.save(fh, arrays[kind])
+                if self.doping_active:
+                    np.save(tr["dir"] / "occupancy.npy",
+                            np.asarray(tr["occupancy_list"], dtype=int))
+            if failure is not None:
+                break
+        # the module-level stream ends where the last trajectory's ended
+        last = trajs[failure[0] if failure else -1]["stream"]
+        rnd.setstate(last.state())
+        if failure is not None:
+            ti, (status, steps) = failure
+            raise nat.NativeError(
+                nat.ERR_STALLED if status == nat.TRAJ_STALLED else nat.ERR_BAD_INDEX,
+                "trajectory %d stopped with status %d after %d steps "
+                "(k_total zero/not finite, or no event selected)" % (ti + 1, status, steps))
         prefix = ""
         if self.electric_field_active:
             prefix = self._drift_mobility_report(drift, dst_path)
         generate_report(self.start_time, dst_path, "Run", 1, prefix)
         return None
+
+    def _advance_group(self, group, num_path, want):
+        """Advance the trajectories of `group` together to the end of their
+        time grids.  Launches run in lockstep: each advances every running
+        trajectory by UNIFORM_BLOCK steps on the next UNIFORM_BLOCK pairs of
+        its own uniforms, so a running trajectory's step count is always
+        launch * UNIFORM_BLOCK and one log offset serves all of them."""
+        import torch
+        from .kmc import KmcBatch, KmcEngine
+        B = self.UNIFORM_BLOCK
+        T = len(group)
+        tables, sys_index = [], []
+        for tr in group:
+            for i, t in enumerate(tables):
+                if t is tr["tables"]:
+                    sys_index.append(i)
+                    break
+            else:
+                sys_index.append(len(tables))
+                tables.append(tr["tables"])
+        batch = KmcBatch(np.asarray([tr["occ"] for tr in group]),
+                         sys_index=sys_index if len(tables) > 1 else None,
+                         energy0=[tr["energy0"] for tr in group],
+                         unwrapped_rows=num_path, step_capacity=B,
+                         energy_grid_rows=num_path if want("energy") else None,
+                         delg0_grid_rows=num_path if want("delg_0") else None,
+                         drift=self.electric_field_active)
+        engine = KmcEngine(tables)
+        host_u = torch.empty((T, 2 * B), dtype=torch.float64, pin_memory=True)
+        ubuf = torch.empty((T, 2 * B), dtype=torch.float64, device="cuda")
+        times = [[] for _ in range(T)]
+        procs = [[] for _ in range(T)]
+        running = np.ones(T, bool)
+        error = [None] * T
+        hu = host_u.numpy()
+        launch = 0
+        while running.any():
+            for t in np.nonzero(running)[0]:
+                group[t]["stream"].fill(hu[t])
+            ubuf.copy_(host_u, non_blocking=True)
+            batch.u_cursor.zero_()
+            batch.step_offset = launch * B
+            engine.advance(batch, B, engine.rng_struct(ubuf))
+            torch.cuda.synchronize()
+            steps = batch.step.cpu().numpy()
+            status = batch.status.cpu().numpy()
+            st_time = batch.step_time.cpu().numpy()
+            st_proc = batch.step_proc.cpu().numpy()
+            for t in np.nonzero(running)[0]:
+                n_done = int(steps[t]) - launch * B
+                times[t].append(st_time[t, :n_done].copy())
+                procs[t].append(st_proc[t, :n_done].copy())
+                group[t]["stream"].used(2 * n_done)
+                if status[t] == nat.TRAJ_RUNNING:
+                    continue
+                running[t] = False
+                if status[t] != nat.TRAJ_DONE:
+                    error[t] = (int(status[t]), int(steps[t]))
+            launch += 1
+        unw = batch.unwrapped[:, :, :3 * self.total_species].cpu().numpy()
+        eg = batch.energy_grid.cpu().numpy() if want("energy") else None
+        dg = batch.delg0_grid.cpu().numpy() if want("delg_0") else None
+        dr = batch.drift[:, :self.total_species].cpu().numpy() \
+            if self.electric_field_active else None
+        out = []
+        for t in range(T):
+            out.append({"error": error[t],
+                        "step_proc": (np.concatenate(procs[t]) if procs[t]
+                                      else np.zeros(0, np.int32)),
+                        "time": np.concatenate([[0.0]] + times[t]),
+                        "unwrapped": unw[t],
+                        "energy": None if eg is None else eg[t],
+                        "delg_0": None if dg is None else dg[t],
+                        "drift": None if dr is None else dr[t]})
+        return out
 
     def _replay_occupancy(self, occ0, step_proc):
         occ = list(occ0)

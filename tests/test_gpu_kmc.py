@@ -24,14 +24,14 @@ pytestmark = pytest.mark.gpu
 TIME_RTOL = 1e-12
 
 
-def _example_run(name, t_final=None, doping=None):
+def _example_run(name, t_final=None, doping=None, n_traj=1):
     cfg, arr = gio.load(name)
     mat, nb = gio.material(cfg)
     p, r = cfg["params"], cfg["run"]
     sysm = System(mat, nb, gio.hop_list(cfg, arr), arr["pmiv"], p["alpha"],
                   p["r_cut"], p["k_cut"])
     run = Run(sysm, arr["A"], r["temp"], r["ion_charge_type"],
-              r["species_charge_type"], 1, t_final or r["t_final"], r["time_interval"],
+              r["species_charge_type"], n_traj, t_final or r["t_final"], r["time_interval"],
               np.asarray(r["species_count"]), r["initial_occupancy"],
               r["relative_energies"], r["external_field"], doping or r["doping"])
     return cfg, arr, run
@@ -54,6 +54,43 @@ def test_do_kmc_steps_reproduces_shipped_trajectory(cuda_ready, name):
     assert np.abs(ts[1:] / arr["time"][1:] - 1).max() < TIME_RTOL
     assert abs(t[-1] / arr["time_last"][0] - 1) < TIME_RTOL
     assert (d / "Run.log").exists()
+
+
+def test_do_kmc_steps_batched_trajectories_equal_runs_alone(cuda_ready, tmp_path):
+    """n_traj = 8 in one call (serial mode: preproduction seeds traj1..traj8
+    from random_seed, as core.py:2566-2580) advances the eight trajectories
+    together.  Every file of every trajectory equals, byte for byte, the file
+    of that trajectory run alone from its initial_rnd_state.dump, and the
+    module's random state ends where the last trajectory's own run leaves
+    it."""
+    import random as rnd
+    import shutil
+    import time
+    cfg, arr, run8 = _example_run("hematite", t_final=2e-6, n_traj=8)
+    od = cfg["run"]["output_data"]
+    d8 = tmp_path / "together"
+    t0 = time.perf_counter()
+    run8.do_kmc_steps(d8, od, 7, "serial")
+    t_together = time.perf_counter() - t0
+    state8 = rnd.getstate()
+    t_alone = 0.0
+    for i in range(8):
+        d1 = tmp_path / f"alone{i + 1}"
+        d1.mkdir()
+        shutil.copy(d8 / f"traj{i + 1}" / "initial_rnd_state.dump", d1)
+        _, _, run1 = _example_run("hematite", t_final=2e-6)
+        t0 = time.perf_counter()
+        run1.do_kmc_steps(d1, od, 7, "parallel")
+        t_alone += time.perf_counter() - t0
+        names = sorted(f.name for f in (d8 / f"traj{i + 1}").glob("*.npy"))
+        assert "unwrapped_traj.npy" in names and "time_data.npy" in names
+        for name in names:
+            assert (d8 / f"traj{i + 1}" / name).read_bytes() == (d1 / name).read_bytes(), \
+                (i, name)
+        assert len(run8.last_run_steps[i]) == len(run1.last_run_steps[0])
+    assert rnd.getstate() == state8
+    print(f"8 trajectories of examples/Hematite to t = 2e-6: one call {t_together:.2f} s, "
+          f"one call each {t_alone:.2f} s")
 
 
 def test_do_kmc_steps_write_every_step_matches_reference(cuda_ready):

@@ -232,3 +232,22 @@ def test_translated_neighbor_list_equals_full_scan(name, cells):
                                           b.neighbor_system_element_indices[i])
                     assert np.array_equal(np.asarray(a.displacement_vector_list[i]).reshape(-1, 3),
                                           np.asarray(b.displacement_vector_list[i]).reshape(-1, 3))
+
+
+def test_mt19937_blocks_equal_cpython_random():
+    """The drop-in KMC path draws each trajectory's uniforms in blocks with
+    NumPy's MT19937: the values and the state after the used ones equal
+    CPython's random.random() stream (PyCD/core.py:2799, 2802)."""
+    import random
+    from pycd_gb300.core import _Mt19937Stream
+    r = random.Random(12345.678)
+    st = _Mt19937Stream(r.getstate())
+    out = np.empty(5000)
+    st.fill(out)
+    ref = np.array([r.random() for _ in range(5000)])
+    assert np.array_equal(out, ref)
+    st.used(1234)
+    r2 = random.Random(12345.678)
+    for _ in range(1234):
+        r2.random()
+    assert st.state() == r2.getstate()
