@@ -37,6 +37,8 @@ CHUNK = 10000
 B_STEP = 8 * N_CARRIERS * (Z + 1) * (N_CARRIERS + N_DOPANTS) + 16 * N_CARRIERS * (Z + 1)
 T_FINAL, DT = 1e30, 1e27  # time grid wide enough that no trajectory ends by time
 SEED = 20251203
+# queue form of the warp-form launch: rounds of this many steps (0 = static)
+SCHED_STEPS = 0
 # FP64 thread instructions per KMC step of kmc_advance_kernel<8, 2, 1> on this
 # workload (ncu: smsp__sass_thread_inst_executed_op_{dadd,dfma,dmul}_pred_on
 # summed, divided by the launch's KMC steps)
@@ -913,6 +915,9 @@ def main():
     ap.add_argument("--warps", type=int, default=0)
     ap.add_argument("--min-blocks", type=int, default=0,
                     help="2 = the 128-register kernel variant")
+    ap.add_argument("--sched-steps", type=int, default=-1,
+                    help="queue form of the warp-form launch: steps per round "
+                         "(0 = static form, -1 = the default)")
     args = ap.parse_args()
     if args.impl == "reference":
         return reference_arm(args)
@@ -954,12 +959,15 @@ def main():
     if args.min_blocks:
         launch["min_blocks_per_sm"] = args.min_blocks
     # launch shape: autotuned (untimed) unless given; it never changes events
+    sched = SCHED_STEPS if args.sched_steps < 0 else args.sched_steps
     bk = BatchedKmc(tables, occ, seed=SEED, chunk_steps=args.chunk,
                     traj_offset=stream_offset(rank, args.traj), launch=launch,
-                    autotune=0 if (args.lanes or args.warps) else 2000)
+                    autotune=0 if (args.lanes or args.warps) else 2000,
+                    schedule_steps=sched)
     tuned = {"lanes_per_traj": bk.buckets[0].engine.launch.lanes_per_traj,
              "warps_per_block": bk.buckets[0].engine.launch.warps_per_block,
-             "min_blocks_per_sm": bk.buckets[0].engine.launch.min_blocks_per_sm}
+             "min_blocks_per_sm": bk.buckets[0].engine.launch.min_blocks_per_sm,
+             "sched_steps": bk.buckets[0].engine.launch.sched_steps}
     flush = torch.empty(256 * 2 ** 20, dtype=torch.uint8, device="cuda")
     for _ in range(args.warmup):
         bk.step_chunk()

@@ -340,6 +340,19 @@ typedef struct PycdKmcLaunch {
    * some spills); only for at most 2 processes per lane.  Results do not
    * depend on it.                                                          */
   int32_t min_blocks_per_sm;
+  /* Work distribution of the warp form (lanes_per_traj <= 32).  0: static,
+   * each warp keeps its trajectories for the whole launch.  > 0: the
+   * trajectories of one warp ("a set") advance in rounds of sched_steps
+   * steps, and each finished round puts the set's next round on a queue
+   * that free warps take from, so every SM sub-partition stays loaded
+   * until the launch ends.  Events, times and state do not change.
+   * d_sched: caller scratch of sched_capacity int32 values, at least
+   * 4 + sets x ceil(max_steps / sched_steps) with sets = ceil(n_traj /
+   * (32 / lanes)); the library clears it (stream-ordered) before each
+   * launch.  Ignored by the block form.                                    */
+  int32_t sched_steps;
+  int32_t* d_sched;
+  int64_t sched_capacity;
 } PycdKmcLaunch;
 
 /* Advance every trajectory by up to max_steps KMC steps, or until its path

@@ -107,7 +107,9 @@ class KmcRng(C.Structure):
 class KmcLaunch(C.Structure):
     _fields_ = [("lanes_per_traj", C.c_int32), ("warps_per_block", C.c_int32),
                 ("blocks", C.c_int32), ("max_processes", C.c_int32),
-                ("max_carriers", C.c_int32), ("min_blocks_per_sm", C.c_int32)]
+                ("max_carriers", C.c_int32), ("min_blocks_per_sm", C.c_int32),
+                ("sched_steps", C.c_int32), ("d_sched", C.c_void_p),
+                ("sched_capacity", C.c_int64)]
 
 
 MSD_MAX_SPECIES = 64

@@ -5,8 +5,11 @@ rates are fixed balanced-tree sums over the process index), so the shape is
 a pure performance choice.  ``tune`` times short probes of every candidate
 (lanes per trajectory x warps per block x register variant, and one block
 of 2 or 4 warps per trajectory) on the real batch, restoring the
-batch state after each probe, and keeps the fastest.  Results are cached per
-(process count, carrier count, trajectory count) in-process.
+batch state after each probe, and keeps the fastest.  Results are cached
+in-process per (each system's site-count bucket, slots and number of
+charged sites; process count, carrier count, trajectory count): the array's
+size sets how much of it the L2 holds, so a shape tuned on a 300-site
+lattice is not reused for a 20,000-site one.
 """
 import numpy as np
 
@@ -34,6 +37,20 @@ def candidates(max_processes, max_carriers):
     return out
 
 
+def _size_bucket(n_sites):
+    """Site counts in factors of two (300-599, 600-1,199, ...)."""
+    return int(np.floor(np.log2(max(1, n_sites) / 300.0))) if n_sites >= 300 else -1
+
+
+def cache_key(engine, batch):
+    systems = tuple(sorted({(_size_bucket(t.n_sites), int(t.n_slots),
+                             int(getattr(t, "q_fixed", None) is not None
+                                 and int((t.q_fixed != 0).sum().item())))
+                            for t in engine.tables}))
+    return (systems, int(engine.launch.max_processes), int(engine.launch.max_carriers),
+            int(batch.n_traj))
+
+
 def _apply(engine, shape):
     engine.launch.lanes_per_traj = shape["lanes_per_traj"]
     engine.launch.warps_per_block = shape["warps_per_block"]
@@ -44,8 +61,7 @@ def tune(engine, batch, rng, probe_steps=200, reps=2, stream=None):
     """Pick the fastest launch shape for (engine, batch); sets it on the
     engine and returns ``{"best": shape, "table": [(shape, ms), ...]}``."""
     import torch
-    key = (int(engine.launch.max_processes), int(engine.launch.max_carriers),
-           int(batch.n_traj))
+    key = cache_key(engine, batch)
     if key in _CACHE:
         best = _CACHE[key]
         _apply(engine, best)

@@ -37,10 +37,12 @@ class BatchedKmc(object):
     def __init__(self, tables, occupancy, sys_index=None, seed=0,
                  chunk_steps=10000, unwrapped=False, step_capacity=0,
                  launch=None, use_graph=True, traj_offset=0, step_limit=None,
-                 autotune=False, n_carriers=None):
+                 autotune=False, n_carriers=None, schedule_steps=0):
         """``occupancy``: T x max_carriers initial sites (rows padded beyond
         each system's carrier count); ``sys_index``: system of each
-        trajectory (default 0); ``step_limit``: per-trajectory step budget."""
+        trajectory (default 0); ``step_limit``: per-trajectory step budget;
+        ``schedule_steps``: > 0 runs the warp-form launches in the queue form
+        (rounds of that many steps handed to free warps; same results)."""
         import torch
         self.tables = list(tables) if isinstance(tables, (list, tuple)) else [tables]
         occ = np.asarray(occupancy, dtype=np.int32)
@@ -76,6 +78,8 @@ class BatchedKmc(object):
                          step_limit=None if limits is None else limits[idx])
             eng = KmcEngine(None, launch, share=self.master)
             eng.restrict_shape(sys_index[idx])
+            if schedule_steps:
+                eng.schedule(schedule_steps)
             ids = torch.as_tensor((idx + int(traj_offset)).astype(np.uint64).view(np.int64)
                                   ).cuda()
             bk = _Bucket(idx, b, eng, ids)

@@ -326,6 +326,8 @@ int pycd_kmc_advance_uploaded(int32_t n_systems, const PycdKmcState* state,
   a.out = *out;
   a.rng = *rng;
   a.max_steps = max_steps;
+  a.sched = nullptr;
+  a.sched_steps = a.sched_rounds = a.sched_sets = 0;
   if (max_steps == 0) return PYCD_OK;
   return kmc_launch(a, launch->max_processes, launch->max_carriers, launch,
                     (cudaStream_t)stream);

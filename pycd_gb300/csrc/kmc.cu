@@ -234,15 +234,41 @@ int kmc_launch(const KmcArgs& a, int max_np, int max_nc,
   const int64_t warps_needed = (a.st.n_traj + tpw - 1) / tpw;
   int blocks = launch && launch->blocks ? launch->blocks
                                         : (int)((warps_needed + wpb - 1) / wpb);
+  KmcArgs b = a;
+  if (launch && launch->sched_steps > 0) {
+    // queue form: rounds of sched_steps steps handed to free warps
+    PYCD_REQUIRE(launch->d_sched != nullptr, "sched_steps > 0 needs d_sched");
+    const int64_t sets = warps_needed;
+    const int64_t rounds = (a.max_steps + launch->sched_steps - 1) / launch->sched_steps;
+    const int64_t need = 4 + sets * rounds;
+    PYCD_REQUIRE(need < ((int64_t)1 << 30), "too many scheduling rounds (%lld)",
+                 (long long)need);
+    PYCD_REQUIRE(need <= launch->sched_capacity,
+                 "d_sched holds %lld values; this launch needs %lld",
+                 (long long)launch->sched_capacity, (long long)need);
+    PYCD_CUDA(cudaMemsetAsync(launch->d_sched, 0, sizeof(int32_t) * (size_t)need, s));
+    b.sched = launch->d_sched;
+    b.sched_steps = launch->sched_steps;
+    b.sched_rounds = rounds;
+    b.sched_sets = sets;
+    if (!launch->blocks) {
+      // two warps per SM sub-partition, or one per set when fewer
+      int dev = 0, sms = 0;
+      PYCD_CUDA(cudaGetDevice(&dev));
+      PYCD_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+      const int64_t warps = sets < 8LL * sms ? sets : 8LL * sms;
+      blocks = (int)((warps + wpb - 1) / wpb);
+    }
+  }
   if (blocks < 1) blocks = 1;
   cudaError_t e = cudaErrorInvalidConfiguration;
   bool found = false;
   if (minb == 2) {
-    e = kmc_launch_capped(a, G, MAXP, wpb, blocks, s, &found);
+    e = kmc_launch_capped(b, G, MAXP, wpb, blocks, s, &found);
   } else {
 #define PYCD_KMC_CASE(g_, m_)                                                \
   if (!found && G == g_ && MAXP == m_) {                                     \
-    e = launch_g<g_, m_, 1>(a, wpb, blocks, s);                              \
+    e = launch_g<g_, m_, 1>(b, wpb, blocks, s);                              \
     found = true;                                                            \
   }
     PYCD_KMC_SHAPES(PYCD_KMC_CASE)

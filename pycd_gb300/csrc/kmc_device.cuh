@@ -594,11 +594,16 @@ struct TimeChain {
 };
 
 // One group of G lanes advances one trajectory by up to max_steps steps.
+// The trajectory's state is read through the L2 (__ldcg): in the queue
+// form its previous round may have run on another SM.  t_launch: the global
+// timer when the launch began for this warp (the time limit's origin), or 0
+// to take it when the trajectory starts.
 template <int G, int MAXP>
 __device__ void advance_trajectory(const KmcArgs& a, int64_t t, int g,
-                                   unsigned gmask) {
+                                   unsigned gmask, int64_t max_steps,
+                                   uint64_t t_launch) {
   const PycdKmcState& st = a.st;
-  int32_t status = st.d_status[t];
+  int32_t status = __ldcg(st.d_status + t);
   if (status != PYCD_TRAJ_RUNNING) return;
   const int sys_id = st.d_sys_index ? st.d_sys_index[t] : 0;
   if (sys_id < 0 || sys_id >= a.n_systems) {
@@ -640,21 +645,21 @@ __device__ void advance_trajectory(const KmcArgs& a, int64_t t, int g,
   const int n_disp = 3 * NC;
   const int n_regs = (n_disp + 1 + G - 1) / G;
   const int64_t sbase = t * 3 * (int64_t)MC;
-  int occ = (g < NC) ? st.d_occ[t * MC + g] : 0;
+  int occ = (g < NC) ? __ldcg(st.d_occ + t * MC + g) : 0;
   double dacc[kSlotRegs], racc[kSlotRegs];
   {
-    const double e0 = st.d_energy ? st.d_energy[t] : 0.0;
+    const double e0 = st.d_energy ? __ldcg(st.d_energy + t) : 0.0;
 #pragma unroll
     for (int r = 0; r < kSlotRegs; ++r) {
       const int j = g + G * r;
-      dacc[r] = (j < n_disp) ? st.d_disp[sbase + j] : (j == n_disp ? e0 : 0.0);
-      racc[r] = (j < n_disp) ? st.d_last_row[sbase + j] : 0.0;
+      dacc[r] = (j < n_disp) ? __ldcg(st.d_disp + sbase + j) : (j == n_disp ? e0 : 0.0);
+      racc[r] = (j < n_disp) ? __ldcg(st.d_last_row + sbase + j) : 0.0;
     }
   }
-  double sim_time = st.d_time[t];
-  int64_t step = st.d_step[t];
-  int64_t start_path = st.d_path_index[t];
-  int64_t ucur = st.d_u_cursor ? st.d_u_cursor[t] : 0;
+  double sim_time = __ldcg(st.d_time + t);
+  int64_t step = (int64_t)__ldcg((const long long*)st.d_step + t);
+  int64_t start_path = (int64_t)__ldcg((const long long*)st.d_path_index + t);
+  int64_t ucur = st.d_u_cursor ? (int64_t)__ldcg((const long long*)st.d_u_cursor + t) : 0;
   const int64_t step_limit = st.d_step_limit ? st.d_step_limit[t] : INT64_MAX;
   const double* ubase = a.rng.d_uniforms
                             ? a.rng.d_uniforms + (int64_t)t * a.rng.u_stride
@@ -684,7 +689,7 @@ __device__ void advance_trajectory(const KmcArgs& a, int64_t t, int g,
   // cooperative stop: lane 0 of the group checks every `poll` steps
   const bool polling = st.d_cancel != nullptr || st.time_limit_ns > 0;
   const int64_t poll = st.poll_interval > 0 ? st.poll_interval : 256;
-  const uint64_t t_start = polling ? global_timer_ns() : 0;
+  const uint64_t t_start = polling ? (t_launch ? t_launch : global_timer_ns()) : 0;
 
   // ---- process cache: geometry, constants, carrier sums ----------------
   ProcCache<MAXP> pc;
@@ -697,13 +702,13 @@ __device__ void advance_trajectory(const KmcArgs& a, int64_t t, int g,
 #pragma unroll
     for (int j = 0; j < MAXP; ++j) {
       const int p = g * MAXP + j;
-      if (pc.valid[j]) { pc.P[j] = csum[p]; pc.Q[j] = csum[half + p]; }
+      if (pc.valid[j]) { pc.P[j] = __ldcg(csum + p); pc.Q[j] = __ldcg(csum + half + p); }
     }
   } else {
     fresh_sums<G, MAXP>(sy, g, gmask, occ, pc);
   }
 
-  for (int64_t it = 0; it < a.max_steps; ++it) {
+  for (int64_t it = 0; it < max_steps; ++it) {
     if (step >= step_limit) { status = PYCD_TRAJ_STEP_LIMIT; break; }
     if (polling && (it & (poll - 1)) == 0) {
       int32_t stop = (g == 0) ? kmc_stop_request(st, t, t_start) : 0;
@@ -825,9 +830,9 @@ __device__ void advance_trajectory(const KmcArgs& a, int64_t t, int g,
         occ = n_sel;
         if (a.out.d_drift) {
           double* dr = a.out.d_drift + ((int64_t)t * MC + g) * 3;
-          dr[0] = dadd(dr[0], dmul(h0, k_sel));
-          dr[1] = dadd(dr[1], dmul(h1, k_sel));
-          dr[2] = dadd(dr[2], dmul(h2, k_sel));
+          dr[0] = dadd(__ldcg(dr), dmul(h0, k_sel));
+          dr[1] = dadd(__ldcg(dr + 1), dmul(h1, k_sel));
+          dr[2] = dadd(__ldcg(dr + 2), dmul(h2, k_sel));
         }
       }
       const int j0 = 3 * c_sel;
@@ -925,6 +930,77 @@ __device__ void advance_trajectory(const KmcArgs& a, int64_t t, int g,
   }
 }
 
+__device__ __forceinline__ int32_t ld_acquire_gpu(const int32_t* p) {
+  int32_t v;
+  asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release_gpu(int32_t* p, int32_t v) {
+  asm volatile("st.release.gpu.global.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// bounded waits of the queue form (each ~0.25 us or more)
+constexpr uint32_t kQueueWaitLimit = 1u << 23;
+
+// Queue form (PycdKmcLaunch.sched_steps > 0).  A set is the 32/G
+// trajectories one warp advances together.  Items are (round, set): items
+// 0 .. sets-1 are round 0 of every set; a warp that finishes round r of a
+// set (its state written and fenced) queues round r + 1, so the queue holds
+// only rounds whose previous round is complete, in the order they became
+// ready.  Warps take items in queue order; a warp whose item is not queued
+// yet waits for it (bounded; every earlier item is held by a running warp,
+// so the wait ends).  Each round advances min(sched_steps, steps left).
+template <int G, int MAXP>
+__device__ void kmc_queue_loop(const KmcArgs& a, int lane, int sub, int g,
+                               unsigned gmask) {
+  constexpr int64_t gpw = 32 / G;
+  const int64_t sets = a.sched_sets, total = sets * a.sched_rounds;
+  int32_t* head = a.sched;
+  int32_t* tail = a.sched + 1;
+  int32_t* fail = a.sched + 2;
+  int32_t* items = a.sched + 4;
+  const bool polling = a.st.d_cancel != nullptr || a.st.time_limit_ns > 0;
+  const uint64_t t_launch = polling ? global_timer_ns() : 0;
+  while (true) {
+    int32_t idx = 0;
+    if (lane == 0) idx = atomicAdd(head, 1);
+    idx = __shfl_sync(0xffffffffu, idx, 0);
+    if (idx >= total) break;
+    int64_t item = idx;
+    if (idx >= sets) {
+      // lane 0 waits and the warp takes its answer, so that every lane
+      // makes the same choice
+      int32_t v = 0;
+      if (lane == 0) {
+        for (uint32_t w = 0; w < kQueueWaitLimit; ++w) {
+          v = ld_acquire_gpu(items + (idx - sets));
+          if (v != 0) break;
+          __nanosleep(256);
+        }
+        if (v == 0) atomicExch(fail, 1);  // cannot happen while every
+                                          // taken item is in progress
+      }
+      v = __shfl_sync(0xffffffffu, v, 0);
+      if (v == 0) break;
+      __threadfence();
+      item = (int64_t)v - 1;
+    }
+    const int64_t r = item / sets, set = item - r * sets;
+    const int64_t left = a.max_steps - r * a.sched_steps;
+    const int64_t steps = left < a.sched_steps ? left : a.sched_steps;
+    const int64_t t = set * gpw + sub;
+    if (t < a.st.n_traj) advance_trajectory<G, MAXP>(a, t, g, gmask, steps, t_launch);
+    if (r + 1 < a.sched_rounds) {
+      __threadfence();  // this lane's state writes before the round is queued
+      __syncwarp();
+      if (lane == 0) {
+        const int32_t j = atomicAdd(tail, 1);
+        st_release_gpu(items + j, (int32_t)((r + 1) * sets + set + 1));
+      }
+    }
+  }
+}
+
 // MINB > 1 caps the registers so that MINB blocks of 256 threads fit on an
 // SM: more resident warps to hide the latency of the row loads, at the price
 // of spills.  The launch shape picks the variant (it does not change results).
@@ -935,12 +1011,16 @@ __global__ void __launch_bounds__(256, MINB) kmc_advance_kernel(KmcArgs a) {
   const int g = lane - sub * G;
   const unsigned gmask =
       (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << (sub * G));
+  if (a.sched) {
+    kmc_queue_loop<G, MAXP>(a, lane, sub, g, gmask);
+    return;
+  }
   const int64_t groups_per_warp = 32 / G;
   const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int64_t n_warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
   for (int64_t t = warp * groups_per_warp + sub; t < a.st.n_traj;
        t += n_warps * groups_per_warp) {
-    advance_trajectory<G, MAXP>(a, t, g, gmask);
+    advance_trajectory<G, MAXP>(a, t, g, gmask, a.max_steps, 0);
   }
 }
 

@@ -24,6 +24,12 @@ struct KmcArgs {
   PycdKmcOutputs out;
   PycdKmcRng rng;
   int64_t max_steps;
+  // queue form of the warp-form launch (PycdKmcLaunch.sched_steps);
+  // sched == nullptr for the static form.  sched[0]: items taken,
+  // sched[1]: items queued, sched[2]: a wait ran out, sched[4 + j]: the
+  // j-th queued item (round * sets + set + 1)
+  int32_t* sched;
+  int64_t sched_steps, sched_rounds, sched_sets;
 };
 
 int kmc_launch(const KmcArgs& a, int max_np, int max_nc,

@@ -310,11 +310,36 @@ class KmcEngine(object):
         r.traj_offset = int(traj_offset)
         return r
 
+    def schedule(self, steps):
+        """Queue form of the warp-form launches: trajectories advance in
+        rounds of ``steps`` steps handed to free warps (0 = static form).
+        Results do not change; the scratch is allocated on first use."""
+        self.launch.sched_steps = int(steps)
+        return self
+
+    def _sched_scratch(self, batch, max_steps):
+        import torch
+        G = int(self.launch.lanes_per_traj or 0)
+        if self.launch.sched_steps <= 0 or G > 32:
+            self.launch.d_sched = None
+            self.launch.sched_capacity = 0
+            return
+        gpw = 32 // G if G else 1  # lanes not chosen yet: one trajectory per set
+        sets = -(-batch.n_traj // gpw)
+        need = 4 + sets * -(-int(max_steps) // int(self.launch.sched_steps))
+        buf = getattr(self, "_sched", None)
+        if buf is None or buf.numel() < need:
+            buf = torch.zeros(need, dtype=torch.int32, device=_dev())
+            self._sched = buf
+        self.launch.d_sched = buf.data_ptr()
+        self.launch.sched_capacity = buf.numel()
+
     def advance(self, batch, max_steps, rng, stream=None):
         """Advance every running trajectory by up to ``max_steps`` steps.
         Asynchronous on ``stream``; the structs are passed by value."""
         if not self._uploaded:
             self.upload(stream)
+        self._sched_scratch(batch, max_steps)
         st = batch.state_struct()
         out = batch.outputs_struct()
         nat.check(nat.lib().pycd_kmc_advance_uploaded(

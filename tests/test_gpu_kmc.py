@@ -614,3 +614,34 @@ def test_cancel_flag_stops_one_trajectory_during_a_launch(cuda_ready, lanes):
     eng.advance(b, n, eng.rng_struct(seed=9))
     torch.cuda.synchronize()
     assert b.step[victim].item() == n
+
+
+@pytest.mark.parametrize("lanes,T", [(8, 600), (8, 16384), (4, 2000), (16, 3000)])
+def test_queue_form_equals_static_form(cuda_ready, lanes, T):
+    """The queue form (rounds of 128 steps handed to free warps, more sets
+    than warps for T = 16,384) gives the static form's events, times and
+    state bit for bit, with step budgets that end inside rounds, and no
+    wait of the queue runs out."""
+    import torch
+    sysm, tables, run, cfg, arr = _corundum3600()
+    n = 1500
+    rng = np.random.default_rng(T + lanes)
+    occ = np.stack([rng.choice(3600, size=4, replace=False) for _ in range(T)])
+    limits = rng.integers(200, n + 1, T)
+    out = []
+    for sched in (0, 128):
+        eng = KmcEngine(tables, launch={"lanes_per_traj": lanes}).schedule(sched)
+        b = KmcBatch(occ, step_limit=limits, step_capacity=n)
+        eng.advance(b, n, eng.rng_struct(seed=41))
+        torch.cuda.synchronize()
+        if sched:
+            assert eng._sched[2].item() == 0
+            assert eng._sched[0].item() >= eng._sched[1].item()
+        st = _state(b)
+        st["status"] = b.status.cpu().numpy()
+        st["proc"] = b.step_proc.cpu().numpy()
+        st["tlog"] = b.step_time.cpu().numpy()
+        out.append(st)
+    assert (out[0]["step"] == limits).all()
+    for k in out[0]:
+        assert np.array_equal(out[0][k], out[1][k]), k
