@@ -129,6 +129,15 @@ typedef struct PycdEwaldDesc {
                                  * get_precomputed_array_real (core.py:1594-
                                  * 1596), the Fourier part alone
                                  * get_precomputed_array_fourier (1598-1602)  */
+  /* Supercell layout, or basis_sites = 0 when unknown.  basis_sites > 0
+   * states that site i is basis site i % basis_sites of cell
+   * c = i / basis_sites, cells in C order over supercell[0..2] (the last
+   * index fastest), and that site positions repeat with the supercell's
+   * cells.  Every entry then depends only on (basis_i, basis_j, cell offset
+   * modulo the supercell), so the split modes take the real-space and self
+   * terms of all rows from the first basis_sites rows.                    */
+  int32_t supercell[3];
+  int32_t basis_sites;
 } PycdEwaldDesc;
 
 #define PYCD_EWALD_PART_REAL 1     /* erfc(sqrt(alpha) r)/(2 r eps), r < r_cut */

@@ -56,7 +56,8 @@ class EwaldDesc(C.Structure):
                 ("sim_cell", C.c_double * 9), ("sim_cell_inv", C.c_double * 9),
                 ("pbc", C.c_int32 * 3), ("alpha", C.c_double),
                 ("r_cut", C.c_double), ("volume", C.c_double),
-                ("dielectric", C.c_double), ("parts", C.c_int32)]
+                ("dielectric", C.c_double), ("parts", C.c_int32),
+                ("supercell", C.c_int32 * 3), ("basis_sites", C.c_int32)]
 
 
 EWALD_PART_REAL = 1

@@ -429,9 +429,19 @@ struct EwaldWs {
   double* ck;
   double* F;
   int64_t ld;
+  double* real_rows;  // split modes on a translation-invariant supercell
 };
 
 static int64_t feature_ld(int64_t K) { return ((2 * K + GK - 1) / GK) * GK; }
+
+// Split modes of a whole array on a described supercell take the real-space
+// and self terms from the first basis_sites rows (RealTable in
+// ewald_split.cu) instead of a pass over all N^2 pairs.
+static bool use_real_table(const PycdEwaldDesc* d, int mode) {
+  const int parts = d->parts ? d->parts : PYCD_EWALD_PART_ALL;
+  return (mode == PYCD_EWALD_BF16X3 || mode == PYCD_EWALD_TF32X3) &&
+         parts == PYCD_EWALD_PART_ALL && d->basis_sites > 0 && d->n_kvec > 0;
+}
 
 static size_t ewald_ws_layout(const PycdEwaldDesc* d, int mode, EwaldWs* ws,
                               char* base) {
@@ -450,6 +460,8 @@ static size_t ewald_ws_layout(const PycdEwaldDesc* d, int mode, EwaldWs* ws,
     w.ld = feature_ld(K);
     w.F = (double*)take(sizeof(double) * (size_t)n * (size_t)w.ld);
   }
+  if (use_real_table(d, mode))
+    w.real_rows = (double*)take(sizeof(double) * (size_t)d->basis_sites * (size_t)n);
   if (ws) *ws = w;
   return off;
 }
@@ -470,6 +482,13 @@ int ewald_validate(const PycdEwaldDesc* d, int mode) {
   if (mode != PYCD_EWALD_FP64_DIRECT)
     PYCD_REQUIRE(d->d_cart != nullptr, "feature modes need d_cart");
   PYCD_REQUIRE(d->n_sites <= 65535, "n_sites above 65535 is not supported");
+  PYCD_REQUIRE(d->basis_sites >= 0, "basis_sites must be >= 0");
+  if (d->basis_sites > 0) {
+    PYCD_REQUIRE(d->supercell[0] > 0 && d->supercell[1] > 0 && d->supercell[2] > 0 &&
+                     (int64_t)d->basis_sites * d->supercell[0] * d->supercell[1] *
+                             d->supercell[2] == d->n_sites,
+                 "basis_sites x supercell cells must equal n_sites");
+  }
   return PYCD_OK;
 }
 
@@ -479,7 +498,7 @@ size_t ewald_workspace_bytes(const PycdEwaldDesc* d, int mode) {
 
 int ewald_build_split(const PycdEwaldDesc* d, int mode, double* out,
                       const double* kc, const double* k2, const double* ck,
-                      void* ws, size_t ws_bytes, cudaStream_t s);
+                      const double* real_rows, void* ws, size_t ws_bytes, cudaStream_t s);
 size_t ewald_split_workspace_bytes(const PycdEwaldDesc* d, int mode);
 
 int ewald_build(const PycdEwaldDesc* d, int mode, double* out, void* ws,
@@ -556,9 +575,18 @@ int ewald_build(const PycdEwaldDesc* d, int mode, double* out, void* ws,
       PYCD_CUDA(cudaEventRecord(e2, s));
     }
   } else {
-    ewald_pair_kernel<false><<<grid, 256, 0, s>>>(
-        g, sqrt_alpha, r_cut, d->dielectric, self_term, w.kc, w.k2,
-        w.ck, 0, out);
+    if (w.real_rows) {
+      // the first basis_sites rows of the real-space and self terms only;
+      // the split kernel writes every entry from them
+      dim3 tgrid((unsigned)((n + 255) / 256), (unsigned)d->basis_sites);
+      ewald_pair_kernel<false><<<tgrid, 256, 0, s>>>(
+          g, sqrt_alpha, r_cut, d->dielectric, self_term, w.kc, w.k2,
+          w.ck, 0, w.real_rows);
+    } else {
+      ewald_pair_kernel<false><<<grid, 256, 0, s>>>(
+          g, sqrt_alpha, r_cut, d->dielectric, self_term, w.kc, w.k2,
+          w.ck, 0, out);
+    }
     PYCD_CUDA(cudaGetLastError());
     if (timing) PYCD_CUDA(cudaEventRecord(e1, s));
     if (K > 0) {
@@ -571,7 +599,7 @@ int ewald_build(const PycdEwaldDesc* d, int mode, double* out, void* ws,
         PYCD_CUDA(cudaGetLastError());
       } else {
         const size_t base = ewald_workspace_bytes(d, mode);
-        rc = ewald_build_split(d, mode, out, w.kc, w.k2, w.ck,
+        rc = ewald_build_split(d, mode, out, w.kc, w.k2, w.ck, w.real_rows,
                                (char*)ws + base, ws_bytes - base, s);
         if (rc) return rc;
       }

@@ -69,8 +69,38 @@ struct SplitErr {
   int* flag;  // device int, set non-zero on a timed-out wait
 };
 
+// Real-space + self terms of a translation-invariant supercell: rows holds
+// the first nb rows of that part (cell 0, basis sites 0..nb-1, all n
+// columns); entry (i, j) is rows[b_i][offset(c_j - c_i) * nb + b_j] with
+// site i = c_i nb + b_i and cell offsets taken modulo (s0, s1, s2).  With
+// rows == nullptr the output already holds those terms and the epilogue
+// adds to it.
+struct RealTable {
+  const double* rows;
+  int nb, s0, s1, s2;
+};
+
+// (basis, cell x, y, z) of site i in the layout of RealTable
+__device__ __forceinline__ void site_cell(const RealTable& rt, int64_t i, int& b, int& x,
+                                          int& y, int& z) {
+  const int64_t c = i / rt.nb;
+  b = (int)(i - c * rt.nb);
+  const int64_t yz = (int64_t)rt.s1 * rt.s2;
+  x = (int)(c / yz);
+  const int64_t r = c - (int64_t)x * yz;
+  y = (int)(r / rt.s2);
+  z = (int)(r - (int64_t)y * rt.s2);
+}
+
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
   return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ double2 cmul2(double2 a, double2 b) {
+  return make_double2(fma(a.x, b.x, -__dmul_rn(a.y, b.y)), fma(a.x, b.y, __dmul_rn(a.y, b.x)));
+}
+__device__ __forceinline__ float2 cmulf(float2 a, float2 b) {
+  return make_float2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x));
 }
 
 __device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
@@ -205,7 +235,7 @@ __global__ void __launch_bounds__(192, 1)
     ewald_split_kernel(const __grid_constant__ CUtensorMap map_h,
                        const __grid_constant__ CUtensorMap map_l, int64_t n,
                        int k_blocks, int chunk_blocks, int nb, double* __restrict__ out,
-                       const double* __restrict__ diag_sum, SplitErr err) {
+                       const double* __restrict__ diag_sum, RealTable rt, SplitErr err) {
   const double diag_value = *diag_sum;
   int bi = 0, bj = 0;
   // lower tiles are written as mirrors; CTAs without a tile leave at once
@@ -369,7 +399,13 @@ __global__ void __launch_bounds__(192, 1)
     }
     if (ok) {
       // diagonal: F_i . F_i = sum_k w_k (cos^2 + sin^2) = sum_k w_k exactly,
-      // taken from the FP64 weight sum instead of the FP32 accumulation
+      // taken from the FP64 weight sum instead of the FP32 accumulation.
+      // With a real-space table the entry (and its mirror) is written once
+      // as table value + Fourier value; otherwise it is added to the real
+      // and self terms already in the output.
+      int rb = 0, rx = 0, ry = 0, rz = 0;
+      if (rt.rows && row < n) site_cell(rt, row, rb, rx, ry, rz);
+      const double* trow = rt.rows ? rt.rows + (int64_t)rb * n : nullptr;
 #pragma unroll 1
       for (int cb = 0; cb < kTile / 16; ++cb) {
         const uint32_t off = (uint32_t)(cb * 16);
@@ -379,14 +415,35 @@ __global__ void __launch_bounds__(192, 1)
         tmem_ld_wait();
         const int64_t col0 = (int64_t)bj * kTile + cb * 16;
         if (row < n) {
+          int cbs = 0, cx = 0, cy = 0, cz = 0;
+          if (trow) site_cell(rt, col0, cbs, cx, cy, cz);
 #pragma unroll
           for (int q = 0; q < 16; ++q) {
             const int64_t col = col0 + q;
             if (col < n) {
               double v = (double)__uint_as_float(h[q]) + (double)__uint_as_float(l[q]);
               if (col == row) v = diag_value;
-              out[row * n + col] += v;
-              if (bi != bj) out[col * n + row] += v;
+              if (trow) {
+                int dx = cx - rx, dy = cy - ry, dz = cz - rz;
+                if (dx < 0) dx += rt.s0;
+                if (dy < 0) dy += rt.s1;
+                if (dz < 0) dz += rt.s2;
+                const int64_t o = (((int64_t)dx * rt.s1 + dy) * rt.s2 + dz) * rt.nb + cbs;
+                const double a = __dadd_rn(__ldg(trow + o), v);
+                out[row * n + col] = a;
+                if (bi != bj) out[col * n + row] = a;
+              } else {
+                out[row * n + col] += v;
+                if (bi != bj) out[col * n + row] += v;
+              }
+            }
+            // next column's site in the layout
+            if (trow && ++cbs == rt.nb) {
+              cbs = 0;
+              if (++cz == rt.s2) {
+                cz = 0;
+                if (++cy == rt.s1) { cy = 0; ++cx; }
+              }
             }
           }
         }
@@ -422,27 +479,122 @@ __global__ void weight_sum_kernel(const double* __restrict__ k2,
   if (threadIdx.x == 0) *out = red[0];
 }
 
-// Split the FP64 feature rows into hi/lo parts, zero-padded to `ld` columns.
+// Feature rows F_i = [sqrt(w_k) cos(k.r_i), sqrt(w_k) sin(k.r_i)]_k,
+// w_k = 2 c_k / (k^2 eps), written directly as the hi + lo operands of the
+// split contraction (no FP64 copy of F), zero-padded to `ld` columns.
+// As in the FP64 feature kernel, every k is m0 b0 + m1 b1 + m2 b2, so
+// e^{i k.r} is the product of per-site tables e^{i m phi_d}, phi_d = b_d . r,
+// built with FP64 sincos.  The BF16 split keeps ~16 bits of each feature,
+// so its two complex products run in FP32 (accurate to ~2e-7, far inside
+// the split); the TF32 split keeps ~22 bits and takes them in FP64.  A block
+// whose tables would not fit evaluates sincos(k . r) in FP64.
+constexpr int kSfSites = 16;
+constexpr int kSfThreads = 256;
+constexpr int kSfSmem = 96 * 1024;
+
 template <bool TF32>
-__global__ void split_features_kernel(const double* __restrict__ F, int64_t n,
-                                      int64_t ldf, int64_t kdim, int64_t ld,
-                                      void* __restrict__ hi, void* __restrict__ lo) {
-  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const int64_t r = blockIdx.y;
-  if (r >= n || c >= ld) return;
-  const double f = c < kdim ? F[r * ldf + c] : 0.0;
-  if (TF32) {
-    uint32_t hb, lb;
-    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(hb) : "f"((float)f));
-    const float h = __uint_as_float(hb);
-    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(lb) : "f"((float)(f - (double)h)));
-    ((float*)hi)[r * ld + c] = h;
-    ((float*)lo)[r * ld + c] = __uint_as_float(lb);
-  } else {
-    const __nv_bfloat16 h = __double2bfloat16(f);
-    const __nv_bfloat16 l = __double2bfloat16(f - (double)__bfloat162float(h));
-    ((__nv_bfloat16*)hi)[r * ld + c] = h;
-    ((__nv_bfloat16*)lo)[r * ld + c] = l;
+__global__ void __launch_bounds__(kSfThreads)
+split_features_direct_kernel(const double* __restrict__ cart, int64_t n,
+                             const int32_t* __restrict__ kv, Mat3 recip,
+                             const double* __restrict__ kc, const double* __restrict__ k2,
+                             const double* __restrict__ ck, int64_t K, double eps,
+                             int64_t ld, void* __restrict__ hi, void* __restrict__ lo) {
+  extern __shared__ double2 tab[];  // [kSfSites][T], float2 pairs for BF16
+  __shared__ int mmax[3];
+  __shared__ double phi[kSfSites][3];
+  const int tid = threadIdx.x;
+  const int64_t site0 = (int64_t)blockIdx.x * kSfSites;
+  const int ns = (int)min((int64_t)kSfSites, n - site0);
+  if (tid < 3) mmax[tid] = 0;
+  if (tid < kSfSites * 3) {
+    const int si = tid / 3, d = tid % 3;
+    double v = 0.0;
+    if (si < ns) {
+      const double* r = cart + (site0 + si) * 3;
+      v = fma(recip.m[d * 3 + 2], r[2], fma(recip.m[d * 3 + 1], r[1], __dmul_rn(recip.m[d * 3], r[0])));
+    }
+    phi[si][d] = v;
+  }
+  __syncthreads();
+  for (int64_t k = tid; k < K; k += kSfThreads) {
+    atomicMax(&mmax[0], abs(kv[k * 3]));
+    atomicMax(&mmax[1], abs(kv[k * 3 + 1]));
+    atomicMax(&mmax[2], abs(kv[k * 3 + 2]));
+  }
+  __syncthreads();
+  const int M0 = mmax[0], M1 = mmax[1], M2 = mmax[2];
+  const int off1 = 2 * M0 + 1, off2 = off1 + 2 * M1 + 1, T = off2 + 2 * M2 + 1;
+  const int64_t esz = TF32 ? sizeof(double2) : sizeof(float2);
+  const bool use_tab = (int64_t)T * kSfSites * esz <= kSfSmem;
+  float2* tabf = (float2*)tab;
+  if (use_tab) {
+    for (int e = tid; e < kSfSites * T; e += kSfThreads) {
+      const int si = e / T, j = e - si * T;
+      const int d = j < off1 ? 0 : (j < off2 ? 1 : 2);
+      const int m = j - (d == 0 ? M0 : (d == 1 ? off1 + M1 : off2 + M2));
+      double sv, cv;
+      sincos(__dmul_rn((double)m, phi[si][d]), &sv, &cv);
+      if (TF32) tab[e] = make_double2(cv, sv);
+      else tabf[e] = make_float2((float)cv, (float)sv);
+    }
+  }
+  __syncthreads();
+  for (int64_t k = tid; 2 * k < ld; k += kSfThreads) {
+    const int64_t c = 2 * k;
+    const bool live = k < K;
+    double w = 0.0;
+    int m0 = 0, m1 = 0, m2 = 0;
+    if (live) {
+      w = sqrt(2.0 * ck[k] / (k2[k] * eps));
+      m0 = kv[k * 3];
+      m1 = kv[k * 3 + 1];
+      m2 = kv[k * 3 + 2];
+    }
+    for (int si = 0; si < ns; ++si) {
+      const int64_t at = (site0 + si) * ld + c;
+      if (TF32) {
+        double2 z = make_double2(0.0, 0.0);
+        if (live) {
+          if (use_tab) {
+            const double2* t = tab + si * T;
+            z = cmul2(cmul2(t[M0 + m0], t[off1 + M1 + m1]), t[off2 + M2 + m2]);
+          } else {
+            const double* r = cart + (site0 + si) * 3;
+            sincos(kc[k * 3] * r[0] + kc[k * 3 + 1] * r[1] + kc[k * 3 + 2] * r[2], &z.y, &z.x);
+          }
+        }
+        const double f0 = w * z.x, f1 = w * z.y;
+        uint32_t h0, h1, l0, l1;
+        asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(h0) : "f"((float)f0));
+        asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(h1) : "f"((float)f1));
+        asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(l0) : "f"((float)(f0 - (double)__uint_as_float(h0))));
+        asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(l1) : "f"((float)(f1 - (double)__uint_as_float(h1))));
+        // c is even and ld a multiple of 32: 8-byte aligned pairs
+        *(float2*)((float*)hi + at) = make_float2(__uint_as_float(h0), __uint_as_float(h1));
+        *(float2*)((float*)lo + at) = make_float2(__uint_as_float(l0), __uint_as_float(l1));
+      } else {
+        float2 z = make_float2(0.f, 0.f);
+        if (live) {
+          if (use_tab) {
+            const float2* t = tabf + si * T;
+            z = cmulf(cmulf(t[M0 + m0], t[off1 + M1 + m1]), t[off2 + M2 + m2]);
+          } else {
+            const double* r = cart + (site0 + si) * 3;
+            double sv, cv;
+            sincos(kc[k * 3] * r[0] + kc[k * 3 + 1] * r[1] + kc[k * 3 + 2] * r[2], &sv, &cv);
+            z = make_float2((float)cv, (float)sv);
+          }
+        }
+        const float wf = (float)w;
+        const float f0 = wf * z.x, f1 = wf * z.y;
+        const __nv_bfloat16 h0 = __float2bfloat16_rn(f0), h1 = __float2bfloat16_rn(f1);
+        const __nv_bfloat16 l0 = __float2bfloat16_rn(f0 - __bfloat162float(h0));
+        const __nv_bfloat16 l1 = __float2bfloat16_rn(f1 - __bfloat162float(h1));
+        // c is even and ld a multiple of 64: 4-byte aligned pairs
+        *(__nv_bfloat162*)((__nv_bfloat16*)hi + at) = __halves2bfloat162(h0, h1);
+        *(__nv_bfloat162*)((__nv_bfloat16*)lo + at) = __halves2bfloat162(l0, l1);
+      }
+    }
   }
 }
 
@@ -479,27 +631,21 @@ static int64_t split_ld(int64_t kdim, bool tf32) {
 
 static size_t align256s(size_t b) { return (b + 255) & ~(size_t)255; }
 
-// feature matrix F (FP64) is laid out by ewald.cu; here only hi/lo + error
+// hi and lo operands, the time-out flag and the weight sum; the real-space
+// table (when used) is laid out by ewald.cu
 size_t ewald_split_workspace_bytes(const PycdEwaldDesc* d, int mode) {
   const bool tf32 = mode == PYCD_EWALD_TF32X3;
   const int64_t kdim = 2 * d->n_kvec;
   const int64_t ld = split_ld(kdim, tf32);
   const size_t es = tf32 ? 4 : 2;
-  const int64_t ldf = ((kdim + 15) / 16) * 16;
-  return align256s(sizeof(double) * (size_t)d->n_sites * (size_t)ldf) +
-         2 * align256s(es * (size_t)d->n_sites * (size_t)ld) + 256;
+  return 2 * align256s(es * (size_t)d->n_sites * (size_t)ld) + 256;
 }
-
-int ewald_features_launch(const double* cart, int64_t n, const int32_t* kv, Mat3 recip,
-                          const double* kc, const double* k2, const double* ck, int64_t K,
-                          double eps, int64_t ld, double* F, cudaStream_t s);
 
 int ewald_build_split(const PycdEwaldDesc* d, int mode, double* out,
                       const double* kc, const double* k2, const double* ck,
-                      void* ws, size_t ws_bytes, cudaStream_t s) {
+                      const double* real_rows, void* ws, size_t ws_bytes, cudaStream_t s) {
   const bool tf32 = mode == PYCD_EWALD_TF32X3;
   const int64_t n = d->n_sites, K = d->n_kvec, kdim = 2 * K;
-  const int64_t ldf = ((kdim + 15) / 16) * 16;
   const int64_t ld = split_ld(kdim, tf32);
   const size_t es = tf32 ? 4 : 2;
   if (ws_bytes < ewald_split_workspace_bytes(d, mode)) {
@@ -507,8 +653,6 @@ int ewald_build_split(const PycdEwaldDesc* d, int mode, double* out,
     return PYCD_ERR_WORKSPACE;
   }
   char* p = (char*)ws;
-  double* F = (double*)p;
-  p += align256s(sizeof(double) * (size_t)n * (size_t)ldf);
   void* hi = p;
   p += align256s(es * (size_t)n * (size_t)ld);
   void* lo = p;
@@ -519,21 +663,33 @@ int ewald_build_split(const PycdEwaldDesc* d, int mode, double* out,
                "split operands must be 16-byte aligned");
   Mat3 recip;
   for (int c = 0; c < 9; ++c) recip.m[c] = d->recip[c];
-  int rc = ewald_features_launch(d->d_cart, n, d->d_kvec, recip, kc, k2, ck, K, d->dielectric,
-                                 ldf, F, s);
-  if (rc) return rc;
   weight_sum_kernel<<<1, 256, 0, s>>>(k2, ck, K, d->dielectric, diag_sum);
   PYCD_CUDA(cudaGetLastError());
-  dim3 sg((unsigned)((ld + 255) / 256), (unsigned)n);
-  if (tf32)
-    split_features_kernel<true><<<sg, 256, 0, s>>>(F, n, ldf, kdim, ld, hi, lo);
-  else
-    split_features_kernel<false><<<sg, 256, 0, s>>>(F, n, ldf, kdim, ld, hi, lo);
+  const unsigned fblocks = (unsigned)((n + kSfSites - 1) / kSfSites);
+  if (tf32) {
+    PYCD_CUDA(cudaFuncSetAttribute(split_features_direct_kernel<true>,
+                                   cudaFuncAttributeMaxDynamicSharedMemorySize, kSfSmem));
+    split_features_direct_kernel<true><<<fblocks, kSfThreads, kSfSmem, s>>>(
+        d->d_cart, n, d->d_kvec, recip, kc, k2, ck, K, d->dielectric, ld, hi, lo);
+  } else {
+    PYCD_CUDA(cudaFuncSetAttribute(split_features_direct_kernel<false>,
+                                   cudaFuncAttributeMaxDynamicSharedMemorySize, kSfSmem));
+    split_features_direct_kernel<false><<<fblocks, kSfThreads, kSfSmem, s>>>(
+        d->d_cart, n, d->d_kvec, recip, kc, k2, ck, K, d->dielectric, ld, hi, lo);
+  }
   PYCD_CUDA(cudaGetLastError());
   PYCD_CUDA(cudaMemsetAsync(flag, 0, sizeof(int), s));
+  RealTable rt{};
+  if (real_rows) {
+    rt.rows = real_rows;
+    rt.nb = d->basis_sites;
+    rt.s0 = d->supercell[0];
+    rt.s1 = d->supercell[1];
+    rt.s2 = d->supercell[2];
+  }
 
   EncodeTiledFn enc;
-  rc = get_encode(&enc);
+  int rc = get_encode(&enc);
   if (rc) return rc;
   CUtensorMap mh, ml;
   const cuuint64_t gdim[2] = {(cuuint64_t)ld, (cuuint64_t)n};
@@ -563,12 +719,12 @@ int ewald_build_split(const PycdEwaldDesc* d, int mode, double* out,
     PYCD_CUDA(cudaFuncSetAttribute(ewald_split_kernel<true>,
                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     ewald_split_kernel<true><<<ctas, 192, smem, s>>>(
-        mh, ml, n, k_blocks, chunk_blocks, nb, out, diag_sum, err);
+        mh, ml, n, k_blocks, chunk_blocks, nb, out, diag_sum, rt, err);
   } else {
     PYCD_CUDA(cudaFuncSetAttribute(ewald_split_kernel<false>,
                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     ewald_split_kernel<false><<<ctas, 192, smem, s>>>(
-        mh, ml, n, k_blocks, chunk_blocks, nb, out, diag_sum, err);
+        mh, ml, n, k_blocks, chunk_blocks, nb, out, diag_sum, rt, err);
   }
   PYCD_CUDA(cudaGetLastError());
   int h_flag = 0;

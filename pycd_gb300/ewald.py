@@ -181,8 +181,38 @@ def make_desc(system, alpha, r_cut, k_cut, pmiv=None, kvecs=None):
     desc.r_cut = float(r_cut)
     desc.volume = float(system.system_volume)
     desc.dielectric = float(system.material.dielectric_constant)
+    layout = supercell_layout(system, pmiv)
+    if layout is not None:
+        desc.supercell[:] = layout[0]
+        desc.basis_sites = layout[1]
     keep = [cart, d_kv] + ([d_pmiv] if d_pmiv is not None else [])
     return desc, keep, k_max
+
+
+def supercell_layout(system, pmiv=None, tol=1e-6):
+    """((s0, s1, s2), n_basis) when site i is basis site i % n_basis of cell
+    i // n_basis (cells in C order, the last index fastest), every site
+    sits at its unit-cell position plus its cell's translation (to `tol`
+    bohr), the Ewald cell is that supercell and any given pmiv is
+    lattice-consistent; otherwise None.  The array is then translation
+    invariant and its real-space rows repeat with the cells."""
+    if not ewald_cell_matches_supercell(system):
+        return None
+    if pmiv is not None and not pmiv_is_lattice_consistent(system, pmiv):
+        return None
+    m = system.material
+    uc = np.asarray(m.cartesian_unit_cell_coords, dtype=np.float64)
+    ss = np.asarray(system.system_size, dtype=int)
+    cart = np.asarray(system.neighbors.bulk_sites.cell_coordinates, dtype=np.float64)
+    nb = len(uc)
+    if nb == 0 or len(cart) != nb * int(np.prod(ss)):
+        return None
+    cells = np.stack(np.meshgrid(np.arange(ss[0]), np.arange(ss[1]), np.arange(ss[2]),
+                                 indexing="ij"), -1).reshape(-1, 3)
+    want = (cells @ np.asarray(m.lattice_matrix, dtype=np.float64))[:, None, :] + uc[None]
+    if np.abs(want.reshape(-1, 3) - cart).max() > tol:
+        return None
+    return [int(v) for v in ss], int(nb)
 
 
 def hop_energy_error(A_ref, A, nbr, n_carriers, n_dopants, samples=4096, seed=0,

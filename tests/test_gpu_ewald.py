@@ -166,3 +166,20 @@ def test_split_precision_large_against_oracle_rows(cuda_ready, cells, k_cut, n_k
         del A
     del ref
     torch.cuda.empty_cache()
+
+
+@pytest.mark.parametrize("precision", ["bf16x3", "tf32x3"])
+def test_split_real_space_table_equals_pair_pass(cuda_ready, monkeypatch, precision):
+    """On a described supercell the split modes take the real-space and self
+    terms of every row from the first basis_sites rows (translation
+    invariance) and write each entry once; without the description they run
+    the pass over all N^2 pairs and add the Fourier part to it.  Both give
+    the same array to rounding (1e-12 eV)."""
+    from pycd_gb300 import ewald as ew
+    sysm = wl.corundum((5, 5, 2), neighbor_list=False)
+    assert ew.supercell_layout(sysm) == ([5, 5, 2], 12)
+    A_table = sysm.get_precomputed_array_device(precision).cpu().numpy()
+    monkeypatch.setattr(ew, "supercell_layout", lambda system, pmiv=None, tol=1e-6: None)
+    A_pairs = sysm.get_precomputed_array_device(precision).cpu().numpy()
+    assert np.isfinite(A_table).all()
+    assert np.abs(A_table - A_pairs).max() < 1e-12 * K.EV2HARTREE

@@ -251,3 +251,16 @@ def test_mt19937_blocks_equal_cpython_random():
     for _ in range(1234):
         r2.random()
     assert st.state() == r2.getstate()
+
+
+def test_supercell_layout_of_synthetic_lattices():
+    """The synthetic corundum and monoclinic supercells are described to the
+    library as basis sites repeated over C-ordered cells; the shipped
+    Hematite example (pmiv from an older min-image code) is not."""
+    from pycd_gb300 import workloads as wl
+    assert ew.supercell_layout(wl.corundum((3, 3, 3), neighbor_list=False)) == ([3, 3, 3], 12)
+    assert ew.supercell_layout(wl.monoclinic((16, 16, 8), 0.9164)) == ([16, 16, 8], 4)
+    cfg, arr = gio.load("hematite")
+    mat, nb = gio.material(cfg)
+    sysm = System(mat, nb, gio.hop_list(cfg, arr), arr["pmiv"], 0.2667, 4.618, 6.998)
+    assert ew.supercell_layout(sysm, arr["pmiv"]) is None
