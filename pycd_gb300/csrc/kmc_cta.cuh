@@ -185,6 +185,7 @@ __device__ void advance_trajectory_cta(const KmcArgs& a, int64_t t, CtaShared& s
   }
   double sim_time = st.d_time[t];
   int64_t step = st.d_step[t];
+  const int64_t step_at_entry = step;
   int64_t start_path = st.d_path_index[t];
   double energy = st.d_energy ? st.d_energy[t] : 0.0;
   int64_t ucur = st.d_u_cursor ? st.d_u_cursor[t] : 0;
@@ -460,7 +461,10 @@ __device__ void advance_trajectory_cta(const KmcArgs& a, int64_t t, CtaShared& s
   }
   if (tc.npend > 0) tc.flush(l, full, sim_time, tlog, a.out.step_capacity);
 
-  if (csum) {
+  // a call that took no step keeps the stored sums: an exact refresh made
+  // at entry is made again at the next entry, and the stored values stay
+  // the ones an uninterrupted run holds
+  if (csum && step != step_at_entry) {
 #pragma unroll
     for (int j = 0; j < MAXP; ++j) {
       const int p = g * MAXP + j;

@@ -658,6 +658,7 @@ __device__ void advance_trajectory(const KmcArgs& a, int64_t t, int g,
   }
   double sim_time = __ldcg(st.d_time + t);
   int64_t step = (int64_t)__ldcg((const long long*)st.d_step + t);
+  const int64_t step_at_entry = step;
   int64_t start_path = (int64_t)__ldcg((const long long*)st.d_path_index + t);
   int64_t ucur = st.d_u_cursor ? (int64_t)__ldcg((const long long*)st.d_u_cursor + t) : 0;
   const int64_t step_limit = st.d_step_limit ? st.d_step_limit[t] : INT64_MAX;
@@ -903,7 +904,10 @@ __device__ void advance_trajectory(const KmcArgs& a, int64_t t, int g,
   if (tc.npend > 0) tc.flush(g, gmask, sim_time, tlog, a.out.step_capacity);
 
   // ---- write the state back ---------------------------------------------
-  if (csum) {
+  // a call that took no step keeps the stored sums: an exact refresh made
+  // at entry is made again at the next entry, and the stored values stay
+  // the ones an uninterrupted run holds
+  if (csum && step != step_at_entry) {
 #pragma unroll
     for (int j = 0; j < MAXP; ++j) {
       const int p = g * MAXP + j;
