@@ -16,7 +16,10 @@
 // its block row / column (a row-major walk over the whole triangle touches
 // one new B panel per CTA).
 //
-// Kernel layout (one CTA per 128 x 128 upper-triangle output tile):
+// Kernel layout (one persistent CTA per SM; each walks its share of the
+// 128 x 128 upper-triangle output tiles in raster order, with TMEM held and
+// the barrier phases carried from tile to tile, so one tile's final
+// epilogue overlaps the next tile's first loads and MMAs):
 //   warp 4      TMA producer: Ah, Al (tile rows) and Bh, Bl (tile columns),
 //               64-byte K slices, SWIZZLE_64B, 7-stage ring
 //   warp 5      MMA issuer: one thread issues tcgen05.mma (M=128, N=128)
@@ -239,12 +242,10 @@ template <bool TF32>
 __global__ void __launch_bounds__(192, 1)
     ewald_split_kernel(const __grid_constant__ CUtensorMap map_h,
                        const __grid_constant__ CUtensorMap map_l, int64_t n,
-                       int k_blocks, int chunk_blocks, int nb, double* __restrict__ out,
-                       const double* __restrict__ diag_sum, RealTable rt, SplitErr err) {
+                       int k_blocks, int chunk_blocks, int nb, int n_slots,
+                       double* __restrict__ out, const double* __restrict__ diag_sum,
+                       RealTable rt, SplitErr err) {
   const double diag_value = *diag_sum;
-  int bi = 0, bj = 0;
-  // lower tiles are written as mirrors; CTAs without a tile leave at once
-  if (!raster_tile((int)blockIdx.x, nb, bi, bj)) return;
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   uint64_t* full = (uint64_t*)(smem + kStages * kStageBytes);
@@ -287,19 +288,25 @@ __global__ void __launch_bounds__(192, 1)
     if (lane == 0) {
       int last_kb[kStages];
       for (int s = 0; s < kStages; ++s) last_kb[s] = -1;
-      for (int kb = 0; kb < k_blocks; ++kb) {
-        const int s = kb % kStages;
-        const uint32_t ph = (uint32_t)(kb / kStages) & 1u;
-        if (!mbar_wait(&empty[s], ph ^ 1u, abort_flag)) { *abort_flag = 1; break; }
-        if (*abort_flag) break;
-        uint8_t* st = smem + s * kStageBytes;
-        mbar_arrive_expect_tx(&full[s], kStageBytes);
-        const int x = kb * (TF32 ? kRowBytes / 4 : kRowBytes / 2);
-        tma_load_2d(st, &map_h, &full[s], x, bi * kTile);
-        tma_load_2d(st + kTileBytes, &map_l, &full[s], x, bi * kTile);
-        tma_load_2d(st + 2 * kTileBytes, &map_h, &full[s], x, bj * kTile);
-        tma_load_2d(st + 3 * kTileBytes, &map_l, &full[s], x, bj * kTile);
-        last_kb[s] = kb;
+      int gkb = 0;  // k-blocks loaded by this CTA over all its tiles
+      bool ok = true;
+      for (int slot = blockIdx.x; slot < n_slots && ok; slot += gridDim.x) {
+        int bi = 0, bj = 0;
+        if (!raster_tile(slot, nb, bi, bj)) continue;
+        for (int kb = 0; kb < k_blocks; ++kb, ++gkb) {
+          const int s = gkb % kStages;
+          const uint32_t ph = (uint32_t)(gkb / kStages) & 1u;
+          if (!mbar_wait(&empty[s], ph ^ 1u, abort_flag)) { *abort_flag = 1; ok = false; break; }
+          if (*abort_flag) { ok = false; break; }
+          uint8_t* st = smem + s * kStageBytes;
+          mbar_arrive_expect_tx(&full[s], kStageBytes);
+          const int x = kb * (TF32 ? kRowBytes / 4 : kRowBytes / 2);
+          tma_load_2d(st, &map_h, &full[s], x, bi * kTile);
+          tma_load_2d(st + kTileBytes, &map_l, &full[s], x, bi * kTile);
+          tma_load_2d(st + 2 * kTileBytes, &map_h, &full[s], x, bj * kTile);
+          tma_load_2d(st + 3 * kTileBytes, &map_l, &full[s], x, bj * kTile);
+          last_kb[s] = gkb;
+        }
       }
       // every copy this thread issued has landed before the CTA moves on
       // (already true on the normal path, where the MMA issuer consumed them)
@@ -312,35 +319,40 @@ __global__ void __launch_bounds__(192, 1)
     // ---------------- MMA issuer ----------------
     if (lane == 0) {
       const int ksteps = TF32 ? kRowBytes / 32 : kRowBytes / 32;  // 32-byte K steps
-      int kb = 0;
+      int gkb = 0, gc = 0;  // k-blocks and chunks of this CTA over all its tiles
       bool ok = true;
-      for (int c = 0; c < n_chunks && ok; ++c) {
-        const int b = c & 1;
-        if (!mbar_wait(&acc_empty[b], ((uint32_t)(c >> 1) & 1u) ^ 1u, abort_flag)) {
-          *abort_flag = 1; ok = false; break;
-        }
-        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        const uint32_t d = tmem + (uint32_t)(b * kTile);
-        const int kb_end = min(k_blocks, (c + 1) * chunk_blocks);
-        for (int first = 1; kb < kb_end; ++kb, first = 0) {
-          const int s = kb % kStages;
-          const uint32_t ph = (uint32_t)(kb / kStages) & 1u;
-          if (!mbar_wait(&full[s], ph, abort_flag)) { *abort_flag = 1; ok = false; break; }
-          asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-          const uint32_t base = smem_u32(smem + s * kStageBytes);
-          const uint64_t ah = sdesc(base), al = sdesc(base + kTileBytes);
-          const uint64_t bh = sdesc(base + 2 * kTileBytes), bl = sdesc(base + 3 * kTileBytes);
-          for (int k = 0; k < ksteps; ++k) {
-            const uint64_t o = (uint64_t)(k * 2);  // +32 bytes in the >>4 field
-            const uint32_t acc0 = (first && k == 0) ? 0u : 1u;
-            umma<TF32>(d, ah + o, bh + o, acc0);
-            umma<TF32>(d, ah + o, bl + o, 1u);
-            umma<TF32>(d, al + o, bh + o, 1u);
+      for (int slot = blockIdx.x; slot < n_slots && ok; slot += gridDim.x) {
+        int bi = 0, bj = 0;
+        if (!raster_tile(slot, nb, bi, bj)) continue;
+        int kb = 0;
+        for (int c = 0; c < n_chunks && ok; ++c, ++gc) {
+          const int b = gc & 1;
+          if (!mbar_wait(&acc_empty[b], ((uint32_t)(gc >> 1) & 1u) ^ 1u, abort_flag)) {
+            *abort_flag = 1; ok = false; break;
           }
-          umma_commit(&empty[s]);  // stage free once these MMAs complete
+          asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+          const uint32_t d = tmem + (uint32_t)(b * kTile);
+          const int kb_end = min(k_blocks, (c + 1) * chunk_blocks);
+          for (int first = 1; kb < kb_end; ++kb, ++gkb, first = 0) {
+            const int s = gkb % kStages;
+            const uint32_t ph = (uint32_t)(gkb / kStages) & 1u;
+            if (!mbar_wait(&full[s], ph, abort_flag)) { *abort_flag = 1; ok = false; break; }
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const uint32_t base = smem_u32(smem + s * kStageBytes);
+            const uint64_t ah = sdesc(base), al = sdesc(base + kTileBytes);
+            const uint64_t bh = sdesc(base + 2 * kTileBytes), bl = sdesc(base + 3 * kTileBytes);
+            for (int k = 0; k < ksteps; ++k) {
+              const uint64_t o = (uint64_t)(k * 2);  // +32 bytes in the >>4 field
+              const uint32_t acc0 = (first && k == 0) ? 0u : 1u;
+              umma<TF32>(d, ah + o, bh + o, acc0);
+              umma<TF32>(d, ah + o, bl + o, 1u);
+              umma<TF32>(d, al + o, bh + o, 1u);
+            }
+            umma_commit(&empty[s]);  // stage free once these MMAs complete
+          }
+          if (!ok) break;
+          umma_commit(&acc_full[b]);  // chunk finished
         }
-        if (!ok) break;
-        umma_commit(&acc_full[b]);  // chunk finished
       }
       // drain: every issued MMA has completed once this commit arrives
       umma_commit(drain);
@@ -353,14 +365,18 @@ __global__ void __launch_bounds__(192, 1)
     // is added with Knuth's error-free TwoSum, the rounding error going to
     // lo, so the pair carries ~48 significant bits; the FP64 result
     // (double)hi + (double)lo is written once per tile.
-    const int64_t row = (int64_t)bi * kTile + warp * 32 + lane;
     const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
     const uint32_t t_hi = lane_base + 2u * kTile, t_lo = lane_base + 3u * kTile;
     bool ok = true;
-    for (int c = 0; c < n_chunks; ++c) {
-      const int b = c & 1;
+    int gc = 0;  // chunks of this CTA over all its tiles
+    for (int slot = blockIdx.x; slot < n_slots && ok; slot += gridDim.x) {
+    int bi = 0, bj = 0;
+    if (!raster_tile(slot, nb, bi, bj)) continue;
+    const int64_t row = (int64_t)bi * kTile + warp * 32 + lane;
+    for (int c = 0; c < n_chunks; ++c, ++gc) {
+      const int b = gc & 1;
       bool got = false;
-      if (lane == 0) got = mbar_wait(&acc_full[b], (uint32_t)(c >> 1) & 1u, abort_flag);
+      if (lane == 0) got = mbar_wait(&acc_full[b], (uint32_t)(gc >> 1) & 1u, abort_flag);
       got = __shfl_sync(0xffffffffu, got, 0);
       if (!got) {
         if (lane == 0) *abort_flag = 1;
@@ -454,6 +470,7 @@ __global__ void __launch_bounds__(192, 1)
         }
       }
     }
+  }  // tiles of this CTA
   }
 
   // ---------------- teardown ----------------
@@ -718,18 +735,24 @@ int ewald_build_split(const PycdEwaldDesc* d, int mode, double* out,
   const size_t smem = (size_t)kStages * kStageBytes + 1024 + 256;
   const int nb = (int)((n + kTile - 1) / kTile);
   const int nbb = (nb + kRaster - 1) / kRaster;
-  const unsigned ctas = (unsigned)(nbb * (nbb + 1) / 2 * kRaster * kRaster);
+  // tile slots of the blocked raster order; one persistent CTA per SM walks
+  // slots blockIdx.x, blockIdx.x + gridDim.x, ... (some slots hold no tile)
+  const int n_slots = nbb * (nbb + 1) / 2 * kRaster * kRaster;
+  int dev = 0, sms = 0;
+  PYCD_CUDA(cudaGetDevice(&dev));
+  PYCD_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  const unsigned ctas = (unsigned)(n_slots < sms ? n_slots : sms);
   SplitErr err{flag};
   if (tf32) {
     PYCD_CUDA(cudaFuncSetAttribute(ewald_split_kernel<true>,
                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     ewald_split_kernel<true><<<ctas, 192, smem, s>>>(
-        mh, ml, n, k_blocks, chunk_blocks, nb, out, diag_sum, rt, err);
+        mh, ml, n, k_blocks, chunk_blocks, nb, n_slots, out, diag_sum, rt, err);
   } else {
     PYCD_CUDA(cudaFuncSetAttribute(ewald_split_kernel<false>,
                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     ewald_split_kernel<false><<<ctas, 192, smem, s>>>(
-        mh, ml, n, k_blocks, chunk_blocks, nb, out, diag_sum, rt, err);
+        mh, ml, n, k_blocks, chunk_blocks, nb, n_slots, out, diag_sum, rt, err);
   }
   PYCD_CUDA(cudaGetLastError());
   int h_flag = 0;
