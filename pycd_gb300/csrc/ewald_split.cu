@@ -21,7 +21,7 @@
 // the barrier phases carried from tile to tile, so one tile's final
 // epilogue overlaps the next tile's first loads and MMAs):
 //   warp 4      TMA producer: Ah, Al (tile rows) and Bh, Bl (tile columns),
-//               64-byte K slices, SWIZZLE_64B, 7-stage ring
+//               128-byte K slices, SWIZZLE_128B, 3-stage ring
 //   warp 5      MMA issuer: one thread issues tcgen05.mma (M=128, N=128)
 //               into one of two TMEM accumulators (double buffered)
 //   warps 0-3   epilogue: tcgen05.ld of a finished chunk (warp w reads TMEM
@@ -40,13 +40,9 @@
 namespace pycd {
 
 constexpr int kTile = 128;               // output tile rows / columns
-// One K slice per row: 64 bytes (32 BF16 / 16 TF32 values, the 64-byte
-// swizzle span), so that a stage is 32 KB and seven stages fit: ~192 KB of
-// operands in flight while the MMAs consume one stage, enough to cover the
-// L2 latency at the tensor pipe's rate (three 64 KB stages covered ~0.8 us).
-constexpr int kRowBytes = 64;
-constexpr int kTileBytes = kTile * kRowBytes;  // 8 KB
-constexpr int kStages = 7;
+constexpr int kRowBytes = 128;           // one K slice per row (swizzle span)
+constexpr int kTileBytes = kTile * kRowBytes;  // 16 KB
+constexpr int kStages = 3;
 constexpr int kStageBytes = 4 * kTileBytes;    // Ah, Al, Bh, Bl
 // TMEM: two 128-column FP32 accumulators, then the hi and lo halves of the
 // cross-chunk sum (128 columns each)
@@ -166,16 +162,15 @@ __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map,
       : "memory");
 }
 
-// Shared-memory matrix descriptor: K-major, 64-byte swizzle, 8-row atoms of
-// 512 bytes (stride-dimension byte offset 8 rows x 64 B), descriptor
-// version 1.
+// Shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row atoms of
+// 1024 bytes (stride-dimension byte offset 1024), descriptor version 1.
 __device__ __forceinline__ uint64_t sdesc(uint32_t saddr) {
   uint64_t d = 0;
   d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);
   d |= (uint64_t)1 << 16;             // leading byte offset (unused here) = 16 B
-  d |= (uint64_t)((8 * kRowBytes) >> 4) << 32;  // stride byte offset = 512 B
+  d |= (uint64_t)(1024 >> 4) << 32;   // stride byte offset = 1024 B
   d |= (uint64_t)1 << 46;             // fixed 0b001
-  d |= (uint64_t)4 << 61;             // 64-byte swizzle
+  d |= (uint64_t)2 << 61;             // 128-byte swizzle
   return d;
 }
 
@@ -591,7 +586,7 @@ split_features_direct_kernel(const double* __restrict__ cart, int64_t n,
         asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(h1) : "f"((float)f1));
         asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(l0) : "f"((float)(f0 - (double)__uint_as_float(h0))));
         asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(l1) : "f"((float)(f1 - (double)__uint_as_float(h1))));
-        // c is even and ld a multiple of 16: 8-byte aligned pairs
+        // c is even and ld a multiple of 32: 8-byte aligned pairs
         *(float2*)((float*)hi + at) = make_float2(__uint_as_float(h0), __uint_as_float(h1));
         *(float2*)((float*)lo + at) = make_float2(__uint_as_float(l0), __uint_as_float(l1));
       } else {
@@ -612,7 +607,7 @@ split_features_direct_kernel(const double* __restrict__ cart, int64_t n,
         const __nv_bfloat16 h0 = __float2bfloat16_rn(f0), h1 = __float2bfloat16_rn(f1);
         const __nv_bfloat16 l0 = __float2bfloat16_rn(f0 - __bfloat162float(h0));
         const __nv_bfloat16 l1 = __float2bfloat16_rn(f1 - __bfloat162float(h1));
-        // c is even and ld a multiple of 32: 4-byte aligned pairs
+        // c is even and ld a multiple of 64: 4-byte aligned pairs
         *(__nv_bfloat162*)((__nv_bfloat16*)hi + at) = __halves2bfloat162(h0, h1);
         *(__nv_bfloat162*)((__nv_bfloat16*)lo + at) = __halves2bfloat162(l0, l1);
       }
@@ -721,10 +716,10 @@ int ewald_build_split(const PycdEwaldDesc* d, int mode, double* out,
   const CUtensorMapDataType dt =
       tf32 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16;
   CUresult r1 = enc(&mh, dt, 2, hi, gdim, gstride, box, estr,
-                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B,
+                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
                     CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   CUresult r2 = enc(&ml, dt, 2, lo, gdim, gstride, box, estr,
-                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B,
+                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
                     CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r1 != CUDA_SUCCESS || r2 != CUDA_SUCCESS) {
     set_error("cuTensorMapEncodeTiled failed (%d, %d)", (int)r1, (int)r2);
