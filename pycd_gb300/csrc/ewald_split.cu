@@ -5,28 +5,47 @@
 // (BF16 or TF32 parts) and
 //     A_fourier ~= Fh Fh^T + Fh Fl^T + Fl Fh^T
 // is accumulated in FP32 in tensor memory over chunks of the K dimension;
-// each finished chunk is added in FP64 to the output, which already holds
-// the real-space and self terms, so the cross-chunk sum is FP64.
+// the chunks are summed without loss (below) and the FP64 result is added
+// to the real-space and self terms.
 //
-// Tile order: the grid is 1-D over blocks of kRaster x kRaster tiles, blocks
-// taken along the upper triangle row by row and tiles row-major inside a
-// block.  The CTAs resident at one time (one per SM) then cover about two
-// blocks, i.e. ~16-24 distinct 128-row operand panels per K slice, and each
-// slice of a panel is read from DRAM once and reused from L2 by the CTAs of
-// its block row / column (a row-major walk over the whole triangle touches
-// one new B panel per CTA).
+// Work units.  The upper triangle is covered by 256 x 256 super-tiles; a
+// unit is one 128-row half of a super-tile: 128 rows x 256 columns, one
+// tcgen05.mma of M = 128, N = 256 per K step.  Per 128-byte K slice a unit
+// reads 2 x 16 KB of A rows and 2 x 32 KB of B rows for 12 MMAs, i.e. 64
+// operand bytes per MMA cycle (128 x 128 tiles need 85).  The L2-to-SM
+// operand stream is what bounds this contraction, so bytes per MMA cycle
+// set its speed.  Off-diagonal super-tiles write each entry and its mirror;
+// diagonal super-tiles are computed whole and each entry is written once,
+// by the half that owns its row.
 //
-// Kernel layout (one persistent CTA per SM; each walks its share of the
-// 128 x 128 upper-triangle output tiles in raster order, with TMEM held and
-// the barrier phases carried from tile to tile, so one tile's final
-// epilogue overlaps the next tile's first loads and MMAs):
-//   warp 4      TMA producer: Ah, Al (tile rows) and Bh, Bl (tile columns),
-//               128-byte K slices, SWIZZLE_128B, 3-stage ring
-//   warp 5      MMA issuer: one thread issues tcgen05.mma (M=128, N=128)
-//               into one of two TMEM accumulators (double buffered)
-//   warps 0-3   epilogue: tcgen05.ld of a finished chunk (warp w reads TMEM
-//               lanes 32w..32w+31 = tile rows), FP64 add into A[i][j] and,
-//               for off-diagonal tiles, into the mirror A[j][i]
+// Schedule.  One persistent CTA per SM takes units from a global counter in
+// a blocked order (kRaster x kRaster super-tiles at a time, the block rows
+// of the upper triangle in turn).  The units in flight at one time then
+// share few operand panels and advance along K together, so each K slice
+// of a panel is read from DRAM about once and reused from L2.  Tensor
+// memory stays allocated from unit to unit and the barrier phases carry
+// over, so one unit's last epilogue overlaps the next unit's loads and MMAs.
+//
+// Sum over chunks.  The tensor core's FP32 accumulation truncates, so one
+// accumulation covers at most kChunkCols K columns (a chunk).  The
+// epilogue adds each finished chunk x to a running FP32 sum s kept in its
+// registers with Knuth's TwoSum (s + x = s' + e exactly) and writes the
+// rounding error e back into the chunk's TMEM accumulator; the next chunk
+// issued into that accumulator adds its products on top of e, so no error
+// is dropped.  A unit's last chunk goes into the same accumulator as the
+// one before it, whose fold also adds in the other accumulator's pending
+// error; the result is (double)s + (double)x_last.
+//
+// Warp roles (320 threads):
+//   warp 8      scheduler and TMA producer: takes units from the counter,
+//               hands them to the other warps through a 4-entry ring, loads
+//               Ah, Al (unit rows) and Bh, Bl (super-tile columns) in
+//               128-byte K slices, SWIZZLE_128B, 2-stage ring of 96 KB
+//   warp 9      MMA issuer: one thread issues tcgen05.mma (M=128, N=256)
+//               into one of two 256-column TMEM accumulators
+//   warps 0-7   epilogue: warp w reads TMEM lanes 32(w%4).. (unit rows) and
+//               columns 128(w/4)..+127; TwoSum fold per chunk; FP64 writes
+//               into A[i][j] and, off the diagonal, the mirror A[j][i]
 // Every mbarrier wait is bounded; on time-out the CTA records an error,
 // stops issuing, waits (bounded) for its own copies and MMAs, frees its
 // tensor memory and returns.
@@ -39,37 +58,71 @@
 
 namespace pycd {
 
-constexpr int kTile = 128;               // output tile rows / columns
-constexpr int kRowBytes = 128;           // one K slice per row (swizzle span)
-constexpr int kTileBytes = kTile * kRowBytes;  // 16 KB
-constexpr int kStages = 3;
-constexpr int kStageBytes = 4 * kTileBytes;    // Ah, Al, Bh, Bl
-// TMEM: two 128-column FP32 accumulators, then the hi and lo halves of the
-// cross-chunk sum (128 columns each)
-constexpr int kTmemCols = 512;
+constexpr int kRows = 128;                  // unit rows (MMA M)
+constexpr int kCols = 256;                  // unit columns, super-tile side (MMA N)
+constexpr int kSlice = 128;                 // K bytes per operand row per stage
+constexpr int kABytes = kRows * kSlice;     // 16 KB
+constexpr int kBBytes = kCols * kSlice;     // 32 KB
+constexpr int kBoxRows = 128;               // rows per TMA box
+constexpr int kStageBytes = 2 * kABytes + 2 * kBBytes;  // Ah, Al, Bh, Bl: 96 KB
+constexpr int kStages = 2;
+constexpr int kTmemCols = 512;              // two 256-column FP32 accumulators
 // K columns accumulated in FP32 per chunk: the tensor core's FP32
 // accumulation truncates, so its error grows with the MMA steps per chunk
 constexpr int kChunkCols = 256;
-constexpr uint32_t kWaitLimit = 1u << 24;      // bounded try_wait iterations
-constexpr int kRaster = 8;                     // tiles per raster block side
+constexpr int kRing = 4;                    // units handed out ahead
+constexpr int kEpiWarps = 8;
+constexpr int kThreads = 32 * (kEpiWarps + 2);
+constexpr int kProducerWarp = kEpiWarps, kMmaWarp = kEpiWarps + 1;
+constexpr uint32_t kWaitLimit = 1u << 24;   // bounded try_wait iterations
+constexpr int kRaster = 8;                  // super-tiles per raster block side
 
-// (bi, bj) of CTA `cta` in the blocked upper-triangle order; false for the
-// CTAs of diagonal and edge blocks that fall below the diagonal or outside
-__device__ __forceinline__ bool raster_tile(int cta, int nb, int& bi, int& bj) {
-  const int nbb = (nb + kRaster - 1) / kRaster;   // blocks per side
-  int blk = cta / (kRaster * kRaster);
-  const int loc = cta - blk * (kRaster * kRaster);
-  int I = 0;
-  while (I < nbb && blk >= nbb - I) { blk -= nbb - I; ++I; }
-  if (I >= nbb) return false;
-  const int J = I + blk;
-  bi = I * kRaster + loc / kRaster;
-  bj = J * kRaster + loc % kRaster;
-  return bi < nb && bj < nb && bi <= bj;
+// (row ti, column tj) of super-tile t in the blocked order: block rows of
+// kRaster super-tile rows in turn; within one, the diagonal block's upper
+// triangle (row-major), then the blocks to its right (row-major inside each)
+__device__ __forceinline__ bool super_tile(int t, int nt, int& ti, int& tj) {
+  for (int r0 = 0; r0 < nt; r0 += kRaster) {
+    const int h = min(kRaster, nt - r0);
+    const int nd = h * (h + 1) / 2;
+    if (t < nd) {
+      int r = 0;
+      while (t >= h - r) { t -= h - r; ++r; }
+      ti = r0 + r;
+      tj = r0 + r + t;
+      return true;
+    }
+    t -= nd;
+    for (int c0 = r0 + h; c0 < nt; c0 += kRaster) {
+      const int w = min(kRaster, nt - c0);
+      if (t < h * w) {
+        ti = r0 + t / w;
+        tj = c0 + t % w;
+        return true;
+      }
+      t -= h * w;
+    }
+  }
+  return false;
+}
+
+// TMEM accumulator of chunk c of a unit whose first chunk uses `base`:
+// chunks alternate, and the last chunk reuses the second-to-last's
+__device__ __forceinline__ int chunk_acc(int base, int c, int n) {
+  if (n == 1) return base;
+  return base ^ ((c < n - 1 ? c : n - 2) & 1);
+}
+// first chunk of the unit in its accumulator (starts from zero)
+__device__ __forceinline__ bool chunk_fresh(int c, int n) {
+  return c == 0 || (c == 1 && n > 2);
+}
+// accumulator of the next unit's first chunk: the one the last chunk left
+__device__ __forceinline__ int next_base(int base, int n) {
+  return n == 1 ? base ^ 1 : base ^ ((n - 2) & 1) ^ 1;
 }
 
 struct SplitErr {
   int* flag;  // device int, set non-zero on a timed-out wait
+  int* next;  // device int, zero at launch: next unit to hand out
 };
 
 // Real-space + self terms of a translation-invariant supercell: rows holds
@@ -153,6 +206,14 @@ __device__ __forceinline__ bool mbar_wait_drain(uint64_t* bar, uint32_t parity) 
   return false;
 }
 
+// Warp-wide bounded wait: lane 0 polls, the warp takes its answer.
+__device__ __forceinline__ bool warp_wait(uint64_t* bar, uint32_t parity,
+                                         volatile int* abort_flag) {
+  bool got = false;
+  if ((threadIdx.x & 31) == 0) got = mbar_wait(bar, parity, abort_flag);
+  return __shfl_sync(0xffffffffu, got, 0);
+}
+
 __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map,
                                             uint64_t* bar, int x, int y) {
   asm volatile(
@@ -174,11 +235,11 @@ __device__ __forceinline__ uint64_t sdesc(uint32_t saddr) {
   return d;
 }
 
-// Instruction descriptor: D = F32, A/B K-major, M = 128, N = 128;
+// Instruction descriptor: D = F32, A/B K-major, M = kRows, N = kCols;
 // operand format 1 = BF16 (kind::f16) or 2 = TF32 (kind::tf32).
 __host__ __device__ constexpr uint32_t idesc(uint32_t ab_format) {
   return (1u << 4) | (ab_format << 7) | (ab_format << 10) |
-         ((uint32_t)(kTile >> 3) << 17) | ((uint32_t)(kTile >> 4) << 24);
+         ((uint32_t)(kCols >> 3) << 17) | ((uint32_t)(kRows >> 4) << 24);
 }
 
 template <bool TF32>
@@ -233,13 +294,58 @@ __device__ __forceinline__ void tmem_st_wait() {
   asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
 }
 
+// 8 consecutive TMEM columns of this thread's lane (no wait)
+__device__ __forceinline__ void tmem_ld8_nowait(uint32_t taddr, uint32_t (&r)[8]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]),
+        "=r"(r[6]), "=r"(r[7])
+      : "r"(taddr));
+}
+
+__device__ __forceinline__ void tmem_st8(uint32_t taddr, const uint32_t (&r)[8]) {
+  asm volatile(
+      "tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8};" ::"r"(
+          taddr),
+      "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7])
+      : "memory");
+}
+
+constexpr int kEpiCols = kCols / 2;  // columns per epilogue thread
+
+// s += x (Knuth TwoSum) over this thread's kEpiCols columns of the chunk in
+// t_acc; the rounding errors, plus with take_other the pending errors held
+// in t_oth, are written back into t_acc for the next chunk to build on.
+__device__ __forceinline__ void fold_chunk(uint32_t t_acc, uint32_t t_oth, bool take_other,
+                                           float (&s)[kEpiCols]) {
+#pragma unroll
+  for (int g = 0; g < kEpiCols / 8; ++g) {
+    uint32_t x[8], o[8];
+    tmem_ld8_nowait(t_acc + (uint32_t)(g * 8), x);
+    if (take_other) tmem_ld8_nowait(t_oth + (uint32_t)(g * 8), o);
+    tmem_ld_wait();
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const float xv = __uint_as_float(x[q]);
+      const float h = s[g * 8 + q];
+      const float sum = __fadd_rn(h, xv);
+      const float bb = __fsub_rn(sum, h);
+      float e = __fadd_rn(__fsub_rn(h, __fsub_rn(sum, bb)), __fsub_rn(xv, bb));
+      if (take_other) e = __fadd_rn(e, __uint_as_float(o[q]));
+      s[g * 8 + q] = sum;
+      x[q] = __float_as_uint(e);
+    }
+    tmem_st8(t_acc + (uint32_t)(g * 8), x);
+  }
+  tmem_st_wait();
+}
+
 template <bool TF32>
-__global__ void __launch_bounds__(192, 1)
+__global__ void __launch_bounds__(kThreads, 1)
     ewald_split_kernel(const __grid_constant__ CUtensorMap map_h,
                        const __grid_constant__ CUtensorMap map_l, int64_t n,
-                       int k_blocks, int chunk_blocks, int nb, int n_slots,
-                       double* __restrict__ out, const double* __restrict__ diag_sum,
-                       RealTable rt, SplitErr err) {
+                       int k_blocks, int chunk_blocks, int nt, double* __restrict__ out,
+                       const double* __restrict__ diag_sum, RealTable rt, SplitErr err) {
   const double diag_value = *diag_sum;
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
@@ -247,12 +353,16 @@ __global__ void __launch_bounds__(192, 1)
   uint64_t* empty = full + kStages;
   uint64_t* acc_full = empty + kStages;
   uint64_t* acc_empty = acc_full + 2;
-  uint64_t* drain = acc_empty + 2;
-  volatile uint32_t* tmem_slot = (volatile uint32_t*)(drain + 1);
+  uint64_t* ring_full = acc_empty + 2;
+  uint64_t* ring_empty = ring_full + kRing;
+  uint64_t* drain = ring_empty + kRing;
+  volatile int* ring_unit = (volatile int*)(drain + 1);
+  volatile uint32_t* tmem_slot = (volatile uint32_t*)(ring_unit + kRing);
   volatile int* abort_flag = (volatile int*)(tmem_slot + 1);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int n_chunks = (k_blocks + chunk_blocks - 1) / chunk_blocks;
+  const int n_units = nt * (nt + 1);  // two halves of nt (nt + 1) / 2 super-tiles
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < kStages; ++s) {
@@ -261,13 +371,17 @@ __global__ void __launch_bounds__(192, 1)
     }
     for (int b = 0; b < 2; ++b) {
       mbar_init(&acc_full[b], 1);
-      mbar_init(&acc_empty[b], 4);
+      mbar_init(&acc_empty[b], kEpiWarps);
+    }
+    for (int r = 0; r < kRing; ++r) {
+      mbar_init(&ring_full[r], 1);
+      mbar_init(&ring_empty[r], 1 + kEpiWarps);
     }
     mbar_init(drain, 1);
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  if (warp == 4) {
+  if (warp == kProducerWarp) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
                      smem_u32((const void*)tmem_slot)),
                  "r"(kTmemCols));
@@ -278,16 +392,34 @@ __global__ void __launch_bounds__(192, 1)
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = *tmem_slot;
 
-  if (warp == 4) {
-    // ---------------- TMA producer ----------------
+  if (warp == kProducerWarp) {
+    // ---------------- scheduler + TMA producer ----------------
     if (lane == 0) {
       int last_kb[kStages];
       for (int s = 0; s < kStages; ++s) last_kb[s] = -1;
-      int gkb = 0;  // k-blocks loaded by this CTA over all its tiles
-      bool ok = true;
-      for (int slot = blockIdx.x; slot < n_slots && ok; slot += gridDim.x) {
-        int bi = 0, bj = 0;
-        if (!raster_tile(slot, nb, bi, bj)) continue;
+      int gkb = 0;  // k-blocks loaded by this CTA over all its units
+      for (int i = 0;; ++i) {
+        // next unit whose rows lie inside the matrix; -1 once none is left
+        int u = -1, ti = 0, tj = 0;
+        for (;;) {
+          const int t = atomicAdd(err.next, 1);
+          if (t >= n_units) break;
+          if (super_tile(t >> 1, nt, ti, tj) &&
+              (int64_t)ti * kCols + (int64_t)(t & 1) * kRows < n) {
+            u = t;
+            break;
+          }
+        }
+        const int r = i % kRing;
+        if (!mbar_wait(&ring_empty[r], ((uint32_t)(i / kRing) & 1u) ^ 1u, abort_flag)) {
+          *abort_flag = 1;
+          break;
+        }
+        ring_unit[r] = u;
+        mbar_arrive(&ring_full[r]);
+        if (u < 0) break;
+        const int row_a = ti * kCols + (u & 1) * kRows, row_b = tj * kCols;
+        bool ok = true;
         for (int kb = 0; kb < k_blocks; ++kb, ++gkb) {
           const int s = gkb % kStages;
           const uint32_t ph = (uint32_t)(gkb / kStages) & 1u;
@@ -295,13 +427,19 @@ __global__ void __launch_bounds__(192, 1)
           if (*abort_flag) { ok = false; break; }
           uint8_t* st = smem + s * kStageBytes;
           mbar_arrive_expect_tx(&full[s], kStageBytes);
-          const int x = kb * (TF32 ? kRowBytes / 4 : kRowBytes / 2);
-          tma_load_2d(st, &map_h, &full[s], x, bi * kTile);
-          tma_load_2d(st + kTileBytes, &map_l, &full[s], x, bi * kTile);
-          tma_load_2d(st + 2 * kTileBytes, &map_h, &full[s], x, bj * kTile);
-          tma_load_2d(st + 3 * kTileBytes, &map_l, &full[s], x, bj * kTile);
+          const int x = kb * (TF32 ? kSlice / 4 : kSlice / 2);
+          // rows at or past n (edge units) are read as zeros
+          tma_load_2d(st, &map_h, &full[s], x, row_a);
+          tma_load_2d(st + kABytes, &map_l, &full[s], x, row_a);
+          uint8_t* sb = st + 2 * kABytes;
+          for (int h = 0; h < kCols / kBoxRows; ++h) {
+            tma_load_2d(sb + h * kBoxRows * kSlice, &map_h, &full[s], x, row_b + h * kBoxRows);
+            tma_load_2d(sb + kBBytes + h * kBoxRows * kSlice, &map_l, &full[s], x,
+                        row_b + h * kBoxRows);
+          }
           last_kb[s] = gkb;
         }
+        if (!ok) break;
       }
       // every copy this thread issued has landed before the CTA moves on
       // (already true on the normal path, where the MMA issuer consumed them)
@@ -310,35 +448,43 @@ __global__ void __launch_bounds__(192, 1)
             !mbar_wait_drain(&full[s], (uint32_t)(last_kb[s] / kStages) & 1u))
           *abort_flag = 1;
     }
-  } else if (warp == 5) {
+  } else if (warp == kMmaWarp) {
     // ---------------- MMA issuer ----------------
     if (lane == 0) {
-      const int ksteps = TF32 ? kRowBytes / 32 : kRowBytes / 32;  // 32-byte K steps
-      int gkb = 0, gc = 0;  // k-blocks and chunks of this CTA over all its tiles
+      const int ksteps = kSlice / 32;  // 32-byte K steps (16 BF16 / 8 TF32)
+      int gkb = 0, base = 0;
+      int uses[2] = {0, 0};  // chunks issued into each accumulator so far
       bool ok = true;
-      for (int slot = blockIdx.x; slot < n_slots && ok; slot += gridDim.x) {
-        int bi = 0, bj = 0;
-        if (!raster_tile(slot, nb, bi, bj)) continue;
+      for (int i = 0; ok; ++i) {
+        const int r = i % kRing;
+        if (!mbar_wait(&ring_full[r], (uint32_t)(i / kRing) & 1u, abort_flag)) {
+          *abort_flag = 1;
+          break;
+        }
+        const int u = ring_unit[r];
+        mbar_arrive(&ring_empty[r]);
+        if (u < 0) break;
         int kb = 0;
-        for (int c = 0; c < n_chunks && ok; ++c, ++gc) {
-          const int b = gc & 1;
-          if (!mbar_wait(&acc_empty[b], ((uint32_t)(gc >> 1) & 1u) ^ 1u, abort_flag)) {
+        for (int c = 0; c < n_chunks; ++c) {
+          const int b = chunk_acc(base, c, n_chunks);
+          if (!mbar_wait(&acc_empty[b], ((uint32_t)uses[b] & 1u) ^ 1u, abort_flag)) {
             *abort_flag = 1; ok = false; break;
           }
           asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-          const uint32_t d = tmem + (uint32_t)(b * kTile);
+          const uint32_t d = tmem + (uint32_t)(b * kCols);
+          const bool fresh = chunk_fresh(c, n_chunks);
           const int kb_end = min(k_blocks, (c + 1) * chunk_blocks);
           for (int first = 1; kb < kb_end; ++kb, ++gkb, first = 0) {
             const int s = gkb % kStages;
             const uint32_t ph = (uint32_t)(gkb / kStages) & 1u;
             if (!mbar_wait(&full[s], ph, abort_flag)) { *abort_flag = 1; ok = false; break; }
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            const uint32_t base = smem_u32(smem + s * kStageBytes);
-            const uint64_t ah = sdesc(base), al = sdesc(base + kTileBytes);
-            const uint64_t bh = sdesc(base + 2 * kTileBytes), bl = sdesc(base + 3 * kTileBytes);
+            const uint32_t sa = smem_u32(smem + s * kStageBytes);
+            const uint64_t ah = sdesc(sa), al = sdesc(sa + kABytes);
+            const uint64_t bh = sdesc(sa + 2 * kABytes), bl = sdesc(sa + 2 * kABytes + kBBytes);
             for (int k = 0; k < ksteps; ++k) {
               const uint64_t o = (uint64_t)(k * 2);  // +32 bytes in the >>4 field
-              const uint32_t acc0 = (first && k == 0) ? 0u : 1u;
+              const uint32_t acc0 = (fresh && first && k == 0) ? 0u : 1u;
               umma<TF32>(d, ah + o, bh + o, acc0);
               umma<TF32>(d, ah + o, bl + o, 1u);
               umma<TF32>(d, al + o, bh + o, 1u);
@@ -347,112 +493,112 @@ __global__ void __launch_bounds__(192, 1)
           }
           if (!ok) break;
           umma_commit(&acc_full[b]);  // chunk finished
+          ++uses[b];
         }
+        base = next_base(base, n_chunks);
       }
       // drain: every issued MMA has completed once this commit arrives
       umma_commit(drain);
       if (!mbar_wait_drain(drain, 0u)) *abort_flag = 1;
     }
   } else {
-    // ---------------- epilogue (warps 0-3) ----------------
-    // Cross-chunk sum per output element as an unevaluated pair hi + lo of
-    // FP32 values kept in TMEM columns [256, 384) and [384, 512): each chunk
-    // is added with Knuth's error-free TwoSum, the rounding error going to
-    // lo, so the pair carries ~48 significant bits; the FP64 result
-    // (double)hi + (double)lo is written once per tile.
-    const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
-    const uint32_t t_hi = lane_base + 2u * kTile, t_lo = lane_base + 3u * kTile;
+    // ---------------- epilogue (warps 0-7) ----------------
+    const int quad = warp & 3, half = warp >> 2;
+    const uint32_t lane_base =
+        tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(half * kEpiCols);
+    float s[kEpiCols];  // running sums of this thread's columns
+    int base = 0;
+    int uses[2] = {0, 0};
     bool ok = true;
-    int gc = 0;  // chunks of this CTA over all its tiles
-    for (int slot = blockIdx.x; slot < n_slots && ok; slot += gridDim.x) {
-    int bi = 0, bj = 0;
-    if (!raster_tile(slot, nb, bi, bj)) continue;
-    const int64_t row = (int64_t)bi * kTile + warp * 32 + lane;
-    for (int c = 0; c < n_chunks; ++c, ++gc) {
-      const int b = gc & 1;
+    for (int i = 0; ok; ++i) {
+      const int r = i % kRing;
       bool got = false;
-      if (lane == 0) got = mbar_wait(&acc_full[b], (uint32_t)(gc >> 1) & 1u, abort_flag);
+      int u = -1;
+      if (lane == 0) {
+        got = mbar_wait(&ring_full[r], (uint32_t)(i / kRing) & 1u, abort_flag);
+        if (got) {
+          u = ring_unit[r];
+          mbar_arrive(&ring_empty[r]);
+        } else {
+          *abort_flag = 1;
+        }
+      }
       got = __shfl_sync(0xffffffffu, got, 0);
-      if (!got) {
-        if (lane == 0) *abort_flag = 1;
-        ok = false;
-        break;
-      }
-      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      const uint32_t t_acc = lane_base + (uint32_t)(b * kTile);
-#pragma unroll 1
-      for (int cb = 0; cb < kTile / 16; ++cb) {
-        const uint32_t off = (uint32_t)(cb * 16);
-        uint32_t a[16], h[16], l[16];
-        tmem_ld16_nowait(t_acc + off, a);
-        if (c > 0) {
-          tmem_ld16_nowait(t_hi + off, h);
-          tmem_ld16_nowait(t_lo + off, l);
-        }
-        tmem_ld_wait();
+      u = __shfl_sync(0xffffffffu, u, 0);
+      if (!got || u < 0) break;
+      int ti = 0, tj = 0;
+      super_tile(u >> 1, nt, ti, tj);
+      const int64_t row = (int64_t)ti * kCols + (u & 1) * kRows + quad * 32 + lane;
+      const int64_t col0 = (int64_t)tj * kCols + half * kEpiCols;
 #pragma unroll
-        for (int q = 0; q < 16; ++q) {
-          const float x = __uint_as_float(a[q]);
-          if (c == 0) {
-            h[q] = a[q];
-            l[q] = 0u;
-          } else {
-            const float hv = __uint_as_float(h[q]);
-            const float s = __fadd_rn(hv, x);
-            const float bb = __fsub_rn(s, hv);
-            const float e = __fadd_rn(__fsub_rn(hv, __fsub_rn(s, bb)), __fsub_rn(x, bb));
-            h[q] = __float_as_uint(s);
-            l[q] = __float_as_uint(__fadd_rn(__uint_as_float(l[q]), e));
+      for (int q = 0; q < kEpiCols; ++q) s[q] = 0.f;
+      for (int c = 0; c < n_chunks; ++c) {
+        const int b = chunk_acc(base, c, n_chunks);
+        if (!warp_wait(&acc_full[b], (uint32_t)uses[b] & 1u, abort_flag)) {
+          if (lane == 0) *abort_flag = 1;
+          ok = false;
+          break;
+        }
+        ++uses[b];
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const uint32_t t_acc = lane_base + (uint32_t)(b * kCols);
+        if (c < n_chunks - 1) {
+          // the second-to-last chunk also takes the other accumulator's
+          // pending error (left there by chunk n - 3, which kept it)
+          const bool take_other = c == n_chunks - 2 && n_chunks >= 3;
+          fold_chunk(t_acc, lane_base + (uint32_t)((b ^ 1) * kCols), take_other, s);
+          asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+          __syncwarp();
+          if (lane == 0) {
+            if (c != n_chunks - 3) mbar_arrive(&acc_empty[b]);
+            if (take_other) mbar_arrive(&acc_empty[b ^ 1]);
           }
+          continue;
         }
-        tmem_st16(t_hi + off, h);
-        tmem_st16(t_lo + off, l);
-      }
-      tmem_st_wait();
-      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-      __syncwarp();
-      if (lane == 0) mbar_arrive(&acc_empty[b]);
-    }
-    if (ok) {
-      // diagonal: F_i . F_i = sum_k w_k (cos^2 + sin^2) = sum_k w_k exactly,
-      // taken from the FP64 weight sum instead of the FP32 accumulation.
-      // With a real-space table the entry (and its mirror) is written once
-      // as table value + Fourier value; otherwise it is added to the real
-      // and self terms already in the output.
-      int rb = 0, rx = 0, ry = 0, rz = 0;
-      if (rt.rows && row < n) site_cell(rt, row, rb, rx, ry, rz);
-      const double* trow = rt.rows ? rt.rows + (int64_t)rb * n : nullptr;
-#pragma unroll 1
-      for (int cb = 0; cb < kTile / 16; ++cb) {
-        const uint32_t off = (uint32_t)(cb * 16);
-        uint32_t h[16], l[16];
-        tmem_ld16_nowait(t_hi + off, h);
-        tmem_ld16_nowait(t_lo + off, l);
-        tmem_ld_wait();
-        const int64_t col0 = (int64_t)bj * kTile + cb * 16;
-        if (row < n) {
-          int cbs = 0, cx = 0, cy = 0, cz = 0;
-          if (trow) site_cell(rt, col0, cbs, cx, cy, cz);
+        // last chunk: write (double)s + (double)x.  The diagonal is
+        // F_i . F_i = sum_k w_k (cos^2 + sin^2) = sum_k w_k exactly, taken
+        // from the FP64 weight sum.  With a real-space table the entry (and
+        // its mirror) is written once as table value + Fourier value;
+        // otherwise it is added to the real and self terms already there.
+        const bool live = row < n;
+        const bool mirror = ti != tj;
+        const int nn = (int)n, irow = (int)row;
+        double* orow = out + (live ? row : 0) * n;  // A[row][.]
+        double* ocol = out + col0 * n + row;        // A[col][row], advanced by n
+        int rx = 0, ry = 0, rz = 0, cbs = 0, cx = 0, cy = 0, cz = 0;
+        const double* trow = nullptr;
+        if (rt.rows) {
+          int rb = 0;
+          if (live) site_cell(rt, row, rb, rx, ry, rz);
+          trow = rt.rows + (int64_t)rb * n;
+          site_cell(rt, col0, cbs, cx, cy, cz);
+        }
 #pragma unroll
-          for (int q = 0; q < 16; ++q) {
-            const int64_t col = col0 + q;
-            if (col < n) {
-              double v = (double)__uint_as_float(h[q]) + (double)__uint_as_float(l[q]);
-              if (col == row) v = diag_value;
+        for (int g = 0; g < kEpiCols / 8; ++g) {
+          uint32_t x[8];
+          tmem_ld8_nowait(t_acc + (uint32_t)(g * 8), x);
+          tmem_ld_wait();
+#pragma unroll
+          for (int q = 0; q < 8; ++q) {
+            const int col = (int)col0 + g * 8 + q;
+            if (live && col < nn) {
+              double v = (double)s[g * 8 + q] + (double)__uint_as_float(x[q]);
+              if (col == irow) v = diag_value;
               if (trow) {
                 int dx = cx - rx, dy = cy - ry, dz = cz - rz;
                 if (dx < 0) dx += rt.s0;
                 if (dy < 0) dy += rt.s1;
                 if (dz < 0) dz += rt.s2;
-                const int64_t o = (((int64_t)dx * rt.s1 + dy) * rt.s2 + dz) * rt.nb + cbs;
+                const int o = ((dx * rt.s1 + dy) * rt.s2 + dz) * rt.nb + cbs;
                 const double a = __dadd_rn(__ldg(trow + o), v);
-                out[row * n + col] = a;
-                if (bi != bj) out[col * n + row] = a;
+                orow[col] = a;
+                if (mirror) *ocol = a;
               } else {
-                out[row * n + col] += v;
-                if (bi != bj) out[col * n + row] += v;
+                orow[col] += v;
+                if (mirror) *ocol += v;
               }
             }
+            ocol += n;
             // next column's site in the layout
             if (trow && ++cbs == rt.nb) {
               cbs = 0;
@@ -463,9 +609,12 @@ __global__ void __launch_bounds__(192, 1)
             }
           }
         }
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&acc_empty[b]);
       }
+      base = next_base(base, n_chunks);
     }
-  }  // tiles of this CTA
   }
 
   // ---------------- teardown ----------------
@@ -474,7 +623,7 @@ __global__ void __launch_bounds__(192, 1)
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-  if (warp == 4) {
+  if (warp == kProducerWarp) {
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
                  "r"(kTmemCols));
   }
@@ -642,7 +791,7 @@ static int get_encode(EncodeTiledFn* fn) {
 }
 
 static int64_t split_ld(int64_t kdim, bool tf32) {
-  const int64_t per = tf32 ? kRowBytes / 4 : kRowBytes / 2;  // elements per K block
+  const int64_t per = tf32 ? kSlice / 4 : kSlice / 2;  // elements per K block
   return ((kdim + per - 1) / per) * per;
 }
 
@@ -674,7 +823,8 @@ int ewald_build_split(const PycdEwaldDesc* d, int mode, double* out,
   p += align256s(es * (size_t)n * (size_t)ld);
   void* lo = p;
   p += align256s(es * (size_t)n * (size_t)ld);
-  int* flag = (int*)p;
+  int* flag = (int*)p;       // time-out flag
+  int* next = flag + 1;      // unit counter of the persistent schedule
   double* diag_sum = (double*)(p + 8);
   PYCD_REQUIRE(((uintptr_t)hi & 15) == 0 && ((uintptr_t)lo & 15) == 0,
                "split operands must be 16-byte aligned");
@@ -695,7 +845,7 @@ int ewald_build_split(const PycdEwaldDesc* d, int mode, double* out,
         d->d_cart, n, d->d_kvec, recip, kc, k2, ck, K, d->dielectric, ld, hi, lo);
   }
   PYCD_CUDA(cudaGetLastError());
-  PYCD_CUDA(cudaMemsetAsync(flag, 0, sizeof(int), s));
+  PYCD_CUDA(cudaMemsetAsync(flag, 0, 2 * sizeof(int), s));
   RealTable rt{};
   if (real_rows) {
     rt.rows = real_rows;
@@ -711,7 +861,7 @@ int ewald_build_split(const PycdEwaldDesc* d, int mode, double* out,
   CUtensorMap mh, ml;
   const cuuint64_t gdim[2] = {(cuuint64_t)ld, (cuuint64_t)n};
   const cuuint64_t gstride[1] = {(cuuint64_t)(ld * es)};
-  const cuuint32_t box[2] = {(cuuint32_t)(kRowBytes / es), (cuuint32_t)kTile};
+  const cuuint32_t box[2] = {(cuuint32_t)(kSlice / es), (cuuint32_t)kBoxRows};
   const cuuint32_t estr[2] = {1, 1};
   const CUtensorMapDataType dt =
       tf32 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16;
@@ -725,29 +875,28 @@ int ewald_build_split(const PycdEwaldDesc* d, int mode, double* out,
     set_error("cuTensorMapEncodeTiled failed (%d, %d)", (int)r1, (int)r2);
     return PYCD_ERR_CUDA;
   }
-  const int k_blocks = (int)(ld / (kRowBytes / es));
-  const int chunk_blocks = (int)(kChunkCols / (kRowBytes / es));
+  const int k_blocks = (int)(ld / (kSlice / es));
+  const int chunk_blocks = (int)(kChunkCols / (kSlice / es));
   const size_t smem = (size_t)kStages * kStageBytes + 1024 + 256;
-  const int nb = (int)((n + kTile - 1) / kTile);
-  const int nbb = (nb + kRaster - 1) / kRaster;
-  // tile slots of the blocked raster order; one persistent CTA per SM walks
-  // slots blockIdx.x, blockIdx.x + gridDim.x, ... (some slots hold no tile)
-  const int n_slots = nbb * (nbb + 1) / 2 * kRaster * kRaster;
+  // super-tiles per side; each of the nt (nt + 1) / 2 upper-triangle
+  // super-tiles is two units, taken by one persistent CTA per SM
+  const int nt = (int)((n + kCols - 1) / kCols);
+  const int n_units = nt * (nt + 1);
   int dev = 0, sms = 0;
   PYCD_CUDA(cudaGetDevice(&dev));
   PYCD_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-  const unsigned ctas = (unsigned)(n_slots < sms ? n_slots : sms);
-  SplitErr err{flag};
+  const unsigned ctas = (unsigned)(n_units < sms ? n_units : sms);
+  SplitErr err{flag, next};
   if (tf32) {
     PYCD_CUDA(cudaFuncSetAttribute(ewald_split_kernel<true>,
                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    ewald_split_kernel<true><<<ctas, 192, smem, s>>>(
-        mh, ml, n, k_blocks, chunk_blocks, nb, n_slots, out, diag_sum, rt, err);
+    ewald_split_kernel<true><<<ctas, kThreads, smem, s>>>(
+        mh, ml, n, k_blocks, chunk_blocks, nt, out, diag_sum, rt, err);
   } else {
     PYCD_CUDA(cudaFuncSetAttribute(ewald_split_kernel<false>,
                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    ewald_split_kernel<false><<<ctas, 192, smem, s>>>(
-        mh, ml, n, k_blocks, chunk_blocks, nb, n_slots, out, diag_sum, rt, err);
+    ewald_split_kernel<false><<<ctas, kThreads, smem, s>>>(
+        mh, ml, n, k_blocks, chunk_blocks, nt, out, diag_sum, rt, err);
   }
   PYCD_CUDA(cudaGetLastError());
   int h_flag = 0;
