@@ -496,9 +496,11 @@ size_t ewald_workspace_bytes(const PycdEwaldDesc* d, int mode) {
   return ewald_ws_layout(d, mode, nullptr, nullptr);
 }
 
+// real_rows (or nullptr): the first basis_sites rows of the real-space and
+// self terms; the split build rewrites them in place as FP32 pairs
 int ewald_build_split(const PycdEwaldDesc* d, int mode, double* out,
                       const double* kc, const double* k2, const double* ck,
-                      const double* real_rows, void* ws, size_t ws_bytes, cudaStream_t s);
+                      double* real_rows, void* ws, size_t ws_bytes, cudaStream_t s);
 size_t ewald_split_workspace_bytes(const PycdEwaldDesc* d, int mode);
 
 int ewald_build(const PycdEwaldDesc* d, int mode, double* out, void* ws,

@@ -34,7 +34,11 @@
 // issued into that accumulator adds its products on top of e, so no error
 // is dropped.  A unit's last chunk goes into the same accumulator as the
 // one before it, whose fold also adds in the other accumulator's pending
-// error; the result is (double)s + (double)x_last.
+// error and then stores s in that other accumulator.  The last chunk's
+// epilogue reads s and x_last from tensor memory in a loop (the running
+// sums in registers need a fully unrolled, instruction-cache-heavy body)
+// and writes s + x_last; the next unit starts once it is done, with both
+// accumulators free.
 //
 // Warp roles (320 threads):
 //   warp 8      scheduler and TMA producer: takes units from the counter,
@@ -46,6 +50,8 @@
 //   warps 0-7   epilogue: warp w reads TMEM lanes 32(w%4).. (unit rows) and
 //               columns 128(w/4)..+127; TwoSum fold per chunk; FP64 writes
 //               into A[i][j] and, off the diagonal, the mirror A[j][i]
+//               (built from FP32 pairs with integer operations: GB300's
+//               FP64 rate is far too low for a conversion per entry)
 // Every mbarrier wait is bounded; on time-out the CTA records an error,
 // stops issuing, waits (bounded) for its own copies and MMAs, frees its
 // tensor memory and returns.
@@ -76,6 +82,13 @@ constexpr int kThreads = 32 * (kEpiWarps + 2);
 constexpr int kProducerWarp = kEpiWarps, kMmaWarp = kEpiWarps + 1;
 constexpr uint32_t kWaitLimit = 1u << 24;   // bounded try_wait iterations
 constexpr int kRaster = 8;                  // super-tiles per raster block side
+// Final-phase staging: per epilogue warp a 32 x 16 tile of 8-byte values
+// (4 KB), XOR-swizzled so that row-wise and column-wise accesses are free
+// of bank conflicts; placed after the barrier block.
+constexpr int kStageTileBytes = 32 * 16 * 8;
+constexpr int kBarrierBytes = 256;
+constexpr size_t kSmemBytes =
+    (size_t)kStages * kStageBytes + kBarrierBytes + kEpiWarps * kStageTileBytes + 1024;
 
 // (row ti, column tj) of super-tile t in the blocked order: block rows of
 // kRaster super-tile rows in turn; within one, the diagonal block's upper
@@ -105,19 +118,14 @@ __device__ __forceinline__ bool super_tile(int t, int nt, int& ti, int& tj) {
   return false;
 }
 
-// TMEM accumulator of chunk c of a unit whose first chunk uses `base`:
-// chunks alternate, and the last chunk reuses the second-to-last's
-__device__ __forceinline__ int chunk_acc(int base, int c, int n) {
-  if (n == 1) return base;
-  return base ^ ((c < n - 1 ? c : n - 2) & 1);
+// TMEM accumulator of chunk c of a unit of n chunks: chunks alternate from
+// accumulator 0, and the last chunk reuses the second-to-last's
+__device__ __forceinline__ int chunk_acc(int c, int n) {
+  return n == 1 ? 0 : ((c < n - 1 ? c : n - 2) & 1);
 }
 // first chunk of the unit in its accumulator (starts from zero)
 __device__ __forceinline__ bool chunk_fresh(int c, int n) {
   return c == 0 || (c == 1 && n > 2);
-}
-// accumulator of the next unit's first chunk: the one the last chunk left
-__device__ __forceinline__ int next_base(int base, int n) {
-  return n == 1 ? base ^ 1 : base ^ ((n - 2) & 1) ^ 1;
 }
 
 struct SplitErr {
@@ -127,14 +135,50 @@ struct SplitErr {
 
 // Real-space + self terms of a translation-invariant supercell: rows holds
 // the first nb rows of that part (cell 0, basis sites 0..nb-1, all n
-// columns); entry (i, j) is rows[b_i][offset(c_j - c_i) * nb + b_j] with
-// site i = c_i nb + b_i and cell offsets taken modulo (s0, s1, s2).  With
+// columns) as FP32 pairs hi + lo of the FP64 values (table_split_kernel);
+// entry (i, j) is rows[b_i][offset(c_j - c_i) * nb + b_j] with site
+// i = c_i nb + b_i and cell offsets taken modulo (s0, s1, s2).  With
 // rows == nullptr the output already holds those terms and the epilogue
 // adds to it.
 struct RealTable {
-  const double* rows;
+  const float2* rows;
   int nb, s0, s1, s2;
 };
+
+// s + e exactly for FP32 a + b (Knuth's TwoSum)
+__device__ __forceinline__ float two_sum(float a, float b, float& e) {
+  const float s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+  return s;
+}
+
+// The double nearest below |a + c| (same sign) for an FP32 pair with
+// |c| <= ulp(a) / 2, built with integer operations only: GB300 issues one
+// FP64 warp instruction per 64 cycles per SM sub-partition, too slow for
+// one conversion per output entry.  a's 24 bits fill the top of the 53-bit
+// significand, c is added at its place below them (bits of c under
+// 2^-29 ulp(a) are dropped: a relative error under 2^-52), and a borrow
+// below the leading bit is renormalised.  |a| below 2^-126 gives 0; an
+// infinite or NaN a is converted as is.
+__device__ __forceinline__ double pair_to_double(float a, float c) {
+  const uint32_t ua = __float_as_uint(a), uc = __float_as_uint(c);
+  const int ea = (int)((ua >> 23) & 0xffu);
+  if (ea == 0) return 0.0;
+  if (ea == 0xff) return (double)a;
+  uint64_t m = (uint64_t)((ua & 0x7fffffu) | 0x800000u) << 29;
+  const int ec = (int)((uc >> 23) & 0xffu);
+  if (ec != 0) {
+    const uint64_t mc = (uc & 0x7fffffu) | 0x800000u;
+    const int sh = ec - ea + 29;  // <= 5: |c| <= ulp(a) / 2
+    const uint64_t cm = sh >= 0 ? (mc << sh) : (sh > -25 ? (mc >> -sh) : 0ull);
+    if ((ua ^ uc) >> 31) m -= cm; else m += cm;
+  }
+  int e = ea - 127 + 1023;
+  if (m < (1ull << 52)) { m <<= 1; --e; }
+  return __longlong_as_double((long long)(((uint64_t)(ua >> 31) << 63) |
+                                          ((uint64_t)e << 52) | (m & ((1ull << 52) - 1))));
+}
 
 // (basis, cell x, y, z) of site i in the layout of RealTable
 __device__ __forceinline__ void site_cell(const RealTable& rt, int64_t i, int& b, int& x,
@@ -147,6 +191,21 @@ __device__ __forceinline__ void site_cell(const RealTable& rt, int64_t i, int& b
   y = (int)(r / rt.s2);
   z = (int)(r - (int64_t)y * rt.s2);
 }
+
+// (basis, cell x, y, z) of site i (32-bit arithmetic, i < 2^31)
+__device__ __forceinline__ void site_cell32(const RealTable& rt, int i, int& b, int& x, int& y,
+                                            int& z) {
+  const int c = i / rt.nb;
+  b = i - c * rt.nb;
+  const int yz = rt.s1 * rt.s2;
+  x = c / yz;
+  const int r = c - x * yz;
+  y = r / rt.s2;
+  z = r - y * rt.s2;
+}
+
+// slot of element (r, c) of a 32 x 16 staging tile
+__device__ __forceinline__ int stage_slot(int r, int c) { return r * 16 + (c ^ (r & 15)); }
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
   return (uint32_t)__cvta_generic_to_shared(p);
@@ -315,9 +374,10 @@ constexpr int kEpiCols = kCols / 2;  // columns per epilogue thread
 
 // s += x (Knuth TwoSum) over this thread's kEpiCols columns of the chunk in
 // t_acc; the rounding errors, plus with take_other the pending errors held
-// in t_oth, are written back into t_acc for the next chunk to build on.
+// in t_oth, are written back into t_acc for the next chunk to build on, and
+// with save_sum the new sums go to t_oth.
 __device__ __forceinline__ void fold_chunk(uint32_t t_acc, uint32_t t_oth, bool take_other,
-                                           float (&s)[kEpiCols]) {
+                                           bool save_sum, float (&s)[kEpiCols]) {
 #pragma unroll
   for (int g = 0; g < kEpiCols / 8; ++g) {
     uint32_t x[8], o[8];
@@ -326,16 +386,17 @@ __device__ __forceinline__ void fold_chunk(uint32_t t_acc, uint32_t t_oth, bool 
     tmem_ld_wait();
 #pragma unroll
     for (int q = 0; q < 8; ++q) {
-      const float xv = __uint_as_float(x[q]);
-      const float h = s[g * 8 + q];
-      const float sum = __fadd_rn(h, xv);
-      const float bb = __fsub_rn(sum, h);
-      float e = __fadd_rn(__fsub_rn(h, __fsub_rn(sum, bb)), __fsub_rn(xv, bb));
+      float e;
+      s[g * 8 + q] = two_sum(s[g * 8 + q], __uint_as_float(x[q]), e);
       if (take_other) e = __fadd_rn(e, __uint_as_float(o[q]));
-      s[g * 8 + q] = sum;
       x[q] = __float_as_uint(e);
     }
     tmem_st8(t_acc + (uint32_t)(g * 8), x);
+    if (save_sum) {
+#pragma unroll
+      for (int q = 0; q < 8; ++q) o[q] = __float_as_uint(s[g * 8 + q]);
+      tmem_st8(t_oth + (uint32_t)(g * 8), o);
+    }
   }
   tmem_st_wait();
 }
@@ -355,10 +416,12 @@ __global__ void __launch_bounds__(kThreads, 1)
   uint64_t* acc_empty = acc_full + 2;
   uint64_t* ring_full = acc_empty + 2;
   uint64_t* ring_empty = ring_full + kRing;
-  uint64_t* drain = ring_empty + kRing;
+  uint64_t* unit_free = ring_empty + kRing;
+  uint64_t* drain = unit_free + 1;
   volatile int* ring_unit = (volatile int*)(drain + 1);
   volatile uint32_t* tmem_slot = (volatile uint32_t*)(ring_unit + kRing);
   volatile int* abort_flag = (volatile int*)(tmem_slot + 1);
+  float2* stage_tiles = (float2*)(smem + kStages * kStageBytes + kBarrierBytes);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int n_chunks = (k_blocks + chunk_blocks - 1) / chunk_blocks;
@@ -377,6 +440,7 @@ __global__ void __launch_bounds__(kThreads, 1)
       mbar_init(&ring_full[r], 1);
       mbar_init(&ring_empty[r], 1 + kEpiWarps);
     }
+    mbar_init(unit_free, kEpiWarps);
     mbar_init(drain, 1);
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -452,8 +516,8 @@ __global__ void __launch_bounds__(kThreads, 1)
     // ---------------- MMA issuer ----------------
     if (lane == 0) {
       const int ksteps = kSlice / 32;  // 32-byte K steps (16 BF16 / 8 TF32)
-      int gkb = 0, base = 0;
-      int uses[2] = {0, 0};  // chunks issued into each accumulator so far
+      int gkb = 0;
+      int waits[2] = {0, 0};  // acc_empty completions awaited so far
       bool ok = true;
       for (int i = 0; ok; ++i) {
         const int r = i % kRing;
@@ -464,15 +528,23 @@ __global__ void __launch_bounds__(kThreads, 1)
         const int u = ring_unit[r];
         mbar_arrive(&ring_empty[r]);
         if (u < 0) break;
+        // both accumulators free: the previous unit's last epilogue is done
+        if (i > 0 && !mbar_wait(unit_free, (uint32_t)(i - 1) & 1u, abort_flag)) {
+          *abort_flag = 1;
+          break;
+        }
         int kb = 0;
         for (int c = 0; c < n_chunks; ++c) {
-          const int b = chunk_acc(base, c, n_chunks);
-          if (!mbar_wait(&acc_empty[b], ((uint32_t)uses[b] & 1u) ^ 1u, abort_flag)) {
-            *abort_flag = 1; ok = false; break;
+          const int b = chunk_acc(c, n_chunks);
+          const bool fresh = chunk_fresh(c, n_chunks);
+          if (!fresh) {
+            if (!mbar_wait(&acc_empty[b], (uint32_t)waits[b] & 1u, abort_flag)) {
+              *abort_flag = 1; ok = false; break;
+            }
+            ++waits[b];
           }
           asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
           const uint32_t d = tmem + (uint32_t)(b * kCols);
-          const bool fresh = chunk_fresh(c, n_chunks);
           const int kb_end = min(k_blocks, (c + 1) * chunk_blocks);
           for (int first = 1; kb < kb_end; ++kb, ++gkb, first = 0) {
             const int s = gkb % kStages;
@@ -493,9 +565,7 @@ __global__ void __launch_bounds__(kThreads, 1)
           }
           if (!ok) break;
           umma_commit(&acc_full[b]);  // chunk finished
-          ++uses[b];
         }
-        base = next_base(base, n_chunks);
       }
       // drain: every issued MMA has completed once this commit arrives
       umma_commit(drain);
@@ -507,10 +577,8 @@ __global__ void __launch_bounds__(kThreads, 1)
     const uint32_t lane_base =
         tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(half * kEpiCols);
     float s[kEpiCols];  // running sums of this thread's columns
-    int base = 0;
-    int uses[2] = {0, 0};
-    bool ok = true;
-    for (int i = 0; ok; ++i) {
+    int seen[2] = {0, 0};  // acc_full completions consumed so far
+    for (int i = 0;; ++i) {
       const int r = i % kRing;
       bool got = false;
       int u = -1;
@@ -532,88 +600,136 @@ __global__ void __launch_bounds__(kThreads, 1)
       const int64_t col0 = (int64_t)tj * kCols + half * kEpiCols;
 #pragma unroll
       for (int q = 0; q < kEpiCols; ++q) s[q] = 0.f;
-      for (int c = 0; c < n_chunks; ++c) {
-        const int b = chunk_acc(base, c, n_chunks);
-        if (!warp_wait(&acc_full[b], (uint32_t)uses[b] & 1u, abort_flag)) {
+      bool ok = true;
+      for (int c = 0; c < n_chunks - 1; ++c) {
+        const int b = chunk_acc(c, n_chunks);
+        if (!warp_wait(&acc_full[b], (uint32_t)seen[b] & 1u, abort_flag)) {
           if (lane == 0) *abort_flag = 1;
           ok = false;
           break;
         }
-        ++uses[b];
+        ++seen[b];
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        const uint32_t t_acc = lane_base + (uint32_t)(b * kCols);
-        if (c < n_chunks - 1) {
-          // the second-to-last chunk also takes the other accumulator's
-          // pending error (left there by chunk n - 3, which kept it)
-          const bool take_other = c == n_chunks - 2 && n_chunks >= 3;
-          fold_chunk(t_acc, lane_base + (uint32_t)((b ^ 1) * kCols), take_other, s);
-          asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-          __syncwarp();
-          if (lane == 0) {
-            if (c != n_chunks - 3) mbar_arrive(&acc_empty[b]);
-            if (take_other) mbar_arrive(&acc_empty[b ^ 1]);
-          }
-          continue;
-        }
-        // last chunk: write (double)s + (double)x.  The diagonal is
-        // F_i . F_i = sum_k w_k (cos^2 + sin^2) = sum_k w_k exactly, taken
-        // from the FP64 weight sum.  With a real-space table the entry (and
-        // its mirror) is written once as table value + Fourier value;
-        // otherwise it is added to the real and self terms already there.
-        const bool live = row < n;
-        const bool mirror = ti != tj;
-        const int nn = (int)n, irow = (int)row;
-        double* orow = out + (live ? row : 0) * n;  // A[row][.]
-        double* ocol = out + col0 * n + row;        // A[col][row], advanced by n
-        int rx = 0, ry = 0, rz = 0, cbs = 0, cx = 0, cy = 0, cz = 0;
-        const double* trow = nullptr;
-        if (rt.rows) {
-          int rb = 0;
-          if (live) site_cell(rt, row, rb, rx, ry, rz);
-          trow = rt.rows + (int64_t)rb * n;
-          site_cell(rt, col0, cbs, cx, cy, cz);
-        }
-#pragma unroll
-        for (int g = 0; g < kEpiCols / 8; ++g) {
-          uint32_t x[8];
-          tmem_ld8_nowait(t_acc + (uint32_t)(g * 8), x);
-          tmem_ld_wait();
-#pragma unroll
-          for (int q = 0; q < 8; ++q) {
-            const int col = (int)col0 + g * 8 + q;
-            if (live && col < nn) {
-              double v = (double)s[g * 8 + q] + (double)__uint_as_float(x[q]);
-              if (col == irow) v = diag_value;
-              if (trow) {
-                int dx = cx - rx, dy = cy - ry, dz = cz - rz;
-                if (dx < 0) dx += rt.s0;
-                if (dy < 0) dy += rt.s1;
-                if (dz < 0) dz += rt.s2;
-                const int o = ((dx * rt.s1 + dy) * rt.s2 + dz) * rt.nb + cbs;
-                const double a = __dadd_rn(__ldg(trow + o), v);
-                orow[col] = a;
-                if (mirror) *ocol = a;
-              } else {
-                orow[col] += v;
-                if (mirror) *ocol += v;
-              }
-            }
-            ocol += n;
-            // next column's site in the layout
-            if (trow && ++cbs == rt.nb) {
-              cbs = 0;
-              if (++cz == rt.s2) {
-                cz = 0;
-                if (++cy == rt.s1) { cy = 0; ++cx; }
-              }
-            }
-          }
-        }
+        // the second-to-last chunk takes the other accumulator's pending
+        // error (left there by chunk n - 3) and leaves s there instead
+        const bool last_fold = c == n_chunks - 2;
+        fold_chunk(lane_base + (uint32_t)(b * kCols), lane_base + (uint32_t)((b ^ 1) * kCols),
+                   last_fold && n_chunks >= 3, last_fold, s);
         asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
         __syncwarp();
-        if (lane == 0) mbar_arrive(&acc_empty[b]);
+        // chunk n - 3's accumulator is not used again in this unit
+        if (lane == 0 && c != n_chunks - 3) mbar_arrive(&acc_empty[b]);
       }
-      base = next_base(base, n_chunks);
+      if (!ok) break;
+      // last chunk: the Fourier part is s + x.  The diagonal is
+      // F_i . F_i = sum_k w_k (cos^2 + sin^2) = sum_k w_k exactly, taken
+      // from the FP64 weight sum.  With a real-space table the entry (and
+      // its mirror) is written once as table value + Fourier value, summed
+      // as FP32 pairs (relative error ~2^-47); otherwise it is added to the
+      // real and self terms already in the output.
+      const int b = chunk_acc(n_chunks - 1, n_chunks);
+      if (!warp_wait(&acc_full[b], (uint32_t)seen[b] & 1u, abort_flag)) {
+        if (lane == 0) *abort_flag = 1;
+        break;
+      }
+      ++seen[b];
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const uint32_t t_x = lane_base + (uint32_t)(b * kCols);
+      const uint32_t t_s = lane_base + (uint32_t)((b ^ 1) * kCols);
+      // Each 16-column group goes through this warp's staging tile: s + x is
+      // formed with lane = row (the TMEM layout), the table value is added
+      // and the entry stored with 16 lanes along a row (contiguous table
+      // reads and row stores), and the mirror is stored with lane = row
+      // again (contiguous column stores).
+      const bool mirror = ti != tj;
+      const int nn = (int)n;
+      const int row0 = (int)(row - lane);       // first row of this warp
+      // this lane's row and, in the row-wise step, its column offset
+      int rpack0 = 0, rpack1 = 0;               // (basis, x) and (y, z) of row
+      if (rt.rows && row < n) {
+        int rb = 0, rx = 0, ry = 0, rz = 0;
+        site_cell32(rt, (int)row, rb, rx, ry, rz);
+        rpack0 = (rb << 16) | rx;
+        rpack1 = (ry << 16) | rz;
+      }
+      float2* tile = stage_tiles + warp * (kStageTileBytes / 8);
+      double* tiled = reinterpret_cast<double*>(tile);
+      const int cc = lane & 15, rsub = lane >> 4;
+#pragma unroll 1
+      for (int g = 0; g < kEpiCols / 16; ++g) {
+        uint32_t x[16], sv[16];
+        tmem_ld16_nowait(t_x + (uint32_t)(g * 16), x);
+        if (n_chunks >= 2) {
+          tmem_ld16_nowait(t_s + (uint32_t)(g * 16), sv);
+        } else {
+#pragma unroll
+          for (int q = 0; q < 16; ++q) sv[q] = 0u;
+        }
+        tmem_ld_wait();
+#pragma unroll
+        for (int q = 0; q < 16; ++q) {
+          float l;
+          const float h = two_sum(__uint_as_float(sv[q]), __uint_as_float(x[q]), l);
+          tile[stage_slot(lane, q)] = make_float2(h, l);
+        }
+        __syncwarp();
+        // row-wise: lanes 0-15 take row 2k, lanes 16-31 row 2k + 1
+        const int gcol = (int)col0 + g * 16 + cc;
+        int cbs = 0, cx = 0, cy = 0, cz = 0;
+        if (rt.rows && gcol < nn) site_cell32(rt, gcol, cbs, cx, cy, cz);
+#pragma unroll 4
+        for (int k = 0; k < 16; ++k) {
+          const int rr = 2 * k + rsub;
+          const int grow = row0 + rr;
+          const int slot = stage_slot(rr, cc);
+          const float2 hl = tile[slot];
+          const int p0 = __shfl_sync(0xffffffffu, rpack0, rr);
+          const int p1 = __shfl_sync(0xffffffffu, rpack1, rr);
+          double a = 0.0;
+          if (grow < nn && gcol < nn) {
+            double* at = out + (int64_t)grow * n + gcol;
+            if (rt.rows) {
+              int dx = cx - (p0 & 0xffff), dy = cy - (p1 >> 16), dz = cz - (p1 & 0xffff);
+              if (dx < 0) dx += rt.s0;
+              if (dy < 0) dy += rt.s1;
+              if (dz < 0) dz += rt.s2;
+              const int o = ((dx * rt.s1 + dy) * rt.s2 + dz) * rt.nb + cbs;
+              const float2 t = __ldg(rt.rows + (int64_t)(p0 >> 16) * n + o);
+              if (gcol == grow) {
+                a = __dadd_rn(__dadd_rn((double)t.x, (double)t.y), diag_value);
+              } else {
+                // table + Fourier in FP32 pairs, then one conversion
+                float e1, e2;
+                const float w1 = two_sum(hl.x, t.x, e1);
+                const float w2 = two_sum(w1, __fadd_rn(__fadd_rn(hl.y, t.y), e1), e2);
+                a = pair_to_double(w2, e2);
+              }
+              *at = a;
+            } else {
+              a = gcol == grow ? diag_value : pair_to_double(hl.x, hl.y);
+              *at += a;
+            }
+          }
+          tiled[slot] = a;
+        }
+        __syncwarp();
+        if (mirror && row < n) {
+          // A[col][row]: lane = row, 32 consecutive doubles per column
+#pragma unroll 4
+          for (int q = 0; q < 16; ++q) {
+            const int mcol = (int)col0 + g * 16 + q;
+            if (mcol < nn) {
+              double* at = out + (int64_t)mcol * n + row;
+              const double a = tiled[stage_slot(lane, q)];
+              if (rt.rows) *at = a; else *at += a;
+            }
+          }
+        }
+        __syncwarp();
+      }
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      __syncwarp();
+      if (lane == 0) mbar_arrive(unit_free);
     }
   }
 
@@ -627,6 +743,17 @@ __global__ void __launch_bounds__(kThreads, 1)
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
                  "r"(kTmemCols));
   }
+}
+
+// The real-space table rewritten in place as FP32 pairs: entry i becomes
+// (hi, lo) = (RN(v), RN(v - hi)), v - hi - lo below 2^-48 |v|.
+__global__ void table_split_kernel(double* __restrict__ rows, int64_t count) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= count) return;
+  const double v = rows[i];
+  const float hi = __double2float_rn(v);
+  const float lo = __double2float_rn(__dsub_rn(v, (double)hi));
+  reinterpret_cast<float2*>(rows)[i] = make_float2(hi, lo);
 }
 
 // sum_k w_k = F_i . F_i, with w_k = 2 c_k / (k^2 eps) as in the feature rows
@@ -809,7 +936,7 @@ size_t ewald_split_workspace_bytes(const PycdEwaldDesc* d, int mode) {
 
 int ewald_build_split(const PycdEwaldDesc* d, int mode, double* out,
                       const double* kc, const double* k2, const double* ck,
-                      const double* real_rows, void* ws, size_t ws_bytes, cudaStream_t s) {
+                      double* real_rows, void* ws, size_t ws_bytes, cudaStream_t s) {
   const bool tf32 = mode == PYCD_EWALD_TF32X3;
   const int64_t n = d->n_sites, K = d->n_kvec, kdim = 2 * K;
   const int64_t ld = split_ld(kdim, tf32);
@@ -848,7 +975,11 @@ int ewald_build_split(const PycdEwaldDesc* d, int mode, double* out,
   PYCD_CUDA(cudaMemsetAsync(flag, 0, 2 * sizeof(int), s));
   RealTable rt{};
   if (real_rows) {
-    rt.rows = real_rows;
+    const int64_t count = (int64_t)d->basis_sites * n;
+    table_split_kernel<<<(unsigned)((count + 255) / 256), 256, 0, s>>>(
+        real_rows, count);
+    PYCD_CUDA(cudaGetLastError());
+    rt.rows = reinterpret_cast<const float2*>(real_rows);
     rt.nb = d->basis_sites;
     rt.s0 = d->supercell[0];
     rt.s1 = d->supercell[1];
@@ -877,7 +1008,7 @@ int ewald_build_split(const PycdEwaldDesc* d, int mode, double* out,
   }
   const int k_blocks = (int)(ld / (kSlice / es));
   const int chunk_blocks = (int)(kChunkCols / (kSlice / es));
-  const size_t smem = (size_t)kStages * kStageBytes + 1024 + 256;
+  const size_t smem = kSmemBytes;
   // super-tiles per side; each of the nt (nt + 1) / 2 upper-triangle
   // super-tiles is two units, taken by one persistent CTA per SM
   const int nt = (int)((n + kCols - 1) / kCols);
