@@ -424,6 +424,11 @@ PYCD_API int pycd_debug_exp(const double* d_x, int64_t n, double* d_ours,
  * doubles).  No counterpart in the reference.                              */
 PYCD_API int pycd_debug_exp_table(double* h_out);
 
+/* The same values as the integer exp's table: h_out[j] = 2^(j/4096) 2^62
+ * rounded to an integer, j < 4096, built from the pairs above with integer
+ * operations (no device needed).  No counterpart in the reference.          */
+PYCD_API int pycd_debug_exp_table_fixed(uint64_t* h_out);
+
 /* ---------------------------------------------------------------------------
  * Mean squared displacement: Analysis.compute_msd (PyCD/core.py:2974-3081)
  * on unwrapped trajectory rows already in device memory.

@@ -164,6 +164,7 @@ _PROTOS = {
     "pycd_debug_exp": (C.c_int, [C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p,
                                  C.c_void_p]),
     "pycd_debug_exp_table": (C.c_int, [C.c_void_p]),
+    "pycd_debug_exp_table_fixed": (C.c_int, [C.c_void_p]),
     "pycd_ewald_kvector_energies": (C.c_int, [P(EwaldDesc), C.c_void_p, C.c_void_p,
                                               C.c_void_p]),
     "pycd_msd_compute": (C.c_int, [P(MsdDesc), C.c_void_p, C.c_void_p, C.c_void_p,

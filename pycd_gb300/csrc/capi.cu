@@ -426,4 +426,13 @@ int pycd_debug_exp_table(double* h_out) {
   return PYCD_OK;
 }
 
+int pycd_debug_exp_table_fixed(uint64_t* h_out) {
+  clear_error();
+  PYCD_REQUIRE(h_out, "bad arguments");
+  double2 pairs[4096];
+  exp_table_host(pairs);
+  exp_fix_host(pairs, h_out);
+  return PYCD_OK;
+}
+
 }  // extern "C"

@@ -6,6 +6,7 @@
 #include <string.h>
 
 #include <cmath>
+#include <cstring>
 #include <mutex>
 
 #include "kmc_device.cuh"
@@ -37,7 +38,29 @@ void exp_table_host(double2* out) {
   }
 }
 
-// Fill the exp table of every KMC translation unit on the current device
+// T_j = round(2^(j/4096) 2^62) from the (hi, lo) pairs, with integer
+// operations only: hi in [1, 2) is its 53-bit significand times 2^10, and
+// lo (|lo| < 2^-53) adds its value in 2^-62 units rounded to nearest.
+void exp_fix_host(const double2* pairs, uint64_t* out) {
+  const uint64_t mask52 = (1ull << 52) - 1;
+  for (int j = 0; j < 4096; ++j) {
+    uint64_t hb, lb;
+    std::memcpy(&hb, &pairs[j].x, sizeof hb);
+    std::memcpy(&lb, &pairs[j].y, sizeof lb);
+    int64_t t = (int64_t)(((hb & mask52) | (1ull << 52)) << 10);
+    const int el = (int)((lb >> 52) & 0x7ff);
+    if (el != 0) {
+      // lo = ml 2^(el - 1075): ml 2^(el - 1013) in 2^-62 units
+      const uint64_t ml = (lb & mask52) | (1ull << 52);
+      const int sh = 1013 - el;  // >= 44
+      const int64_t q = sh < 64 ? (int64_t)((ml + (1ull << (sh - 1))) >> sh) : 0;
+      t += (lb >> 63) ? -q : q;
+    }
+    out[j] = (uint64_t)t;
+  }
+}
+
+// Fill the exp tables of every KMC translation unit on the current device
 // (once per device; device ordinals >= kMaxDevices are rejected).  A
 // cudaDeviceReset zeroes the tables without clearing this record: the
 // library is not usable across a device reset.
@@ -45,6 +68,7 @@ int kmc_exp_init() {
   static std::mutex mu;
   static bool done[kMaxDevices] = {false};
   static double2 host[4096];
+  static uint64_t host_fix[4096];
   static bool built = false;
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
@@ -54,11 +78,12 @@ int kmc_exp_init() {
   if (done[dev]) return PYCD_OK;
   if (!built) {
     exp_table_host(host);
+    exp_fix_host(host, host_fix);
     built = true;
   }
-  e = exp_table_upload(host);
-  if (e == cudaSuccess) e = kmc_exp_upload_capped(host);
-  if (e == cudaSuccess) e = kmc_exp_upload_cta(host);
+  e = exp_table_upload(host, host_fix);
+  if (e == cudaSuccess) e = kmc_exp_upload_capped(host, host_fix);
+  if (e == cudaSuccess) e = kmc_exp_upload_cta(host, host_fix);
   if (e != cudaSuccess) return cuda_fail(e, "exp table upload", __FILE__, __LINE__);
   done[dev] = true;
   return PYCD_OK;
@@ -131,7 +156,7 @@ __global__ void exp_probe_kernel(const double* __restrict__ x, int64_t n,
                                  double* __restrict__ ref) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  ours[i] = exp_tang(x[i]);
+  ours[i] = kmc_exp(x[i]);
   ref[i] = exp(x[i]);
 }
 

@@ -30,7 +30,9 @@ cudaError_t kmc_preload_capped() {
   return e;
 }
 
-// this translation unit's copy of the exp table
-cudaError_t kmc_exp_upload_capped(const double2* h_tab) { return exp_table_upload(h_tab); }
+// this translation unit's copy of the exp tables
+cudaError_t kmc_exp_upload_capped(const double2* h_tab, const uint64_t* h_fix) {
+  return exp_table_upload(h_tab, h_fix);
+}
 
 }  // namespace pycd

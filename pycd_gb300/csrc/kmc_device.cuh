@@ -34,9 +34,12 @@
 //   (the plain form) and inside a batch of thousands give identical events.
 //   The event is the first process whose cumulative rate exceeds u1 k_tot
 //   (core.py:2796-2800); t -= log(u2) / k_tot (core.py:2802-2803).
-// exp() is Tang's table-driven method (ACM TOMS 15(2), 1989): reduction by
-// ln2/4096 with a 4096-entry table of 2^(j/4096) in two parts and a degree-3
-// polynomial on |r| <= ln2/8192 (about 0.52 ulp; 9 FP64 instructions).
+// exp() is a table-driven method after Tang (ACM TOMS 15(2), 1989):
+// x = n ln2/4096 + r, exp(x) = 2^(n/4096) (1 + expm1(r)).  For |x| < 704 it
+// runs on the integer pipe (kmc_exp, below): GB300 issues one FP64 warp
+// instruction per 64 cycles per SM sub-partition, and the rates' exp() was
+// the largest share of the step's FP64 instructions.  Outside that range
+// the FP64 form of the same method is used.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -62,9 +65,13 @@ __device__ __forceinline__ double ddiv(double a, double b) { return __ddiv_rn(a,
 // includes this header has its own copy; the library fills each once per
 // device (exp_table_upload) before any kernel of the unit runs.
 static __device__ double2 g_exp2_tab[4096];
+// g_exp2_fix[j] = 2^(j/4096) 2^62 rounded to an integer (exp_fix_host)
+static __device__ uint64_t g_exp2_fix[4096];
 
-static inline cudaError_t exp_table_upload(const double2* h_tab) {
-  return cudaMemcpyToSymbol(g_exp2_tab, h_tab, sizeof(double2) * 4096);
+static inline cudaError_t exp_table_upload(const double2* h_tab, const uint64_t* h_fix) {
+  cudaError_t e = cudaMemcpyToSymbol(g_exp2_tab, h_tab, sizeof(double2) * 4096);
+  if (e == cudaSuccess) e = cudaMemcpyToSymbol(g_exp2_fix, h_fix, sizeof(uint64_t) * 4096);
+  return e;
 }
 
 // v = 2^(j/4096) (1 + expm1(r)) in [2^-1/8192, 2^(1+1/8192)) for
@@ -99,13 +106,69 @@ static __device__ __noinline__ double exp_tang_wide(double x) {
   return dmul(v2, 5.421010862427522e-20);  // 2^-64
 }
 
-__device__ __forceinline__ double exp_tang(double x) {
-  // |x| < 704 (high word below 0x40860000) keeps |m| <= 1016: no overflow,
-  // no subnormal result, and the range test stays off the FP64 pipe
+// exp(x) for |x| < 704 with integer instructions only.
+//   n:  round(|x| 4096/ln2) from the top 32 bits of x's significand times
+//       4096/ln2 in 32 bits (off by at most one from the true rounding, so
+//       |r| <= 0.51 ln2/4096);
+//   r:  x - n ln2/4096 in 2^-88 units (x is exact there; ln2/4096 to 76
+//       bits), kept in 2^-64 units; for |x| < 2^-13, n = 0 and r = x;
+//   p:  expm1(r) = r + r^2/2 + r^3/6 + r^4/24 in 2^-64 units (r^5/120 is
+//       below one unit);
+//   v:  2^(j/4096) (1 + p) from the 62-bit table, j = n mod 4096, rounded
+//       once to 53 bits and scaled by 2^floor(n/4096) in the exponent.
+// v carries a relative error near 2^-61, so the result is within ~0.502
+// ulp of exp(x) (correctly rounded in all but ~0.1 % of arguments).
+constexpr uint64_t kExpC19 = 3098164009ull;           // 4096/ln2 2^19
+constexpr uint64_t kExpL88Hi = 0xb17ull;              // ln2/4096 2^88 =
+constexpr uint64_t kExpL88Lo = 0x217f7d1cf79abc9eull;  //   Hi 2^64 + Lo
+
+__device__ __forceinline__ double exp_int(double x) {
+  const uint64_t b = (uint64_t)__double_as_longlong(x);
+  const bool neg = (b >> 63) != 0;
+  const int eb = (int)((b >> 52) & 0x7ff);
+  const uint64_t mx = (b & 0xFFFFFFFFFFFFFull) | (eb ? (1ull << 52) : 0ull);
+  const int ex = eb - 1023;  // |x| = mx 2^(ex - 52)
+  int64_t nm = 0, rm;        // |n| and the reduced magnitude
+  if (ex >= -13) {
+    const int sh = 50 - ex;  // 41 ... 63 for ex in [-13, 9]
+    const uint64_t pr = (mx >> 21) * kExpC19;
+    nm = (int64_t)((pr + (1ull << (sh - 1))) >> sh);
+    const unsigned __int128 xf = (unsigned __int128)mx << (ex + 36);
+    const unsigned __int128 lf = ((unsigned __int128)kExpL88Hi << 64) | kExpL88Lo;
+    const __int128 d = (__int128)(xf - (unsigned __int128)(uint64_t)nm * lf);
+    rm = (int64_t)(d >> 24);
+  } else {
+    const int s = -ex - 12;  // >= 2
+    rm = s < 64 ? (int64_t)(mx >> s) : 0;
+  }
+  const int64_t n = neg ? -nm : nm;
+  const int64_t r = neg ? -rm : rm;
+  const int64_t r2 = __mul64hi(r, r);
+  const int64_t r3 = __mul64hi(r2, r);
+  const int64_t r4 = __mul64hi(r2, r2);
+  const int64_t p = r + (r2 >> 1) + r3 / 6 + r4 / 24;
+  const uint64_t t = __ldg(reinterpret_cast<const unsigned long long*>(g_exp2_fix) +
+                           (n & 4095));
+  // 2^(j/4096) (1 + p) in 2^-62 units: the top bit is bit 61 or 62
+  const uint64_t v = t + (uint64_t)__mul64hi((int64_t)t, p);
+  const int lead = 63 - __clzll((long long)v);
+  const int sh = lead - 52;
+  uint64_t m53 = v >> sh;
+  const uint64_t rem = v & ((1ull << sh) - 1), half = 1ull << (sh - 1);
+  if (rem > half || (rem == half && (m53 & 1))) ++m53;
+  int e = lead - 62 + (int)(n >> 12) + 1023;
+  if (m53 >> 53) {
+    m53 >>= 1;
+    ++e;
+  }
+  return __longlong_as_double((long long)(((uint64_t)e << 52) | (m53 & 0xFFFFFFFFFFFFFull)));
+}
+
+// The KMC kernels' exp: the integer form for |x| < 704 (high word below
+// 0x40860000, a test on the integer pipe), the FP64 form outside.
+__device__ __forceinline__ double kmc_exp(double x) {
   if ((__double2hiint(x) & 0x7fffffff) >= 0x40860000) return exp_tang_wide(x);
-  int m;
-  const double v = exp_tang_core(x, m);
-  return __hiloint2double(__double2hiint(v) + (m << 20), __double2loint(v));
+  return exp_int(x);
 }
 
 // a > b for doubles known to be >= +0 and not NaN: their bit patterns order
@@ -506,7 +569,7 @@ __device__ __forceinline__ void process_rates(const ProcCache<MAXP>& pc, double 
     if (pc.valid[j]) {
       term[j] = fma(q, dsub(pc.P[j], pc.Q[j]), pc.cq[j]);
       const double xs = fma(pc.xa[j], term[j], pc.xb[j]);
-      kp[j] = exp_tang(fma(-xs, xs, pc.c0[j]));
+      kp[j] = kmc_exp(fma(-xs, xs, pc.c0[j]));
     }
   }
 }

@@ -35,12 +35,14 @@ struct KmcArgs {
 int kmc_launch(const KmcArgs& a, int max_np, int max_nc,
                const PycdKmcLaunch* launch, cudaStream_t s);
 int kmc_preload();
-// the exp table: built on the host (exp_table_host, 4096 (hi, lo) pairs),
-// copied into each KMC translation unit once per device (kmc_exp_init)
+// the exp tables: built on the host (exp_table_host, 4096 (hi, lo) pairs;
+// exp_fix_host, the same values as 62-bit integers), copied into each KMC
+// translation unit once per device (kmc_exp_init)
 void exp_table_host(double2* out);
+void exp_fix_host(const double2* pairs, uint64_t* out);
 int kmc_exp_init();
-cudaError_t kmc_exp_upload_capped(const double2* h_tab);
-cudaError_t kmc_exp_upload_cta(const double2* h_tab);
+cudaError_t kmc_exp_upload_capped(const double2* h_tab, const uint64_t* h_fix);
+cudaError_t kmc_exp_upload_cta(const double2* h_tab, const uint64_t* h_fix);
 int kmc_default_lanes(int max_np, int max_nc, int64_t n_traj);
 // the register-capped instances (kmc_capped.cu); *found = false when
 // there is no instance for (G, MAXP)

@@ -64,6 +64,19 @@ def test_exp_table_is_correctly_rounded():
         assert abs(lo[j]) < math.ulp(hi[j]) / 2 and hi[j] + lo[j] == hi[j], j
 
 
+def test_exp_fixed_table_is_correctly_rounded():
+    """The integer exp's table: 2^(j/4096) 2^62 rounded to the nearest
+    integer, built by the library from the (hi, lo) pairs with integer
+    operations only (so every host builds the same table)."""
+    mp = pytest.importorskip("mpmath")
+    mp.mp.prec = 200
+    out = np.zeros(4096, np.uint64)
+    nat.check(nat.lib().pycd_debug_exp_table_fixed(out.ctypes.data_as(ctypes.c_void_p)))
+    for j in range(4096):
+        exact = int(mp.nint(mp.mpf(2) ** (mp.mpf(j) / 4096) * mp.mpf(2) ** 62))
+        assert int(out[j]) == exact, j
+
+
 def test_library_reports_missing_device_as_error():
     import torch
     if torch.cuda.is_available():
