@@ -104,7 +104,10 @@ typedef enum PycdEwaldMode {
   PYCD_EWALD_FP64_GEMM = 1,
   /* Same contraction on tcgen05 tensor cores: F split into BF16 hi + lo,
    * three products (hi.hi + hi.lo + lo.hi), FP32 accumulation in TMEM per
-   * K-chunk, FP64 sum across chunks.                                       */
+   * K-chunk, error-free sum across chunks.  Runs on CTA pairs (2-CTA
+   * clusters, 256-row MMAs) where the device can place them, else on
+   * single CTAs; the environment variable PYCD_SPLIT_FORM=single forces
+   * the single-CTA form (same results).                                    */
   PYCD_EWALD_BF16X3 = 2,
   /* As BF16X3 with TF32 operands (hi + lo split, three products).         */
   PYCD_EWALD_TF32X3 = 3

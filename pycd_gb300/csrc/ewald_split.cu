@@ -40,6 +40,10 @@
 // and writes s + x_last; the next unit starts once it is done, with both
 // accumulators free.
 //
+// A CTA-pair form (ewald_split_pair_kernel, below) computes whole
+// super-tiles on 2-CTA clusters with 256-row MMAs and is used where the
+// device can place such clusters; the single-CTA form is the fallback.
+//
 // Warp roles (320 threads):
 //   warp 8      scheduler and TMA producer: takes units from the counter,
 //               hands them to the other warps through a 4-entry ring, loads
@@ -59,6 +63,8 @@
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
 
 #include "common.cuh"
 
@@ -401,6 +407,110 @@ __device__ __forceinline__ void fold_chunk(uint32_t t_acc, uint32_t t_oth, bool 
   tmem_st_wait();
 }
 
+// Last chunk of a unit: writes s + x (x in t_x, s in t_s; s = 0 for a
+// one-chunk unit) plus the real-space table for this thread's row `row` and
+// columns col0 .. col0 + kEpiCols - 1, and with `mirror` the transposed
+// entries.  The diagonal is F_i . F_i = sum_k w_k (cos^2 + sin^2) =
+// sum_k w_k exactly, taken from the FP64 weight sum.  With a real-space
+// table the entry (and its mirror) is written once as table value + Fourier
+// value, summed as FP32 pairs (relative error ~2^-47); otherwise it is
+// added to the real and self terms already in the output.
+__device__ __forceinline__ void write_unit(uint32_t t_x, uint32_t t_s, int n_chunks,
+                                           int64_t row, int64_t col0, bool mirror, int64_t n,
+                                           double* __restrict__ out, const RealTable& rt,
+                                           double diag_value, float2* tile) {
+  const int lane = threadIdx.x & 31;
+  // Each 16-column group goes through this warp's staging tile: s + x is
+  // formed with lane = row (the TMEM layout), the table value is added
+  // and the entry stored with 16 lanes along a row (contiguous table
+  // reads and row stores), and the mirror is stored with lane = row
+  // again (contiguous column stores).
+  const int nn = (int)n;
+  const int row0 = (int)(row - lane);       // first row of this warp
+  // this lane's row and, in the row-wise step, its column offset
+  int rpack0 = 0, rpack1 = 0;               // (basis, x) and (y, z) of row
+  if (rt.rows && row < n) {
+    int rb = 0, rx = 0, ry = 0, rz = 0;
+    site_cell32(rt, (int)row, rb, rx, ry, rz);
+    rpack0 = (rb << 16) | rx;
+    rpack1 = (ry << 16) | rz;
+  }
+  double* tiled = reinterpret_cast<double*>(tile);
+  const int cc = lane & 15, rsub = lane >> 4;
+#pragma unroll 1
+  for (int g = 0; g < kEpiCols / 16; ++g) {
+    uint32_t x[16], sv[16];
+    tmem_ld16_nowait(t_x + (uint32_t)(g * 16), x);
+    if (n_chunks >= 2) {
+      tmem_ld16_nowait(t_s + (uint32_t)(g * 16), sv);
+    } else {
+#pragma unroll
+      for (int q = 0; q < 16; ++q) sv[q] = 0u;
+    }
+    tmem_ld_wait();
+#pragma unroll
+    for (int q = 0; q < 16; ++q) {
+      float l;
+      const float h = two_sum(__uint_as_float(sv[q]), __uint_as_float(x[q]), l);
+      tile[stage_slot(lane, q)] = make_float2(h, l);
+    }
+    __syncwarp();
+    // row-wise: lanes 0-15 take row 2k, lanes 16-31 row 2k + 1
+    const int gcol = (int)col0 + g * 16 + cc;
+    int cbs = 0, cx = 0, cy = 0, cz = 0;
+    if (rt.rows && gcol < nn) site_cell32(rt, gcol, cbs, cx, cy, cz);
+#pragma unroll 4
+    for (int k = 0; k < 16; ++k) {
+      const int rr = 2 * k + rsub;
+      const int grow = row0 + rr;
+      const int slot = stage_slot(rr, cc);
+      const float2 hl = tile[slot];
+      const int p0 = __shfl_sync(0xffffffffu, rpack0, rr);
+      const int p1 = __shfl_sync(0xffffffffu, rpack1, rr);
+      double a = 0.0;
+      if (grow < nn && gcol < nn) {
+        double* at = out + (int64_t)grow * n + gcol;
+        if (rt.rows) {
+          int dx = cx - (p0 & 0xffff), dy = cy - (p1 >> 16), dz = cz - (p1 & 0xffff);
+          if (dx < 0) dx += rt.s0;
+          if (dy < 0) dy += rt.s1;
+          if (dz < 0) dz += rt.s2;
+          const int o = ((dx * rt.s1 + dy) * rt.s2 + dz) * rt.nb + cbs;
+          const float2 t = __ldg(rt.rows + (int64_t)(p0 >> 16) * n + o);
+          if (gcol == grow) {
+            a = __dadd_rn(__dadd_rn((double)t.x, (double)t.y), diag_value);
+          } else {
+            // table + Fourier in FP32 pairs, then one conversion
+            float e1, e2;
+            const float w1 = two_sum(hl.x, t.x, e1);
+            const float w2 = two_sum(w1, __fadd_rn(__fadd_rn(hl.y, t.y), e1), e2);
+            a = pair_to_double(w2, e2);
+          }
+          *at = a;
+        } else {
+          a = gcol == grow ? diag_value : pair_to_double(hl.x, hl.y);
+          *at += a;
+        }
+      }
+      tiled[slot] = a;
+    }
+    __syncwarp();
+    if (mirror && row < n) {
+      // A[col][row]: lane = row, 32 consecutive doubles per column
+#pragma unroll 4
+      for (int q = 0; q < 16; ++q) {
+        const int mcol = (int)col0 + g * 16 + q;
+        if (mcol < nn) {
+          double* at = out + (int64_t)mcol * n + row;
+          const double a = tiled[stage_slot(lane, q)];
+          if (rt.rows) *at = a; else *at += a;
+        }
+      }
+    }
+    __syncwarp();
+  }
+}
+
 template <bool TF32>
 __global__ void __launch_bounds__(kThreads, 1)
     ewald_split_kernel(const __grid_constant__ CUtensorMap map_h,
@@ -621,12 +731,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         if (lane == 0 && c != n_chunks - 3) mbar_arrive(&acc_empty[b]);
       }
       if (!ok) break;
-      // last chunk: the Fourier part is s + x.  The diagonal is
-      // F_i . F_i = sum_k w_k (cos^2 + sin^2) = sum_k w_k exactly, taken
-      // from the FP64 weight sum.  With a real-space table the entry (and
-      // its mirror) is written once as table value + Fourier value, summed
-      // as FP32 pairs (relative error ~2^-47); otherwise it is added to the
-      // real and self terms already in the output.
+      // last chunk: the Fourier part is s + x
       const int b = chunk_acc(n_chunks - 1, n_chunks);
       if (!warp_wait(&acc_full[b], (uint32_t)seen[b] & 1u, abort_flag)) {
         if (lane == 0) *abort_flag = 1;
@@ -634,99 +739,9 @@ __global__ void __launch_bounds__(kThreads, 1)
       }
       ++seen[b];
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      const uint32_t t_x = lane_base + (uint32_t)(b * kCols);
-      const uint32_t t_s = lane_base + (uint32_t)((b ^ 1) * kCols);
-      // Each 16-column group goes through this warp's staging tile: s + x is
-      // formed with lane = row (the TMEM layout), the table value is added
-      // and the entry stored with 16 lanes along a row (contiguous table
-      // reads and row stores), and the mirror is stored with lane = row
-      // again (contiguous column stores).
-      const bool mirror = ti != tj;
-      const int nn = (int)n;
-      const int row0 = (int)(row - lane);       // first row of this warp
-      // this lane's row and, in the row-wise step, its column offset
-      int rpack0 = 0, rpack1 = 0;               // (basis, x) and (y, z) of row
-      if (rt.rows && row < n) {
-        int rb = 0, rx = 0, ry = 0, rz = 0;
-        site_cell32(rt, (int)row, rb, rx, ry, rz);
-        rpack0 = (rb << 16) | rx;
-        rpack1 = (ry << 16) | rz;
-      }
-      float2* tile = stage_tiles + warp * (kStageTileBytes / 8);
-      double* tiled = reinterpret_cast<double*>(tile);
-      const int cc = lane & 15, rsub = lane >> 4;
-#pragma unroll 1
-      for (int g = 0; g < kEpiCols / 16; ++g) {
-        uint32_t x[16], sv[16];
-        tmem_ld16_nowait(t_x + (uint32_t)(g * 16), x);
-        if (n_chunks >= 2) {
-          tmem_ld16_nowait(t_s + (uint32_t)(g * 16), sv);
-        } else {
-#pragma unroll
-          for (int q = 0; q < 16; ++q) sv[q] = 0u;
-        }
-        tmem_ld_wait();
-#pragma unroll
-        for (int q = 0; q < 16; ++q) {
-          float l;
-          const float h = two_sum(__uint_as_float(sv[q]), __uint_as_float(x[q]), l);
-          tile[stage_slot(lane, q)] = make_float2(h, l);
-        }
-        __syncwarp();
-        // row-wise: lanes 0-15 take row 2k, lanes 16-31 row 2k + 1
-        const int gcol = (int)col0 + g * 16 + cc;
-        int cbs = 0, cx = 0, cy = 0, cz = 0;
-        if (rt.rows && gcol < nn) site_cell32(rt, gcol, cbs, cx, cy, cz);
-#pragma unroll 4
-        for (int k = 0; k < 16; ++k) {
-          const int rr = 2 * k + rsub;
-          const int grow = row0 + rr;
-          const int slot = stage_slot(rr, cc);
-          const float2 hl = tile[slot];
-          const int p0 = __shfl_sync(0xffffffffu, rpack0, rr);
-          const int p1 = __shfl_sync(0xffffffffu, rpack1, rr);
-          double a = 0.0;
-          if (grow < nn && gcol < nn) {
-            double* at = out + (int64_t)grow * n + gcol;
-            if (rt.rows) {
-              int dx = cx - (p0 & 0xffff), dy = cy - (p1 >> 16), dz = cz - (p1 & 0xffff);
-              if (dx < 0) dx += rt.s0;
-              if (dy < 0) dy += rt.s1;
-              if (dz < 0) dz += rt.s2;
-              const int o = ((dx * rt.s1 + dy) * rt.s2 + dz) * rt.nb + cbs;
-              const float2 t = __ldg(rt.rows + (int64_t)(p0 >> 16) * n + o);
-              if (gcol == grow) {
-                a = __dadd_rn(__dadd_rn((double)t.x, (double)t.y), diag_value);
-              } else {
-                // table + Fourier in FP32 pairs, then one conversion
-                float e1, e2;
-                const float w1 = two_sum(hl.x, t.x, e1);
-                const float w2 = two_sum(w1, __fadd_rn(__fadd_rn(hl.y, t.y), e1), e2);
-                a = pair_to_double(w2, e2);
-              }
-              *at = a;
-            } else {
-              a = gcol == grow ? diag_value : pair_to_double(hl.x, hl.y);
-              *at += a;
-            }
-          }
-          tiled[slot] = a;
-        }
-        __syncwarp();
-        if (mirror && row < n) {
-          // A[col][row]: lane = row, 32 consecutive doubles per column
-#pragma unroll 4
-          for (int q = 0; q < 16; ++q) {
-            const int mcol = (int)col0 + g * 16 + q;
-            if (mcol < nn) {
-              double* at = out + (int64_t)mcol * n + row;
-              const double a = tiled[stage_slot(lane, q)];
-              if (rt.rows) *at = a; else *at += a;
-            }
-          }
-        }
-        __syncwarp();
-      }
+      write_unit(lane_base + (uint32_t)(b * kCols), lane_base + (uint32_t)((b ^ 1) * kCols),
+                 n_chunks, row, col0, ti != tj, n, out, rt, diag_value,
+                 stage_tiles + warp * (kStageTileBytes / 8));
       asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
       __syncwarp();
       if (lane == 0) mbar_arrive(unit_free);
@@ -741,6 +756,350 @@ __global__ void __launch_bounds__(kThreads, 1)
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   if (warp == kProducerWarp) {
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                 "r"(kTmemCols));
+  }
+}
+
+// ---------------------------------------------------------------------------
+// CTA-pair form (tcgen05 cta_group::2).  A cluster of two CTAs computes one
+// 256 x 256 super-tile per unit with MMAs of M = 256 (each CTA's TMEM holds
+// its 128 rows x 256 columns) and N = 256.  Each CTA loads its own 128 rows
+// of A and 128 of the 256 B rows (the pair's MMA reads B from both CTAs'
+// shared memory), so a 128-byte K slice costs 64 KB per SM for the same 12
+// MMAs per SM as the single-CTA form's 96 KB: 43 operand bytes per MMA
+// cycle instead of 64.
+//   - Each CTA's TMA loads signal its own full barrier; in the second CTA
+//     of the pair (rank 1) warp 9 passes each completed stage on to the
+//     first CTA's full barrier, which counts its own arrival plus that one.
+//     Every CTA can so wait for its own copies.
+//   - One thread of the first CTA issues the MMAs and commits them to the
+//     empty / acc_full barriers of both CTAs.
+//   - Both CTAs' epilogue warps release accumulators and units through the
+//     first CTA's acc_empty / unit_free barriers (16 arrivals each).
+//   - Units are taken statically: pair p takes super-tiles p, p + P, ... of
+//     the blocked order (all units cost the same).
+//   - A time-out in either CTA sets the abort flag of both.
+// ---------------------------------------------------------------------------
+constexpr int kPairStageBytes = 4 * kABytes;  // Ah, Al, and this CTA's Bh, Bl rows: 64 KB
+constexpr int kPairStages = 3;
+constexpr size_t kPairSmemBytes = (size_t)kPairStages * kPairStageBytes + kBarrierBytes +
+                                  kEpiWarps * kStageTileBytes + 1024;
+
+__host__ __device__ constexpr uint32_t idesc_pair(uint32_t ab_format) {
+  return (1u << 4) | (ab_format << 7) | (ab_format << 10) |
+         ((uint32_t)(kCols >> 3) << 17) | ((uint32_t)((2 * kRows) >> 4) << 24);
+}
+
+__device__ __forceinline__ uint32_t cluster_rank() {
+  uint32_t r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+__device__ __forceinline__ uint32_t cluster_index() {
+  uint32_t r;
+  asm volatile("mov.u32 %0, %%clusterid.x;" : "=r"(r));
+  return r;
+}
+__device__ __forceinline__ uint32_t cluster_count() {
+  uint32_t r;
+  asm volatile("mov.u32 %0, %%nclusterid.x;" : "=r"(r));
+  return r;
+}
+// address of this CTA's shared location `saddr` in CTA `rank` of the cluster
+__device__ __forceinline__ uint32_t map_rank(uint32_t saddr, uint32_t rank) {
+  uint32_t r;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(saddr), "r"(rank));
+  return r;
+}
+__device__ __forceinline__ void mbar_arrive_remote(uint32_t caddr) {
+  asm volatile("mbarrier.arrive.release.cluster.shared::cluster.b64 _, [%0];" ::"r"(caddr)
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait_cl(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// bounded wait with cluster-scope acquire (arrivals from the other CTA)
+__device__ __forceinline__ bool mbar_wait_cl(uint64_t* bar, uint32_t parity,
+                                             volatile int* abort_flag) {
+  for (uint32_t i = 0; i < kWaitLimit; ++i) {
+    if (mbar_try_wait_cl(bar, parity)) return true;
+    if ((i & 1023) == 1023 && *abort_flag) return false;
+  }
+  return false;
+}
+__device__ __forceinline__ bool warp_wait_cl(uint64_t* bar, uint32_t parity,
+                                            volatile int* abort_flag) {
+  bool got = false;
+  if ((threadIdx.x & 31) == 0) got = mbar_wait_cl(bar, parity, abort_flag);
+  return __shfl_sync(0xffffffffu, got, 0);
+}
+__device__ __forceinline__ void cluster_sync() {
+  asm volatile(
+      "barrier.cluster.arrive.release.aligned;\n\t"
+      "barrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void st_remote_u32(uint32_t caddr, uint32_t v) {
+  asm volatile("st.shared::cluster.u32 [%0], %1;" ::"r"(caddr), "r"(v) : "memory");
+}
+
+template <bool TF32>
+__device__ __forceinline__ void umma_pair(uint32_t d_tmem, uint64_t a, uint64_t b,
+                                          uint32_t acc) {
+  if (TF32) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::2.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+        "l"(a), "l"(b), "r"(idesc_pair(2)), "r"(acc));
+  } else {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::2.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+        "l"(a), "l"(b), "r"(idesc_pair(1)), "r"(acc));
+  }
+}
+// arrive on the barrier at this offset in both CTAs once the MMAs issued so
+// far have completed
+__device__ __forceinline__ void umma_commit_both(uint64_t* bar) {
+  asm volatile(
+      "tcgen05.commit.cta_group::2.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64"
+      " [%0], %1;" ::"r"(smem_u32(bar)),
+      "h"((uint16_t)3)
+      : "memory");
+}
+__device__ __forceinline__ void umma_commit_own(uint64_t* bar) {
+  asm volatile(
+      "tcgen05.commit.cta_group::2.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+          smem_u32(bar))
+      : "memory");
+}
+
+template <bool TF32>
+__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kThreads, 1)
+    ewald_split_pair_kernel(const __grid_constant__ CUtensorMap map_h,
+                            const __grid_constant__ CUtensorMap map_l, int64_t n,
+                            int k_blocks, int chunk_blocks, int nt,
+                            double* __restrict__ out, const double* __restrict__ diag_sum,
+                            RealTable rt, SplitErr err) {
+  const double diag_value = *diag_sum;
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  uint64_t* full = (uint64_t*)(smem + kPairStages * kPairStageBytes);
+  uint64_t* empty = full + kPairStages;
+  uint64_t* acc_full = empty + kPairStages;
+  uint64_t* acc_empty = acc_full + 2;
+  uint64_t* unit_free = acc_empty + 2;
+  uint64_t* drain = unit_free + 1;
+  volatile uint32_t* tmem_slot = (volatile uint32_t*)(drain + 1);
+  volatile int* abort_flag = (volatile int*)(tmem_slot + 1);
+  float2* stage_tiles = (float2*)(smem + kPairStages * kPairStageBytes + kBarrierBytes);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const uint32_t rank = cluster_rank();
+  const bool leader = rank == 0;
+  const int pair = (int)cluster_index(), n_pairs = (int)cluster_count();
+  const int n_chunks = (k_blocks + chunk_blocks - 1) / chunk_blocks;
+  const int n_tiles = nt * (nt + 1) / 2;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < kPairStages; ++s) {
+      mbar_init(&full[s], leader ? 2 : 1);
+      mbar_init(&empty[s], 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&acc_full[b], 1);
+      mbar_init(&acc_empty[b], 2 * kEpiWarps);
+    }
+    mbar_init(unit_free, 2 * kEpiWarps);
+    mbar_init(drain, 1);
+    *abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == kProducerWarp) {
+    asm volatile("tcgen05.alloc.cta_group::2.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32((const void*)tmem_slot)),
+                 "r"(kTmemCols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::2.sync.aligned;");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  cluster_sync();  // both CTAs' barriers are initialised before any remote use
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *tmem_slot;
+  // the first CTA's barriers and the other CTA's abort flag, cluster-wide
+  const uint32_t lead_full = map_rank(smem_u32(full), 0);
+  const uint32_t lead_acc_empty = map_rank(smem_u32(acc_empty), 0);
+  const uint32_t lead_unit_free = map_rank(smem_u32(unit_free), 0);
+  const uint32_t other_abort = map_rank(smem_u32((const void*)abort_flag), rank ^ 1u);
+  auto set_abort = [&]() {
+    *abort_flag = 1;
+    st_remote_u32(other_abort, 1u);
+  };
+
+  if (warp == kProducerWarp) {
+    // ---------------- TMA producer (both CTAs) ----------------
+    if (lane == 0) {
+      int last_kb[kPairStages];
+      for (int s = 0; s < kPairStages; ++s) last_kb[s] = -1;
+      int gkb = 0;
+      bool ok = true;
+      for (int t = pair; t < n_tiles && ok; t += n_pairs) {
+        int ti = 0, tj = 0;
+        super_tile(t, nt, ti, tj);
+        const int row_a = ti * kCols + (int)rank * kRows;
+        const int row_b = tj * kCols + (int)rank * kRows;
+        for (int kb = 0; kb < k_blocks; ++kb, ++gkb) {
+          const int s = gkb % kPairStages;
+          const uint32_t ph = (uint32_t)(gkb / kPairStages) & 1u;
+          if (!mbar_wait_cl(&empty[s], ph ^ 1u, abort_flag)) { set_abort(); ok = false; break; }
+          if (*abort_flag) { ok = false; break; }
+          uint8_t* st = smem + s * kPairStageBytes;
+          mbar_arrive_expect_tx(&full[s], kPairStageBytes);
+          const int x = kb * (TF32 ? kSlice / 4 : kSlice / 2);
+          // rows at or past n are read as zeros
+          tma_load_2d(st, &map_h, &full[s], x, row_a);
+          tma_load_2d(st + kABytes, &map_l, &full[s], x, row_a);
+          tma_load_2d(st + 2 * kABytes, &map_h, &full[s], x, row_b);
+          tma_load_2d(st + 3 * kABytes, &map_l, &full[s], x, row_b);
+          last_kb[s] = gkb;
+        }
+      }
+      // this CTA's copies have landed before it moves on (in the first CTA
+      // the barrier also waits for the other CTA's hand-over)
+      for (int s = 0; s < kPairStages; ++s)
+        if (last_kb[s] >= 0 &&
+            !mbar_wait_drain(&full[s], (uint32_t)(last_kb[s] / kPairStages) & 1u))
+          set_abort();
+    }
+  } else if (warp == kMmaWarp && !leader) {
+    // ---------------- hand-over of loaded stages (second CTA) ----------------
+    if (lane == 0) {
+      int gkb = 0;
+      bool ok = true;
+      for (int t = pair; t < n_tiles && ok; t += n_pairs) {
+        for (int kb = 0; kb < k_blocks; ++kb, ++gkb) {
+          const int s = gkb % kPairStages;
+          if (!mbar_wait(&full[s], (uint32_t)(gkb / kPairStages) & 1u, abort_flag)) {
+            set_abort(); ok = false; break;
+          }
+          mbar_arrive_remote(lead_full + (uint32_t)(s * 8));
+        }
+      }
+    }
+  } else if (warp == kMmaWarp) {
+    // ---------------- MMA issuer (first CTA) ----------------
+    if (lane == 0) {
+      const int ksteps = kSlice / 32;
+      int gkb = 0, ui = 0;
+      int waits[2] = {0, 0};
+      bool ok = true;
+      for (int t = pair; t < n_tiles && ok; t += n_pairs, ++ui) {
+        // both accumulators free in both CTAs: the previous unit is written
+        if (ui > 0 && !mbar_wait_cl(unit_free, (uint32_t)(ui - 1) & 1u, abort_flag)) {
+          set_abort();
+          break;
+        }
+        int kb = 0;
+        for (int c = 0; c < n_chunks; ++c) {
+          const int b = chunk_acc(c, n_chunks);
+          const bool fresh = chunk_fresh(c, n_chunks);
+          if (!fresh) {
+            if (!mbar_wait_cl(&acc_empty[b], (uint32_t)waits[b] & 1u, abort_flag)) {
+              set_abort(); ok = false; break;
+            }
+            ++waits[b];
+          }
+          asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+          const uint32_t d = tmem + (uint32_t)(b * kCols);
+          const int kb_end = min(k_blocks, (c + 1) * chunk_blocks);
+          for (int first = 1; kb < kb_end; ++kb, ++gkb, first = 0) {
+            const int s = gkb % kPairStages;
+            const uint32_t ph = (uint32_t)(gkb / kPairStages) & 1u;
+            if (!mbar_wait_cl(&full[s], ph, abort_flag)) { set_abort(); ok = false; break; }
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const uint32_t sa = smem_u32(smem + s * kPairStageBytes);
+            const uint64_t ah = sdesc(sa), al = sdesc(sa + kABytes);
+            const uint64_t bh = sdesc(sa + 2 * kABytes), bl = sdesc(sa + 3 * kABytes);
+            for (int k = 0; k < ksteps; ++k) {
+              const uint64_t o = (uint64_t)(k * 2);  // +32 bytes in the >>4 field
+              const uint32_t acc0 = (fresh && first && k == 0) ? 0u : 1u;
+              umma_pair<TF32>(d, ah + o, bh + o, acc0);
+              umma_pair<TF32>(d, ah + o, bl + o, 1u);
+              umma_pair<TF32>(d, al + o, bh + o, 1u);
+            }
+            umma_commit_both(&empty[s]);  // both CTAs' stage s free after these
+          }
+          if (!ok) break;
+          umma_commit_both(&acc_full[b]);  // chunk finished in both CTAs
+        }
+      }
+      umma_commit_own(drain);
+      if (!mbar_wait_drain(drain, 0u)) set_abort();
+    }
+  } else if (warp < kEpiWarps) {
+    // ---------------- epilogue (warps 0-7 of both CTAs) ----------------
+    const int quad = warp & 3, half = warp >> 2;
+    const uint32_t lane_base =
+        tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(half * kEpiCols);
+    float s[kEpiCols];
+    int seen[2] = {0, 0};
+    bool ok = true;
+    for (int t = pair; t < n_tiles && ok; t += n_pairs) {
+      int ti = 0, tj = 0;
+      super_tile(t, nt, ti, tj);
+      const int64_t row = (int64_t)ti * kCols + (int64_t)rank * kRows + quad * 32 + lane;
+      const int64_t col0 = (int64_t)tj * kCols + half * kEpiCols;
+#pragma unroll
+      for (int q = 0; q < kEpiCols; ++q) s[q] = 0.f;
+      for (int c = 0; c < n_chunks - 1; ++c) {
+        const int b = chunk_acc(c, n_chunks);
+        if (!warp_wait_cl(&acc_full[b], (uint32_t)seen[b] & 1u, abort_flag)) {
+          if (lane == 0) set_abort();
+          ok = false;
+          break;
+        }
+        ++seen[b];
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const bool last_fold = c == n_chunks - 2;
+        fold_chunk(lane_base + (uint32_t)(b * kCols), lane_base + (uint32_t)((b ^ 1) * kCols),
+                   last_fold && n_chunks >= 3, last_fold, s);
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+        __syncwarp();
+        if (lane == 0 && c != n_chunks - 3) mbar_arrive_remote(lead_acc_empty + (uint32_t)(b * 8));
+      }
+      if (!ok) break;
+      const int b = chunk_acc(n_chunks - 1, n_chunks);
+      if (!warp_wait_cl(&acc_full[b], (uint32_t)seen[b] & 1u, abort_flag)) {
+        if (lane == 0) set_abort();
+        break;
+      }
+      ++seen[b];
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      write_unit(lane_base + (uint32_t)(b * kCols), lane_base + (uint32_t)((b ^ 1) * kCols),
+                 n_chunks, row, col0, ti != tj, n, out, rt, diag_value,
+                 stage_tiles + warp * (kStageTileBytes / 8));
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      __syncwarp();
+      if (lane == 0) mbar_arrive_remote(lead_unit_free);
+    }
+  }
+
+  // ---------------- teardown ----------------
+  __syncthreads();
+  if (threadIdx.x == 0 && *abort_flag) atomicExch(err.flag, 1);
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  cluster_sync();  // no MMA of the pair touches either CTA's memory after this
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  if (warp == kProducerWarp) {
+    asm volatile("tcgen05.dealloc.cta_group::2.sync.aligned.b32 %0, %1;" ::"r"(tmem),
                  "r"(kTmemCols));
   }
 }
@@ -1013,21 +1372,53 @@ int ewald_build_split(const PycdEwaldDesc* d, int mode, double* out,
   // super-tiles is two units, taken by one persistent CTA per SM
   const int nt = (int)((n + kCols - 1) / kCols);
   const int n_units = nt * (nt + 1);
-  int dev = 0, sms = 0;
-  PYCD_CUDA(cudaGetDevice(&dev));
-  PYCD_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-  const unsigned ctas = (unsigned)(n_units < sms ? n_units : sms);
   SplitErr err{flag, next};
-  if (tf32) {
-    PYCD_CUDA(cudaFuncSetAttribute(ewald_split_kernel<true>,
-                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    ewald_split_kernel<true><<<ctas, kThreads, smem, s>>>(
-        mh, ml, n, k_blocks, chunk_blocks, nt, out, diag_sum, rt, err);
+  // CTA-pair form when 2-CTA clusters of this size can be co-resident
+  const int n_tiles = nt * (nt + 1) / 2;
+  const void* pair_fn = tf32 ? (const void*)ewald_split_pair_kernel<true>
+                             : (const void*)ewald_split_pair_kernel<false>;
+  PYCD_CUDA(cudaFuncSetAttribute(pair_fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)kPairSmemBytes));
+  int pairs = 0;
+  {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(2 * (unsigned)n_tiles);
+    cfg.blockDim = dim3(kThreads);
+    cfg.dynamicSmemBytes = kPairSmemBytes;
+    cfg.stream = s;
+    if (cudaOccupancyMaxActiveClusters(&pairs, pair_fn, &cfg) != cudaSuccess) {
+      (void)cudaGetLastError();
+      pairs = 0;
+    }
+  }
+  // PYCD_SPLIT_FORM=single: the single-CTA form (same results), e.g. where
+  // clusters are restricted
+  const char* form = getenv("PYCD_SPLIT_FORM");
+  if (form && strcmp(form, "single") == 0) pairs = 0;
+  if (pairs > 0) {
+    const unsigned grid = 2u * (unsigned)(pairs < n_tiles ? pairs : n_tiles);
+    if (tf32)
+      ewald_split_pair_kernel<true><<<grid, kThreads, kPairSmemBytes, s>>>(
+          mh, ml, n, k_blocks, chunk_blocks, nt, out, diag_sum, rt, err);
+    else
+      ewald_split_pair_kernel<false><<<grid, kThreads, kPairSmemBytes, s>>>(
+          mh, ml, n, k_blocks, chunk_blocks, nt, out, diag_sum, rt, err);
   } else {
-    PYCD_CUDA(cudaFuncSetAttribute(ewald_split_kernel<false>,
-                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    ewald_split_kernel<false><<<ctas, kThreads, smem, s>>>(
-        mh, ml, n, k_blocks, chunk_blocks, nt, out, diag_sum, rt, err);
+    int dev = 0, sms = 0;
+    PYCD_CUDA(cudaGetDevice(&dev));
+    PYCD_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    const unsigned ctas = (unsigned)(n_units < sms ? n_units : sms);
+    if (tf32) {
+      PYCD_CUDA(cudaFuncSetAttribute(ewald_split_kernel<true>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      ewald_split_kernel<true><<<ctas, kThreads, smem, s>>>(
+          mh, ml, n, k_blocks, chunk_blocks, nt, out, diag_sum, rt, err);
+    } else {
+      PYCD_CUDA(cudaFuncSetAttribute(ewald_split_kernel<false>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      ewald_split_kernel<false><<<ctas, kThreads, smem, s>>>(
+          mh, ml, n, k_blocks, chunk_blocks, nt, out, diag_sum, rt, err);
+    }
   }
   PYCD_CUDA(cudaGetLastError());
   int h_flag = 0;

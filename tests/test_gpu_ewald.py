@@ -183,3 +183,19 @@ def test_split_real_space_table_equals_pair_pass(cuda_ready, monkeypatch, precis
     A_pairs = sysm.get_precomputed_array_device(precision).cpu().numpy()
     assert np.isfinite(A_table).all()
     assert np.abs(A_table - A_pairs).max() < 1e-12 * K.EV2HARTREE
+
+
+@pytest.mark.parametrize("precision", ["bf16x3", "tf32x3"])
+def test_split_pair_form_equals_single_cta_form(cuda_ready, monkeypatch, precision):
+    """The CTA-pair contraction (tcgen05 cta_group::2: 256-row MMAs, each CTA
+    loading half of the B rows) and the single-CTA form it falls back to
+    (PYCD_SPLIT_FORM=single) give the same array: 1,200 sites, five
+    super-tile rows, the last one partly outside the matrix."""
+    sysm = wl.corundum((10, 10, 1), neighbor_list=False)
+    A_pair = sysm.get_precomputed_array_device(precision).cpu().numpy()
+    monkeypatch.setenv("PYCD_SPLIT_FORM", "single")
+    A_single = sysm.get_precomputed_array_device(precision).cpu().numpy()
+    assert np.isfinite(A_pair).all()
+    assert np.abs(A_pair - A_single).max() < 1e-12 * K.EV2HARTREE
+    ref = sysm.get_precomputed_array_device("fp64").cpu().numpy()
+    assert np.abs(A_pair - ref).max() < SPLIT_TOL_HA
