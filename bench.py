@@ -39,14 +39,17 @@ T_FINAL, DT = 1e30, 1e27  # time grid wide enough that no trajectory ends by tim
 SEED = 20251203
 # queue form of the warp-form launch: rounds of this many steps (0 = static)
 SCHED_STEPS = 0
-# FP64 thread instructions per KMC step of kmc_advance_kernel<8, 2, 1> on this
-# workload (ncu: smsp__sass_thread_inst_executed_op_{dadd,dfma,dmul}_pred_on
-# summed, divided by the launch's KMC steps)
-FP64_INSTR_PER_STEP = 424
-# DRAM bytes per KMC step of the same kernel (ncu: dram__bytes_read.sum +
-# dram__bytes_write.sum of one 10,000-step chunk launch of this workload,
-# 7,648,000 + 0 bytes, divided by its 4.096e7 KMC steps)
-DRAM_BYTES_PER_STEP = 7648000 / 40960000
+# FP64 thread instructions per KMC step on this workload, by launch shape
+# (lanes per trajectory, register variant): ncu
+# smsp__sass_thread_inst_executed_op_{dadd,dfma,dmul}_pred_on summed over one
+# 1,000-step chunk launch, divided by its 4.096e6 KMC steps.  The autotuner
+# picks (16, 2), i.e. kmc_advance_kernel<16, 1, 2>; with 8 lanes the step's
+# shared FP64 work is repeated on fewer lanes.
+FP64_INSTR_PER_STEP = {(16, 2): 428, (8, 1): 280}
+# DRAM bytes per KMC step of kmc_advance_kernel<16, 1, 2> (ncu:
+# dram__bytes_read.sum + dram__bytes_write.sum of one 10,000-step chunk launch
+# of this workload, 7,420,928 + 3,072 bytes, divided by its 4.096e7 KMC steps)
+DRAM_BYTES_PER_STEP = (7420928 + 3072) / 40960000
 
 
 def peaks():
@@ -1035,7 +1038,10 @@ def main():
     # measured DGEMM flop rate (2 flops per DFMA slot).
     fp64_tf = fp64_peak_tflops()
     fp64_peak_instr = fp64_tf * 1e12 / 2.0
-    fp64_achieved = FP64_INSTR_PER_STEP * steps_per_launch / (launch_ms / 1e3)
+    fp64_per_step = FP64_INSTR_PER_STEP.get(
+        (tuned["lanes_per_traj"], tuned["min_blocks_per_sm"]))
+    fp64_achieved = (fp64_per_step * steps_per_launch / (launch_ms / 1e3)
+                     if fp64_per_step else None)
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_baseline_1core(system, run, dopants, occ)
@@ -1072,10 +1078,11 @@ def main():
                          "peak_kind": peak_kind,
                          "bytes_per_step": B_STEP, "launch_ms": launch_ms,
                          "fp64_issue": {
-                             "instr_per_step": FP64_INSTR_PER_STEP,
+                             "instr_per_step": fp64_per_step,
                              "achieved": fp64_achieved, "peak": fp64_peak_instr,
                              "unit": "FP64 thread instr/s",
-                             "frac": fp64_achieved / fp64_peak_instr,
+                             "frac": (fp64_achieved / fp64_peak_instr
+                                      if fp64_achieved else None),
                              "peak_kind": "measured: cuBLAS DGEMM 4096^3 this run, "
                                           f"{fp64_tf:.3f} TFLOP/s / 2 flops per DFMA"}},
             "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": args.steps,
