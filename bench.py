@@ -711,12 +711,17 @@ def msd_bench(args):
 
 
 def plain_bench(args):
+    """The plain configuration as its own JSON line (plain_record)."""
+    print(json.dumps(plain_record()), flush=True)
+
+
+def plain_record():
     """The plain, CPU-runnable configuration: corundum 3x3x3 = 324 sites, one
     electron on site default_rng(0).integers(324), FP64 Ewald array, 1e5 steps
     with injected uniforms default_rng(0).random(2e5) (time grid 1e-9 s up to
-    1e-6 s).  One JSON line: the plain GPU form's steps/s, the FP64 array
-    build, and the NumPy port of the reference loop on this host's cores over
-    the same 1e5 steps, with the event streams compared step by step."""
+    1e-6 s).  The plain GPU form's steps/s, the FP64 array build, and the
+    NumPy port of the reference loop on one host core over the same 1e5
+    steps, with the event streams compared step by step."""
     import torch
     from oracle import ewald_oracle as eo
     from oracle import kmc_oracle as ko
@@ -769,7 +774,7 @@ def plain_bench(args):
     same_events = bool(np.array_equal(o["proc"], proc[:len(o["proc"])]))
     t_rel = float(np.abs(o["time"][1:len(times) + 1] / times[:len(o["time"]) - 1] - 1).max())
     flops = 4.0 * n * n * (system.last_build_info["n_kvec"])
-    print(json.dumps({
+    return {
         "workload": "plain", "metric": "KMC steps/s (plain form, one trajectory)",
         "value": n_steps / best, "unit": "steps/s", "steps": n_steps, "dtype": "f64",
         "data": "synthetic",
@@ -783,7 +788,7 @@ def plain_bench(args):
         "time_max_rel_diff": t_rel, "gpu_steps_recorded": steps,
         "cpu_baseline": {"value": o["steps"] / cpu_s, "unit": "steps/s", "cores": 1,
                          "kind": "port", "sample": "the same 1e5 steps, NumPy port of the "
-                         "reference loop"}}), flush=True)
+                         "reference loop"}}
 
 
 OUTPUT_DATA = {"unwrapped_traj": {"file_name": "unwrapped_traj.npy", "write": 1,
@@ -912,6 +917,8 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-serving", action="store_true",
                     help="leave the serving record out of the default line")
+    ap.add_argument("--no-plain", action="store_true",
+                    help="leave the plain configuration's record out of the default line")
     ap.add_argument("--no-ewald", action="store_true",
                     help="leave the split-precision build record out of the default line")
     ap.add_argument("--lanes", type=int, default=0)
@@ -1046,6 +1053,8 @@ def main():
     if rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_baseline_1core(system, run, dopants, occ)
     extra = {}
+    if rank == 0 and not args.no_plain:
+        extra["plain_config"] = plain_record()
     if rank == 0 and not args.no_ewald:
         n, kk = 8192, 4096
         extra["ewald_split"] = ewald_split_record(n, kk, EWALD_SIZES[n][1][0], cpu=False)
