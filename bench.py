@@ -313,6 +313,7 @@ def ewald_split_record(n, kk, kc, modes=("fp64", "bf16x3", "tf32x3"), cpu=True):
     error of the hop energy dE0 over sampled 16-carrier, 16-dopant
     configurations as a fraction of kT (300 K)."""
     import torch
+    from pycd_gb300 import autotune
     from pycd_gb300 import constants as K
     from pycd_gb300 import ewald as ew
     from pycd_gb300 import workloads as wl
@@ -328,6 +329,10 @@ def ewald_split_record(n, kk, kc, modes=("fp64", "bf16x3", "tf32x3"), cpu=True):
     ref = None
     for mode in modes:
         reps = 1 if mode == "fp64" else 3
+        if mode != "fp64":
+            # launch shape of the tcgen05 contraction (untimed; same array)
+            tuned = autotune.tune_split(system, mode, reps=1)
+            times.setdefault("launch_shapes", {})[mode] = tuned["best"]
         system.get_precomputed_array_device(mode)  # warm-up / workspace
         torch.cuda.synchronize()
         best = None
@@ -353,6 +358,7 @@ def ewald_split_record(n, kk, kc, modes=("fp64", "bf16x3", "tf32x3"), cpu=True):
             times[mode]["dE_rms_err_over_kT"] = de_rms / kT
         if mode != "fp64":
             del A
+    line["split_launch"] = times.pop("launch_shapes", {})
     kn = line["n_kvec"]
     flops = 4.0 * n * n * kn  # N x 2K by 2K x N
     for mode in modes:

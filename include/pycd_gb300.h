@@ -42,7 +42,7 @@
 extern "C" {
 #endif
 
-#define PYCD_ABI_VERSION 3
+#define PYCD_ABI_VERSION 4
 
 #if defined(__GNUC__)
 #define PYCD_API __attribute__((visibility("default")))
@@ -106,8 +106,7 @@ typedef enum PycdEwaldMode {
    * three products (hi.hi + hi.lo + lo.hi), FP32 accumulation in TMEM per
    * K-chunk, error-free sum across chunks.  Runs on CTA pairs (2-CTA
    * clusters, 256-row MMAs) where the device can place them, else on
-   * single CTAs; the environment variable PYCD_SPLIT_FORM=single forces
-   * the single-CTA form (same results).                                    */
+   * single CTAs (PycdEwaldDesc.split_form; same results).                  */
   PYCD_EWALD_BF16X3 = 2,
   /* As BF16X3 with TF32 operands (hi + lo split, three products).         */
   PYCD_EWALD_TF32X3 = 3
@@ -141,6 +140,14 @@ typedef struct PycdEwaldDesc {
    * terms of all rows from the first basis_sites rows.                    */
   int32_t supercell[3];
   int32_t basis_sites;
+  /* Launch shape of the split modes; 0 = the library's default.  The array
+   * does not depend on it (pycd_gb300/autotune.py picks it by timing).
+   * split_form: 1 = CTA pairs (2-CTA clusters, 256-row MMAs; single CTAs
+   * where the device cannot place the clusters), 2 = single CTAs.
+   * split_raster: super-tiles per side of the blocked tile order, 1-64
+   * (default 8).  No counterpart in the reference.                         */
+  int32_t split_form;
+  int32_t split_raster;
 } PycdEwaldDesc;
 
 #define PYCD_EWALD_PART_REAL 1     /* erfc(sqrt(alpha) r)/(2 r eps), r < r_cut */

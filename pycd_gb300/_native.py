@@ -21,7 +21,7 @@ ERR_WORKSPACE = -6
 
 # trajectory status (PycdTrajStatus)
 # ABI version of include/pycd_gb300.h that these ctypes structs mirror
-ABI_VERSION = 3
+ABI_VERSION = 4
 
 TRAJ_RUNNING = 0
 TRAJ_DONE = 1
@@ -57,7 +57,12 @@ class EwaldDesc(C.Structure):
                 ("pbc", C.c_int32 * 3), ("alpha", C.c_double),
                 ("r_cut", C.c_double), ("volume", C.c_double),
                 ("dielectric", C.c_double), ("parts", C.c_int32),
-                ("supercell", C.c_int32 * 3), ("basis_sites", C.c_int32)]
+                ("supercell", C.c_int32 * 3), ("basis_sites", C.c_int32),
+                ("split_form", C.c_int32), ("split_raster", C.c_int32)]
+
+
+# PycdEwaldDesc.split_form
+SPLIT_FORMS = {"auto": 0, "pair": 1, "single": 2}
 
 
 EWALD_PART_REAL = 1

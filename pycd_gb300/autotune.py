@@ -1,4 +1,5 @@
-"""Launch-shape autotuner for the KMC kernel.
+"""Launch-shape autotuners: the KMC kernel (``tune``) and the tcgen05
+split-precision Ewald contraction (``tune_split``).
 
 The kernel's event streams do not depend on its launch shape (cumulative
 rates are fixed balanced-tree sums over the process index), so the shape is
@@ -90,4 +91,57 @@ def tune(engine, batch, rng, probe_steps=200, reps=2, stream=None):
     best = min(table, key=lambda x: x[1])[0]
     _apply(engine, best)
     _CACHE[key] = best
+    return {"best": best, "table": table, "cached": False}
+
+
+# ---------------------------------------------------------------------------
+# Split-precision Ewald build
+# ---------------------------------------------------------------------------
+_SPLIT_CACHE = {}
+
+# (form, raster): CTA pairs or single CTAs, super-tiles per raster block side
+SPLIT_CANDIDATES = (("pair", 4), ("pair", 8), ("pair", 16), ("single", 8))
+
+
+def split_cache_key(system, precision):
+    """(precision, site-count bucket, k-count bucket): factors of two of N and
+    of the k list length, which set the tile count and the operand panels'
+    length, so the L2 reuse the raster order buys."""
+    n = int(system.neighbors.num_system_elements)
+    info = getattr(system, "last_build_info", None) or {}
+    k = int(info.get("n_kvec", 0))
+    return (precision, int(np.log2(max(1, n))), int(np.log2(max(1, k))))
+
+
+def tune_split(system, precision="bf16x3", reps=2, candidates=SPLIT_CANDIDATES):
+    """Pick the fastest launch shape of the split-precision build of
+    ``system`` by timing each candidate's whole build (the array does not
+    depend on the shape), set it as ``system.split_launch`` and return
+    ``{"best": shape, "table": [(shape, ms), ...]}``.  Cached in-process per
+    ``split_cache_key``."""
+    import torch
+    system.get_precomputed_array_device(precision)  # k count for the key; loads kernels
+    key = split_cache_key(system, precision)
+    if key in _SPLIT_CACHE:
+        system.split_launch = dict(_SPLIT_CACHE[key])
+        return {"best": system.split_launch, "table": [], "cached": True}
+    table = []
+    for form, raster in candidates:
+        system.split_launch = {"form": form, "raster": raster}
+        times = []
+        for r in range(reps + 1):
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record()
+            A = system.get_precomputed_array_device(precision)
+            e1.record()
+            e1.synchronize()
+            del A
+            if r:
+                times.append(e0.elapsed_time(e1))
+        table.append(({"form": form, "raster": raster}, float(np.median(times))))
+    best = min(table, key=lambda x: x[1])[0]
+    system.split_launch = dict(best)
+    _SPLIT_CACHE[key] = dict(best)
     return {"best": best, "table": table, "cached": False}

@@ -81,6 +81,9 @@ class System(EwaldParameterSearch):
         self.system_size = self.neighbors.system_size
         self.num_cells = self.system_size.prod()
         self.pairwise_min_image_vector_data = pairwise_min_image_vector_data
+        # launch shape of the split-precision builds (None: the library's
+        # default; autotune.tune_split sets a timed choice)
+        self.split_launch = None
         # Ewald cell: np.multiply(system_size, lattice) scales COLUMNS
         # (core.py:709-710); it equals the supercell only when s_i = s_j
         # wherever lattice[i][j] != 0.  Kept as the reference has it.
@@ -149,7 +152,8 @@ class System(EwaldParameterSearch):
         from .ewald import build_device_array
         alpha, r_cut, k_cut, _ = self._ewald_parameters()
         A, info = build_device_array(self, alpha, r_cut, k_cut, precision,
-                                     pmiv, stream)
+                                     pmiv, stream,
+                                     split_launch=self.split_launch)
         self.last_build_info = info
         return A
 

@@ -483,6 +483,10 @@ int ewald_validate(const PycdEwaldDesc* d, int mode) {
     PYCD_REQUIRE(d->d_cart != nullptr, "feature modes need d_cart");
   PYCD_REQUIRE(d->n_sites <= 65535, "n_sites above 65535 is not supported");
   PYCD_REQUIRE(d->basis_sites >= 0, "basis_sites must be >= 0");
+  PYCD_REQUIRE(d->split_form >= 0 && d->split_form <= 2,
+               "split_form must be 0 (default), 1 (CTA pairs) or 2 (single CTAs)");
+  PYCD_REQUIRE(d->split_raster >= 0 && d->split_raster <= 64,
+               "split_raster must be 0 (default) or 1-64");
   if (d->basis_sites > 0) {
     PYCD_REQUIRE(d->supercell[0] > 0 && d->supercell[1] > 0 && d->supercell[2] > 0 &&
                      (int64_t)d->basis_sites * d->supercell[0] * d->supercell[1] *

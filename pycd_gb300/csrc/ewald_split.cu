@@ -19,8 +19,8 @@
 // by the half that owns its row.
 //
 // Schedule.  One persistent CTA per SM takes units from a global counter in
-// a blocked order (kRaster x kRaster super-tiles at a time, the block rows
-// of the upper triangle in turn).  The units in flight at one time then
+// a blocked order (raster x raster super-tiles at a time, the block rows
+// of the upper triangle in turn; raster from PycdEwaldDesc.split_raster).  The units in flight at one time then
 // share few operand panels and advance along K together, so each K slice
 // of a panel is read from DRAM about once and reused from L2.  Tensor
 // memory stays allocated from unit to unit and the barrier phases carry
@@ -63,8 +63,6 @@
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
-#include <stdlib.h>
-#include <string.h>
 
 #include "common.cuh"
 
@@ -87,7 +85,7 @@ constexpr int kEpiWarps = 8;
 constexpr int kThreads = 32 * (kEpiWarps + 2);
 constexpr int kProducerWarp = kEpiWarps, kMmaWarp = kEpiWarps + 1;
 constexpr uint32_t kWaitLimit = 1u << 24;   // bounded try_wait iterations
-constexpr int kRaster = 8;                  // super-tiles per raster block side
+constexpr int kRasterDefault = 8;           // super-tiles per raster block side
 // Final-phase staging: per epilogue warp a 32 x 16 tile of 8-byte values
 // (4 KB), XOR-swizzled so that row-wise and column-wise accesses are free
 // of bank conflicts; placed after the barrier block.
@@ -97,11 +95,11 @@ constexpr size_t kSmemBytes =
     (size_t)kStages * kStageBytes + kBarrierBytes + kEpiWarps * kStageTileBytes + 1024;
 
 // (row ti, column tj) of super-tile t in the blocked order: block rows of
-// kRaster super-tile rows in turn; within one, the diagonal block's upper
+// `raster` super-tile rows in turn; within one, the diagonal block's upper
 // triangle (row-major), then the blocks to its right (row-major inside each)
-__device__ __forceinline__ bool super_tile(int t, int nt, int& ti, int& tj) {
-  for (int r0 = 0; r0 < nt; r0 += kRaster) {
-    const int h = min(kRaster, nt - r0);
+__device__ __forceinline__ bool super_tile(int t, int nt, int raster, int& ti, int& tj) {
+  for (int r0 = 0; r0 < nt; r0 += raster) {
+    const int h = min(raster, nt - r0);
     const int nd = h * (h + 1) / 2;
     if (t < nd) {
       int r = 0;
@@ -111,8 +109,8 @@ __device__ __forceinline__ bool super_tile(int t, int nt, int& ti, int& tj) {
       return true;
     }
     t -= nd;
-    for (int c0 = r0 + h; c0 < nt; c0 += kRaster) {
-      const int w = min(kRaster, nt - c0);
+    for (int c0 = r0 + h; c0 < nt; c0 += raster) {
+      const int w = min(raster, nt - c0);
       if (t < h * w) {
         ti = r0 + t / w;
         tj = c0 + t % w;
@@ -515,8 +513,9 @@ template <bool TF32>
 __global__ void __launch_bounds__(kThreads, 1)
     ewald_split_kernel(const __grid_constant__ CUtensorMap map_h,
                        const __grid_constant__ CUtensorMap map_l, int64_t n,
-                       int k_blocks, int chunk_blocks, int nt, double* __restrict__ out,
-                       const double* __restrict__ diag_sum, RealTable rt, SplitErr err) {
+                       int k_blocks, int chunk_blocks, int nt, int raster,
+                       double* __restrict__ out, const double* __restrict__ diag_sum,
+                       RealTable rt, SplitErr err) {
   const double diag_value = *diag_sum;
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
@@ -578,7 +577,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         for (;;) {
           const int t = atomicAdd(err.next, 1);
           if (t >= n_units) break;
-          if (super_tile(t >> 1, nt, ti, tj) &&
+          if (super_tile(t >> 1, nt, raster, ti, tj) &&
               (int64_t)ti * kCols + (int64_t)(t & 1) * kRows < n) {
             u = t;
             break;
@@ -705,7 +704,7 @@ __global__ void __launch_bounds__(kThreads, 1)
       u = __shfl_sync(0xffffffffu, u, 0);
       if (!got || u < 0) break;
       int ti = 0, tj = 0;
-      super_tile(u >> 1, nt, ti, tj);
+      super_tile(u >> 1, nt, raster, ti, tj);
       const int64_t row = (int64_t)ti * kCols + (u & 1) * kRows + quad * 32 + lane;
       const int64_t col0 = (int64_t)tj * kCols + half * kEpiCols;
 #pragma unroll
@@ -885,7 +884,7 @@ template <bool TF32>
 __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kThreads, 1)
     ewald_split_pair_kernel(const __grid_constant__ CUtensorMap map_h,
                             const __grid_constant__ CUtensorMap map_l, int64_t n,
-                            int k_blocks, int chunk_blocks, int nt,
+                            int k_blocks, int chunk_blocks, int nt, int raster,
                             double* __restrict__ out, const double* __restrict__ diag_sum,
                             RealTable rt, SplitErr err) {
   const double diag_value = *diag_sum;
@@ -952,7 +951,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kThreads, 1)
       bool ok = true;
       for (int t = pair; t < n_tiles && ok; t += n_pairs) {
         int ti = 0, tj = 0;
-        super_tile(t, nt, ti, tj);
+        super_tile(t, nt, raster, ti, tj);
         const int row_a = ti * kCols + (int)rank * kRows;
         const int row_b = tj * kCols + (int)rank * kRows;
         for (int kb = 0; kb < k_blocks; ++kb, ++gkb) {
@@ -1053,7 +1052,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kThreads, 1)
     bool ok = true;
     for (int t = pair; t < n_tiles && ok; t += n_pairs) {
       int ti = 0, tj = 0;
-      super_tile(t, nt, ti, tj);
+      super_tile(t, nt, raster, ti, tj);
       const int64_t row = (int64_t)ti * kCols + (int64_t)rank * kRows + quad * 32 + lane;
       const int64_t col0 = (int64_t)tj * kCols + half * kEpiCols;
 #pragma unroll
@@ -1373,6 +1372,7 @@ int ewald_build_split(const PycdEwaldDesc* d, int mode, double* out,
   const int nt = (int)((n + kCols - 1) / kCols);
   const int n_units = nt * (nt + 1);
   SplitErr err{flag, next};
+  const int raster = d->split_raster > 0 ? d->split_raster : kRasterDefault;
   // CTA-pair form when 2-CTA clusters of this size can be co-resident
   const int n_tiles = nt * (nt + 1) / 2;
   const void* pair_fn = tf32 ? (const void*)ewald_split_pair_kernel<true>
@@ -1391,18 +1391,15 @@ int ewald_build_split(const PycdEwaldDesc* d, int mode, double* out,
       pairs = 0;
     }
   }
-  // PYCD_SPLIT_FORM=single: the single-CTA form (same results), e.g. where
-  // clusters are restricted
-  const char* form = getenv("PYCD_SPLIT_FORM");
-  if (form && strcmp(form, "single") == 0) pairs = 0;
+  if (d->split_form == 2) pairs = 0;  // single CTAs asked for
   if (pairs > 0) {
     const unsigned grid = 2u * (unsigned)(pairs < n_tiles ? pairs : n_tiles);
     if (tf32)
       ewald_split_pair_kernel<true><<<grid, kThreads, kPairSmemBytes, s>>>(
-          mh, ml, n, k_blocks, chunk_blocks, nt, out, diag_sum, rt, err);
+          mh, ml, n, k_blocks, chunk_blocks, nt, raster, out, diag_sum, rt, err);
     else
       ewald_split_pair_kernel<false><<<grid, kThreads, kPairSmemBytes, s>>>(
-          mh, ml, n, k_blocks, chunk_blocks, nt, out, diag_sum, rt, err);
+          mh, ml, n, k_blocks, chunk_blocks, nt, raster, out, diag_sum, rt, err);
   } else {
     int dev = 0, sms = 0;
     PYCD_CUDA(cudaGetDevice(&dev));
@@ -1412,12 +1409,12 @@ int ewald_build_split(const PycdEwaldDesc* d, int mode, double* out,
       PYCD_CUDA(cudaFuncSetAttribute(ewald_split_kernel<true>,
                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
       ewald_split_kernel<true><<<ctas, kThreads, smem, s>>>(
-          mh, ml, n, k_blocks, chunk_blocks, nt, out, diag_sum, rt, err);
+          mh, ml, n, k_blocks, chunk_blocks, nt, raster, out, diag_sum, rt, err);
     } else {
       PYCD_CUDA(cudaFuncSetAttribute(ewald_split_kernel<false>,
                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
       ewald_split_kernel<false><<<ctas, kThreads, smem, s>>>(
-          mh, ml, n, k_blocks, chunk_blocks, nt, out, diag_sum, rt, err);
+          mh, ml, n, k_blocks, chunk_blocks, nt, raster, out, diag_sum, rt, err);
     }
   }
   PYCD_CUDA(cudaGetLastError());

@@ -110,7 +110,8 @@ def choose_mode(system, pmiv, requested="auto"):
 
 
 def build_device_array(system, alpha, r_cut, k_cut, precision="auto",
-                       pmiv="system", stream=None, out=None, parts=0, kvecs=None):
+                       pmiv="system", stream=None, out=None, parts=0, kvecs=None,
+                       split_launch=None):
     """Build the N x N FP64 array on the current CUDA device.
 
     Returns ``(A, info)``: ``A`` a CUDA float64 tensor, ``info`` a dict with
@@ -119,6 +120,10 @@ def build_device_array(system, alpha, r_cut, k_cut, precision="auto",
     ``parts``: a mask of ``_native.EWALD_PART_*`` (0 = the whole array).
     ``kvecs``: an explicit (K, 3) integer k list instead of the one k_cut
     selects.
+    ``split_launch``: launch shape of the split modes, ``{"form": "auto" |
+    "pair" | "single", "raster": super-tiles per raster block side (0 =
+    default)}`` (``autotune.tune_split`` picks one); the array does not
+    depend on it.
     """
     import torch
     nat.require_device()
@@ -128,6 +133,9 @@ def build_device_array(system, alpha, r_cut, k_cut, precision="auto",
     mode = choose_mode(system, pmiv, precision)
     desc, keep, k_max = make_desc(system, alpha, r_cut, k_cut, pmiv, kvecs)
     desc.parts = int(parts)
+    if split_launch:
+        desc.split_form = nat.SPLIT_FORMS[split_launch.get("form", "auto")]
+        desc.split_raster = int(split_launch.get("raster", 0))
     dev = keep[0].device
     L = nat.lib()
     code = nat.EWALD_MODES[mode]

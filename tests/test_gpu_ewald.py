@@ -186,16 +186,28 @@ def test_split_real_space_table_equals_pair_pass(cuda_ready, monkeypatch, precis
 
 
 @pytest.mark.parametrize("precision", ["bf16x3", "tf32x3"])
-def test_split_pair_form_equals_single_cta_form(cuda_ready, monkeypatch, precision):
+def test_split_launch_shapes_give_the_same_array(cuda_ready, precision):
     """The CTA-pair contraction (tcgen05 cta_group::2: 256-row MMAs, each CTA
-    loading half of the B rows) and the single-CTA form it falls back to
-    (PYCD_SPLIT_FORM=single) give the same array: 1,200 sites, five
-    super-tile rows, the last one partly outside the matrix."""
+    loading half of the B rows) and the single-CTA form it falls back to,
+    with raster blocks of 1, 3 and 8 super-tiles, give the same array:
+    1,200 sites, five super-tile rows, the last one partly outside the
+    matrix.  The autotuner picks one of them and keeps it for the system."""
+    from pycd_gb300 import autotune
     sysm = wl.corundum((10, 10, 1), neighbor_list=False)
-    A_pair = sysm.get_precomputed_array_device(precision).cpu().numpy()
-    monkeypatch.setenv("PYCD_SPLIT_FORM", "single")
-    A_single = sysm.get_precomputed_array_device(precision).cpu().numpy()
-    assert np.isfinite(A_pair).all()
-    assert np.abs(A_pair - A_single).max() < 1e-12 * K.EV2HARTREE
     ref = sysm.get_precomputed_array_device("fp64").cpu().numpy()
+    out = {}
+    for form, raster in (("pair", 8), ("single", 8), ("pair", 1), ("single", 3)):
+        sysm.split_launch = {"form": form, "raster": raster}
+        out[form, raster] = sysm.get_precomputed_array_device(precision).cpu().numpy()
+    A_pair = out["pair", 8]
+    assert np.isfinite(A_pair).all()
     assert np.abs(A_pair - ref).max() < SPLIT_TOL_HA
+    for shape, A in out.items():
+        assert np.abs(A - A_pair).max() < 1e-12 * K.EV2HARTREE, shape
+    sysm.split_launch = None
+    res = autotune.tune_split(sysm, precision, reps=1)
+    assert sysm.split_launch == res["best"]
+    assert {(c["form"], c["raster"]) for c, _ in res["table"]} == set(
+        autotune.SPLIT_CANDIDATES)
+    A_tuned = sysm.get_precomputed_array_device(precision).cpu().numpy()
+    assert np.abs(A_tuned - A_pair).max() < 1e-12 * K.EV2HARTREE

@@ -25,7 +25,7 @@ def test_library_exports_every_declared_symbol():
     for name in declared:
         assert hasattr(lib, name), name
         assert name in nat.exported_symbols(), name
-    assert lib.pycd_abi_version() == 3
+    assert lib.pycd_abi_version() == nat.ABI_VERSION == 4
 
 
 def test_default_lanes_rule():
@@ -75,6 +75,30 @@ def test_exp_fixed_table_is_correctly_rounded():
     for j in range(4096):
         exact = int(mp.nint(mp.mpf(2) ** (mp.mpf(j) / 4096) * mp.mpf(2) ** 62))
         assert int(out[j]) == exact, j
+
+
+def test_split_launch_fields_are_validated():
+    """PycdEwaldDesc.split_form / split_raster: the defaults (0) and every
+    allowed value size the workspace; values outside are rejected on the
+    host with PYCD_ERR_INVALID_ARG (no device needed)."""
+    d = nat.EwaldDesc()
+    d.n_sites, d.n_kvec = 512, 100
+    d.d_cart, d.d_kvec = 16, 16  # not dereferenced by the size query
+    d.alpha, d.volume, d.dielectric = 0.1, 1000.0, 12.0
+    size = nat.C.c_size_t()
+    L = nat.lib()
+    mode = nat.EWALD_MODES["bf16x3"]
+    assert L.pycd_ewald_workspace_size(ctypes.byref(d), mode, ctypes.byref(size)) == 0
+    base = size.value
+    for form, raster in ((1, 1), (2, 64), (1, 0)):
+        d.split_form, d.split_raster = form, raster
+        assert L.pycd_ewald_workspace_size(ctypes.byref(d), mode, ctypes.byref(size)) == 0
+        assert size.value == base
+    for form, raster in ((3, 0), (-1, 0), (0, 65), (0, -1)):
+        d.split_form, d.split_raster = form, raster
+        rc = L.pycd_ewald_workspace_size(ctypes.byref(d), mode, ctypes.byref(size))
+        assert rc == nat.ERR_INVALID_ARG, (form, raster)
+        assert "split_" in nat.lib().pycd_last_error().decode()
 
 
 def test_library_reports_missing_device_as_error():
