@@ -19,12 +19,13 @@
 // by the half that owns its row.
 //
 // Schedule.  One persistent CTA per SM takes units from a global counter in
-// a blocked order (raster x raster super-tiles at a time, the block rows
-// of the upper triangle in turn; raster from PycdEwaldDesc.split_raster).  The units in flight at one time then
-// share few operand panels and advance along K together, so each K slice
-// of a panel is read from DRAM about once and reused from L2.  Tensor
-// memory stays allocated from unit to unit and the barrier phases carry
-// over, so one unit's last epilogue overlaps the next unit's loads and MMAs.
+// a blocked order (raster x raster super-tiles at a time, the block rows of
+// the upper triangle in turn; raster from PycdEwaldDesc.split_raster).  The
+// units in flight at one time then share few operand panels and advance
+// along K together, so each K slice of a panel is read from DRAM about once
+// and reused from L2.  Tensor memory stays allocated from unit to unit and
+// the barrier phases carry over, so the next unit's first loads overlap one
+// unit's last epilogue.
 //
 // Sum over chunks.  The tensor core's FP32 accumulation truncates, so one
 // accumulation covers at most kChunkCols K columns (a chunk).  The

@@ -22,9 +22,11 @@ produced by the reference's code or ships with it:
       digest and Ewald array rows, and its event stream for 1e5 steps driven
       by injected uniforms np.random.default_rng(0).random(2e5).
   corundum3600.json/.npz
-      the 3,600-site lattice with 4 electrons and 4 fixed +1 dopants: the
-      reference's event stream for a 2,000-step prefix of two trajectories,
-      run on the oracle's array and our hop list (both pinned above).
+      the 3,600-site lattice (10x10x3 cells) with 4 electrons and 4 fixed +1
+      dopants: digests of the reference's own hop-neighbour list and pmiv,
+      rows of its own FP64 Ewald array (the carrier and dopant sites), and
+      its event stream for a 2,000-step prefix of two trajectories run on
+      that array.
   ewald_params.json/.npz
       get_ewald_parameters of the reference on the Hematite example lattice:
       automatic r_cut, automatic r_cut and k_cut, automatic alpha (2x2x1,
@@ -59,6 +61,8 @@ import numpy as np
 
 HERE = Path(__file__).resolve().parent
 REPO = HERE.parent.parent
+sys.path[:0] = [str(HERE.parent), str(REPO)]
+from golden_io import hop_digest, hop_to_arrays  # noqa: E402  (same canonical form as the tests)
 REF = Path(os.environ["PYCD_REFERENCE"]) if os.environ.get("PYCD_REFERENCE") else None
 
 
@@ -206,23 +210,6 @@ def poscar_text(comment, lattice, types_, counts, frac):
 
 
 # ---------------------------------------------------------------- helpers
-def hop_to_arrays(hop):
-    meta, arrs = {}, {}
-    for key, per_class in hop.items():
-        meta[key] = []
-        for ci, per_type in enumerate(per_class):
-            meta[key].append(len(per_type))
-            for ti, rv in enumerate(per_type):
-                tag = f"hop|{key}|{ci}|{ti}"
-                arrs[tag + "|count"] = np.asarray(rv.num_neighbors, np.int64)
-                idx = [np.asarray(x, np.int64) for x in rv.neighbor_system_element_indices]
-                vec = [np.asarray(x, np.float64).reshape(-1, 3)
-                       for x in rv.displacement_vector_list]
-                arrs[tag + "|idx"] = np.concatenate(idx) if idx else np.zeros(0, np.int64)
-                arrs[tag + "|vec"] = np.concatenate(vec) if vec else np.zeros((0, 3))
-    return meta, arrs
-
-
 def material_objects(core, params, poscar, system_size, pbc, tmp):
     p = dict(params)
     p.pop("precision_parameters", None)
@@ -517,35 +504,35 @@ def corundum324(core):
 def corundum3600(core):
     sys.path.insert(0, str(REPO))
     from oracle import ewald_oracle as eo
-    import pycd_gb300.lattice as ml
     frac = corundum_frac()
     poscar = poscar_text("corundum Fe sublattice", CORUNDUM_LATTICE, ["Fe"], [12], frac)
     tmp = tempfile.mkdtemp()
     params = dict(CORUNDUM)
     mat, nb = material_objects(core, params, poscar, [10, 10, 3], [1, 1, 1], tmp)
-    p = dict(params)
-    p.pop("precision_parameters")
-    (Path(tmp) / "P2").write_text(poscar)
-    p["input_coord_file_location"] = Path(tmp) / "P2"
-    mm = ml.Material(ml.ReturnValues(**p))
-    mn = ml.Neighbors(mm, np.array([10, 10, 3]), np.array([1, 1, 1]))
     t0 = time.time()
-    hop = mn.generate_neighbor_list(None, (3, 3, 3), save=False)
-    print(f"corundum3600: hop list (this package) {time.time() - t0:.1f} s")
-    lat = mm.lattice_matrix
-    # units as System: alpha / ANG2BOHR, r_cut * ANG2BOHR, k_cut / ANG2BOHR
-    from pycd_gb300 import constants as K
-    alpha = params["alpha"] / K.ANG2BOHR
+    nb.generate_neighbor_list(Path(tmp), np.array([3, 3, 3]))
+    hop = np.load(Path(tmp) / "hop_neighbor_list.npy", allow_pickle=True)[()]
+    nb.get_pairwise_min_image_vector_data(Path(tmp))
+    pmiv = np.load(Path(tmp) / "pairwise_min_image_vector_data.npy")
+    t_nbr = time.time() - t0
+    print(f"corundum3600: reference neighbour list + pmiv in {t_nbr:.1f} s")
+    system = make_system(core, mat, nb, hop, pmiv, params)
     t0 = time.time()
-    A = eo.class_array(mm.cartesian_unit_cell_coords, lat, [10, 10, 3], alpha,
-                       params["r_cut"] * K.ANG2BOHR, params["k_cut"] / K.ANG2BOHR,
-                       params["dielectric_constant"])
-    print(f"corundum3600: oracle class array {time.time() - t0:.1f} s")
-    system = core.System(mat, nb, hop, None, params["alpha"], params["r_cut"],
-                         params["k_cut"], params["precision_parameters"], [], [])
+    A = ref_array(system, mat, nb)
+    t_ewald = time.time() - t0
+    print(f"corundum3600: reference Ewald array in {t_ewald:.1f} s")
     rng = np.random.default_rng(3600)
     sites = rng.choice(3600, size=8, replace=False)
     carriers, dopants = sites[:4].tolist(), sites[4:].tolist()
+    rows = np.array(carriers + dopants)
+    # the oracle's translation-class evaluation against the reference's rows
+    from pycd_gb300 import constants as K
+    orc = eo.class_array(mat.cartesian_unit_cell_coords, mat.lattice_matrix, [10, 10, 3],
+                         params["alpha"] / K.ANG2BOHR, params["r_cut"] * K.ANG2BOHR,
+                         params["k_cut"] / K.ANG2BOHR, params["dielectric_constant"],
+                         rows=rows)
+    orc_err = float(np.abs(orc - A[rows]).max())
+    print(f"corundum3600: oracle rows vs reference rows {orc_err:.3e} Ha")
     # dopants: lattice charge 0 overwritten by +1 (charge_config, core.py:2550-2554)
     doping = {"num_dopants": [4], "doping_element_map": ["Fe:D"],
               "insertion_type": ["manual"], "charge": {"full": {"D": 1.0}},
@@ -598,10 +585,13 @@ def corundum3600(core):
     cfg = {"name": "corundum3600", "params": params, "poscar": poscar,
            "system_size": [10, 10, 3], "pbc": [1, 1, 1], "carriers": carriers,
            "dopants": dopants, "dopant_charge": 1.0, "uniform_seeds": [1000, 1001],
-           "n_steps": 2000, "t_final": 1e30, "time_interval": 1e27}
+           "n_steps": 2000, "t_final": 1e30, "time_interval": 1e27,
+           "hop_sha256": hop_digest(hop), "pmiv_sha256": sha(pmiv),
+           "A_diag": float(A[0, 0]), "A_diag_ptp": float(np.ptp(np.diag(A))),
+           "oracle_rows_max_abs_ha": orc_err,
+           "reference_neighbor_seconds": t_nbr, "reference_ewald_seconds": t_ewald}
     np.savez_compressed(HERE / "corundum3600.npz", proc=np.asarray(procs_all, np.uint8),
-                        time=np.asarray(times_all),
-                        A_rows=A[np.array(carriers + dopants)])
+                        time=np.asarray(times_all), A_rows=A[rows])
     (HERE / "corundum3600.json").write_text(json.dumps(cfg, indent=1))
 
 

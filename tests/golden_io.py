@@ -1,4 +1,6 @@
-"""Load the golden fixtures of tests/golden into this package's objects."""
+"""Load the golden fixtures of tests/golden into this package's objects, and
+the canonical array form of a hop-neighbour list shared with the generator."""
+import hashlib
 import json
 import tempfile
 from pathlib import Path
@@ -51,3 +53,34 @@ def material(cfg, system_size=None):
     ss = np.asarray(system_size if system_size is not None else cfg["system_size"])
     nb = Neighbors(mat, ss, np.asarray(cfg["pbc"]))
     return mat, nb
+
+
+def hop_to_arrays(hop):
+    """A hop-neighbour list ({key: [class][type] -> neighbour record}) as
+    (meta, arrays): per record the neighbour counts, the concatenated
+    neighbour indices (int64) and displacement vectors (float64, (n, 3))."""
+    meta, arrs = {}, {}
+    for key, per_class in hop.items():
+        meta[key] = []
+        for ci, per_type in enumerate(per_class):
+            meta[key].append(len(per_type))
+            for ti, rv in enumerate(per_type):
+                tag = f"hop|{key}|{ci}|{ti}"
+                arrs[tag + "|count"] = np.asarray(rv.num_neighbors, np.int64)
+                idx = [np.asarray(x, np.int64) for x in rv.neighbor_system_element_indices]
+                vec = [np.asarray(x, np.float64).reshape(-1, 3)
+                       for x in rv.displacement_vector_list]
+                arrs[tag + "|idx"] = np.concatenate(idx) if idx else np.zeros(0, np.int64)
+                arrs[tag + "|vec"] = np.concatenate(vec) if vec else np.zeros((0, 3))
+    return meta, arrs
+
+
+def hop_digest(hop):
+    """sha256 over a hop-neighbour list's per-site counts, neighbour indices
+    and displacement vectors, in key / class / type order."""
+    meta, arrs = hop_to_arrays(hop)
+    h = hashlib.sha256(json.dumps(meta, sort_keys=True).encode())
+    for tag in sorted(arrs):
+        h.update(tag.encode())
+        h.update(np.ascontiguousarray(arrs[tag]).tobytes())
+    return h.hexdigest()

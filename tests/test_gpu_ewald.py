@@ -70,10 +70,18 @@ def test_build_without_pmiv_uses_device_min_image(cuda_ready):
 
 
 def test_corundum3600_build_properties_and_oracle_rows(cuda_ready):
+    """The batched configuration's array (3,600 sites): the carrier and
+    dopant rows within 1e-10 eV of the reference's own FP64 array
+    (fixture), sampled rows within 1e-10 eV of the oracle, symmetric, equal
+    diagonal."""
     sysm = wl.corundum((10, 10, 3))
     A = sysm.get_precomputed_array_device("fp64")
     assert sysm.last_build_info["n_kvec"] == 3151
     An = A.cpu().numpy()
+    cfg, arr = gio.load("corundum3600")
+    fixture_rows = np.array(cfg["carriers"] + cfg["dopants"])
+    assert np.abs(An[fixture_rows] - arr["A_rows"]).max() < TOL_HA
+    assert abs(An[0, 0] - cfg["A_diag"]) < TOL_HA
     # symmetric, equal diagonal, translation invariant (size-independent)
     assert np.abs(An - An.T).max() < TOL_HA
     assert np.ptp(np.diag(An)) < TOL_HA

@@ -326,6 +326,41 @@ def test_kernel_exp_within_ulps_of_cuda_and_libm(cuda_ready):
     assert np.isinf(o[x >= 709.8]).all() and (o[x <= -745.2] == 0).all()
 
 
+def test_kernel_exp_integer_path_edges(cuda_ready):
+    """The integer-pipe exp (|x| < 704) at its internal edges: around
+    |x| = 2^-13 (where the reduction starts), tiny and subnormal arguments,
+    arguments half a step of ln2/4096 apart (the rounding of n), results
+    whose 53-bit rounding carries into the exponent, and the switch to the
+    FP64 form at |x| = 704.  Within 1 ulp of NumPy's exp (the kernels' exp is
+    within ~0.502 ulp of exp(x))."""
+    import math
+    import torch
+    rng = np.random.default_rng(11)
+    step = math.log(2) / 4096
+    k = rng.integers(-4_000_000, 4_000_000, 50000)
+    x = np.concatenate([
+        rng.uniform(-2.5e-4, 2.5e-4, 100000),
+        np.array([s * np.ldexp(1.0, e) * (1 + 1e-9 * i) for s in (1, -1)
+                        for e in range(-80, -9) for i in range(-3, 4)]),
+        (k + 0.5) * step + rng.uniform(-1e-12, 1e-12, len(k)),
+        # exp(x) just below a power of two (mantissa all ones before rounding)
+        np.log(np.nextafter(np.ldexp(1.0, np.arange(-900, 1000, 7)), 0)),
+        rng.uniform(703.0, 704.5, 20000), rng.uniform(-704.5, -703.0, 20000),
+        np.array([5e-324, -5e-324, 2.2e-308, -2.2e-308, 2 ** -13, -2 ** -13,
+                  np.nextafter(2 ** -13, 0), -np.nextafter(2 ** -13, 0), 703.99999999,
+                  -703.99999999]),
+    ])
+    xd = torch.as_tensor(x).cuda()
+    ours = torch.empty_like(xd)
+    ref = torch.empty_like(xd)
+    nat.check(nat.lib().pycd_debug_exp(xd.data_ptr(), len(x), ours.data_ptr(),
+                                       ref.data_ptr(), nat.stream_handle()))
+    torch.cuda.synchronize()
+    o, h = ours.cpu().numpy(), np.exp(x)
+    assert np.isfinite(o).all()
+    assert _ulp_diff(o, h).max() <= 1
+
+
 def test_event_stream_independent_of_launch_shape(cuda_ready):
     """Cumulative rates are balanced-tree sums over the process index, so
     the lanes-per-trajectory choice must not change any event or time."""

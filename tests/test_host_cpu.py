@@ -127,6 +127,16 @@ def test_neighbor_list_matches_reference_corundum324():
                                           rv.displacement_vector_list[i])
 
 
+def test_neighbor_list_matches_reference_corundum3600():
+    """The 3,600-site lattice of the batched configuration (10x10x3 cells):
+    our hop-neighbour list equals the reference's own (its digest over
+    counts, indices and displacement vectors, generated by the reference)."""
+    cfg, arr = gio.load("corundum3600")
+    mat, nb = gio.material(cfg)
+    ours = nb.generate_neighbor_list(None, (3, 3, 3), save=False)
+    assert gio.hop_digest(ours) == cfg["hop_sha256"]
+
+
 def test_pmiv_matches_reference_corundum324():
     import hashlib
     cfg, arr = gio.load("corundum324")
