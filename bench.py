@@ -42,13 +42,14 @@ SCHED_STEPS = 0
 # FP64 thread instructions per KMC step on this workload, by launch shape
 # (lanes per trajectory, register variant): ncu
 # smsp__sass_thread_inst_executed_op_{dadd,dfma,dmul}_pred_on summed over one
-# 10,000-step chunk launch, divided by its 4.096e7 KMC steps.  The autotuner
-# picks (8, 1), i.e. kmc_advance_kernel<8, 2, 1>; other shapes report null.
-FP64_INSTR_PER_STEP = {(8, 1): 351.5}
-# DRAM bytes per KMC step of kmc_advance_kernel<8, 2, 1> (ncu:
-# dram__bytes_read.sum + dram__bytes_write.sum of the same launch,
-# 7,833,856 + 0 bytes, divided by its 4.096e7 KMC steps)
-DRAM_BYTES_PER_STEP = 7833856 / 40960000
+# 1,000-step chunk launch, divided by its 4.096e6 KMC steps.  The autotuner
+# picks (16, 2), i.e. kmc_advance_kernel<16, 1, 2>; with 8 lanes the step's
+# shared FP64 work is repeated on fewer lanes.
+FP64_INSTR_PER_STEP = {(16, 2): 428, (8, 1): 280}
+# DRAM bytes per KMC step of kmc_advance_kernel<16, 1, 2> (ncu:
+# dram__bytes_read.sum + dram__bytes_write.sum of one 10,000-step chunk launch
+# of this workload, 7,420,928 + 3,072 bytes, divided by its 4.096e7 KMC steps)
+DRAM_BYTES_PER_STEP = (7420928 + 3072) / 40960000
 
 
 def peaks():
@@ -151,7 +152,7 @@ def time_plain(tables, occ, n_steps=20000):
     import torch
     from pycd_gb300.kmc import KmcBatch, KmcEngine
     best = 0.0
-    for lanes in (8, 16, 32, 64, 128):  # 64, 128: one block of 2 or 4 warps
+    for lanes in (4, 8, 16, 32, 64, 128):  # 64, 128: one block of 2 or 4 warps
         eng = KmcEngine(tables, launch={"lanes_per_traj": lanes})
         b = KmcBatch(occ[:1])
         eng.advance(b, 2000, eng.rng_struct(seed=SEED))
@@ -749,7 +750,7 @@ def plain_record():
     u = np.random.default_rng(0).random(2 * n_steps)
     u_dev = torch.as_tensor(u).cuda()[None, :]
     best, proc, times = None, None, None
-    for lanes in (8, 16, 32, 64, 128):  # the plain form at its fastest lane count
+    for lanes in (2, 4, 8, 16, 32, 64, 128):  # the plain form at its fastest lane count
         eng = KmcEngine(tables, launch={"lanes_per_traj": lanes})
         for rep in range(2):
             b = KmcBatch([[site]], step_capacity=n_steps,

@@ -424,10 +424,8 @@ PYCD_API int pycd_kmc_default_lanes(int32_t max_processes, int32_t max_carriers,
 PYCD_API int pycd_philox_uniforms(uint64_t seed, uint64_t traj, int64_t step0,
                          int64_t n_steps, double* d_out, void* stream);
 
-/* Self-check of the kernels' exp(): d_ours[i] = the KMC kernels' exp(d_x[i])
- * in the form the rate of an even (FP64 form) or odd (integer form) process
- * index i uses, d_cuda[i] = CUDA's exp(d_x[i]).  No counterpart in the
- * reference.                                                               */
+/* Self-check of the kernels' exp(): d_ours[i] = the KMC kernels' exp(d_x[i]),
+ * d_cuda[i] = CUDA's exp(d_x[i]).  No counterpart in the reference.        */
 PYCD_API int pycd_debug_exp(const double* d_x, int64_t n, double* d_ours,
                             double* d_cuda, void* stream);
 

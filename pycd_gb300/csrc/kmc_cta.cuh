@@ -270,7 +270,7 @@ __device__ void advance_trajectory_cta(const KmcArgs& a, int64_t t, CtaShared& s
 
     // ---- rates ----------------------------------------------------------
     double kp[MAXP], term[MAXP];
-    process_rates<MAXP>(pc, g, q, two_q, kp, term);
+    process_rates<MAXP>(pc, q, two_q, kp, term);
 
     // ---- tree: lane, warp, then the W warp totals -----------------------
     LocalTree<MAXP> lt;

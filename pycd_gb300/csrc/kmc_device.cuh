@@ -171,22 +171,6 @@ __device__ __forceinline__ double kmc_exp(double x) {
   return exp_int(x);
 }
 
-// The FP64 form throughout (9 FP64 instructions for |x| < 704).
-__device__ __forceinline__ double kmc_exp_fp64(double x) {
-  if ((__double2hiint(x) & 0x7fffffff) >= 0x40860000) return exp_tang_wide(x);
-  int m;
-  const double v = exp_tang_core(x, m);
-  return __hiloint2double(__double2hiint(v) + (m << 20), __double2loint(v));
-}
-
-// Rate exp of process p: even processes take the FP64 form, odd ones the
-// integer form, so a lane with two or more processes runs two independent
-// exp chains on two pipes.  Fixed by the process index, so every launch
-// shape gives the same rates.
-__device__ __forceinline__ double rate_exp(int p, double x) {
-  return (p & 1) ? kmc_exp(x) : kmc_exp_fp64(x);
-}
-
 // a > b for doubles known to be >= +0 and not NaN: their bit patterns order
 // as integers, which keeps the comparison on the integer pipe
 __device__ __forceinline__ bool nonneg_gt(double a, double b) {
@@ -575,7 +559,7 @@ __device__ __forceinline__ bool rebuild_moved(const PycdKmcSystem& sy,
 //   term = q (P - Q) + cq,   x' = sqrt(-c1) (lam + dE0) = xa term + xb,
 //   k = exp(c0 - x'^2),      dE0 = 2q term + de (for the selected process).
 template <int MAXP>
-__device__ __forceinline__ void process_rates(const ProcCache<MAXP>& pc, int g, double q,
+__device__ __forceinline__ void process_rates(const ProcCache<MAXP>& pc, double q,
                                               double two_q, double (&kp)[MAXP],
                                               double (&term)[MAXP]) {
 #pragma unroll
@@ -585,7 +569,7 @@ __device__ __forceinline__ void process_rates(const ProcCache<MAXP>& pc, int g, 
     if (pc.valid[j]) {
       term[j] = fma(q, dsub(pc.P[j], pc.Q[j]), pc.cq[j]);
       const double xs = fma(pc.xa[j], term[j], pc.xb[j]);
-      kp[j] = rate_exp(g * MAXP + j, fma(-xs, xs, pc.c0[j]));
+      kp[j] = kmc_exp(fma(-xs, xs, pc.c0[j]));
     }
   }
 }
@@ -822,7 +806,7 @@ __device__ void advance_trajectory(const KmcArgs& a, int64_t t, int g,
 
     // ---- rates (core.py:1989-2050) ------------------------------------
     double kp[MAXP], term[MAXP];
-    process_rates<MAXP>(pc, g, q, two_q, kp, term);
+    process_rates<MAXP>(pc, q, two_q, kp, term);
 
     // ---- selection (core.py:2796-2800) on the balanced tree ------------
     LocalTree<MAXP> lt;

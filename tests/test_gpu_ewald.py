@@ -111,6 +111,27 @@ def test_split_precision_small_matches_fp64(cuda_ready, precision, tol_ev):
     assert np.abs(A - A.T).max() < SPLIT_TOL_HA
 
 
+@pytest.mark.parametrize("cells", [(2, 2, 1), (3, 3, 1), (4, 4, 1)])
+def test_split_precision_small_systems(cuda_ready, cells):
+    """48, 108 and 192 sites: one super-tile whose second 128-row half (the
+    second CTA of a pair) lies wholly or partly outside the matrix.  Both
+    launch forms within 2e-6 eV of the FP64 feature build (the small-K floor
+    of the BF16 split), symmetric, and equal to each other."""
+    sysm = wl.corundum(cells, neighbor_list=False)
+    ref = sysm.get_precomputed_array_device("fp64").cpu().numpy()
+    for precision in ("bf16x3", "tf32x3"):
+        got = {}
+        for form in ("pair", "single"):
+            sysm.split_launch = {"form": form}
+            A = sysm.get_precomputed_array_device(precision).cpu().numpy()
+            assert np.isfinite(A).all()
+            assert np.abs(A - ref).max() < 2e-6 * K.EV2HARTREE, (precision, form)
+            assert np.abs(A - A.T).max() < SPLIT_TOL_HA
+            got[form] = A
+        assert np.abs(got["pair"] - got["single"]).max() < 1e-12 * K.EV2HARTREE
+    sysm.split_launch = None
+
+
 @pytest.mark.parametrize("precision", ["bf16x3", "tf32x3"])
 def test_split_precision_monoclinic_8192(cuda_ready, precision):
     """N = 8,192 monoclinic (16x16x8 cells), K = 4,095: every entry within

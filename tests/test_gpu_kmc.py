@@ -303,9 +303,8 @@ def _ulp_diff(a, b):
 
 
 def test_kernel_exp_within_ulps_of_cuda_and_libm(cuda_ready):
-    """The kernels' table-driven exp (both forms: even indices the FP64
-    form, odd the integer form) against CUDA's exp and NumPy's exp on the
-    range the rates use and across the whole finite range."""
+    """The kernels' table-driven exp against CUDA's exp and NumPy's exp on
+    the range the rates use and across the whole finite range."""
     import torch
     rng = np.random.default_rng(3)
     x = np.concatenate([rng.uniform(-80.0, 40.0, 400000),
@@ -328,13 +327,12 @@ def test_kernel_exp_within_ulps_of_cuda_and_libm(cuda_ready):
 
 
 def test_kernel_exp_integer_path_edges(cuda_ready):
-    """Both forms of the kernels' exp (even indices FP64, odd indices the
-    integer pipe, as the rates of even and odd processes) at the integer
-    form's internal edges: around |x| = 2^-13 (where the reduction starts),
-    tiny and subnormal arguments, arguments half a step of ln2/4096 apart
-    (the rounding of n), results whose 53-bit rounding carries into the
-    exponent, and the switch to the FP64 form at |x| = 704.  Within 1 ulp of
-    NumPy's exp (each form is within ~0.52 ulp of exp(x))."""
+    """The integer-pipe exp (|x| < 704) at its internal edges: around
+    |x| = 2^-13 (where the reduction starts), tiny and subnormal arguments,
+    arguments half a step of ln2/4096 apart (the rounding of n), results
+    whose 53-bit rounding carries into the exponent, and the switch to the
+    FP64 form at |x| = 704.  Within 1 ulp of NumPy's exp (the kernels' exp is
+    within ~0.502 ulp of exp(x))."""
     import math
     import torch
     rng = np.random.default_rng(11)
