@@ -208,6 +208,18 @@ def write_cpu_inputs(system, run, dopants, tmpdir):
     return str(a_path), str(tab_path)
 
 
+def batched_config(args, world):
+    """The workload both arms report (the reference arm times a sample of it,
+    described in its cpu_baseline)."""
+    return {"workload": "batched uniform: corundum 10x10x3 = 3,600 sites, "
+                        "4 electrons + 4 fixed +1 dopants, FP64 Ewald array "
+                        "(103.7 MB), Philox streams",
+            "trajectories_per_gpu": args.traj, "steps_per_chunk": args.chunk,
+            "chunk": "one CUDA-graph launch of the persistent kernel",
+            "l2": "256 MiB buffer written between timed chunks",
+            "parallelism": f"replicas x{world}"}
+
+
 def reference_arm(args):
     """--impl reference: the reference's algorithm (oracle port) on all host
     cores, one trajectory per process as the reference's 'parallel' mode."""
@@ -251,9 +263,7 @@ def reference_arm(args):
             "ms_per_step": 1e3 * total_s / max(1, args.steps),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f64", "data": "synthetic",
-            "config": {"workload": "batched uniform corundum 10x10x3 (3,600 sites), "
-                                   "4 electrons + 4 fixed +1 dopants, FP64 array",
-                       "sample_per_step": f"{cores} trajectories x {m} KMC steps"},
+            "config": batched_config(args, int(os.environ.get("WORLD_SIZE", "1"))),
             "cpu_baseline": {"value": value, "unit": "steps/s", "cores": cores,
                              "kind": "port",
                              "sample": f"{cores} trajectories x {m} steps per bench "
@@ -1075,13 +1085,7 @@ def main():
             "warmup": args.warmup, "ms_per_step": 1e3 * wall_max / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f64", "data": "synthetic",
-            "config": {"workload": "batched uniform: corundum 10x10x3 = 3,600 sites, "
-                                   "4 electrons + 4 fixed +1 dopants, FP64 Ewald array "
-                                   "(103.7 MB), Philox streams",
-                       "trajectories_per_gpu": args.traj, "steps_per_chunk": args.chunk,
-                       "chunk": "one CUDA-graph launch of the persistent kernel",
-                       "l2": "256 MiB buffer written between timed chunks",
-                       "parallelism": f"replicas x{world}"},
+            "config": batched_config(args, world),
             "plain_steps_per_s": plain, "batched_over_plain": value / world / plain,
             "launch_shape": tuned,
             "status_counts": status,
