@@ -105,11 +105,14 @@ SPLIT_CANDIDATES = (("pair", 4), ("pair", 8), ("pair", 16), ("single", 8))
 
 def split_cache_key(system, precision):
     """(precision, site-count bucket, k-count bucket): factors of two of N and
-    of the k list length, which set the tile count and the operand panels'
-    length, so the L2 reuse the raster order buys."""
+    of the k list length (enumerated on the host, as the build does), which
+    set the tile count and the operand panels' length, so the L2 reuse the
+    raster order buys."""
+    from . import ewald as ew
     n = int(system.neighbors.num_system_elements)
-    info = getattr(system, "last_build_info", None) or {}
-    k = int(info.get("n_kvec", 0))
+    _, _, k_cut, _ = system._ewald_parameters()
+    k_max = ew.k_max_for(system, k_cut)
+    k = len(ew.effective_k_vectors(system.reciprocal_lattice_matrix, k_max, k_cut))
     return (precision, int(np.log2(max(1, n))), int(np.log2(max(1, k))))
 
 
@@ -120,7 +123,6 @@ def tune_split(system, precision="bf16x3", reps=2, candidates=SPLIT_CANDIDATES):
     ``{"best": shape, "table": [(shape, ms), ...]}``.  Cached in-process per
     ``split_cache_key``."""
     import torch
-    system.get_precomputed_array_device(precision)  # k count for the key; loads kernels
     key = split_cache_key(system, precision)
     if key in _SPLIT_CACHE:
         system.split_launch = dict(_SPLIT_CACHE[key])
