@@ -1378,21 +1378,18 @@ int ewald_build_split(const PycdEwaldDesc* d, int mode, double* out,
   const int n_tiles = nt * (nt + 1) / 2;
   const void* pair_fn = tf32 ? (const void*)ewald_split_pair_kernel<true>
                              : (const void*)ewald_split_pair_kernel<false>;
-  PYCD_CUDA(cudaFuncSetAttribute(pair_fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)kPairSmemBytes));
   int pairs = 0;
-  {
+  if (d->split_form != 2 &&
+      cudaFuncSetAttribute(pair_fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)kPairSmemBytes) == cudaSuccess) {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(2 * (unsigned)n_tiles);
     cfg.blockDim = dim3(kThreads);
     cfg.dynamicSmemBytes = kPairSmemBytes;
     cfg.stream = s;
-    if (cudaOccupancyMaxActiveClusters(&pairs, pair_fn, &cfg) != cudaSuccess) {
-      (void)cudaGetLastError();
-      pairs = 0;
-    }
+    if (cudaOccupancyMaxActiveClusters(&pairs, pair_fn, &cfg) != cudaSuccess) pairs = 0;
   }
-  if (d->split_form == 2) pairs = 0;  // single CTAs asked for
+  (void)cudaGetLastError();  // a device without such clusters takes single CTAs
   if (pairs > 0) {
     const unsigned grid = 2u * (unsigned)(pairs < n_tiles ? pairs : n_tiles);
     if (tf32)
