@@ -197,6 +197,45 @@ def test_split_precision_large_against_oracle_rows(cuda_ready, cells, k_cut, n_k
     torch.cuda.empty_cache()
 
 
+def test_split_precision_32768_against_oracle_rows(cuda_ready):
+    """The largest split-precision configuration, N = 32,768 (16x16x32
+    monoclinic cells), K = 4,097: BF16x3 and TF32x3 builds within 1e-6 eV of
+    the FP64 feature build everywhere and of the oracle's FP64 evaluation of
+    the reference's formula on rows at the 128-row and 256-row tile edges,
+    the middle, the last super-tile and two random rows; the FP64 build's
+    rows within 1e-10 eV of the oracle; hop-energy error far below kT."""
+    import torch
+    from pycd_gb300 import ewald as ew
+    cells = (16, 16, 32)
+    sysm = wl.monoclinic(cells, 0.5765, neighbor_list=True)
+    n = sysm.neighbors.num_system_elements
+    m = sysm.material
+    rng = np.random.default_rng(n)
+    rows = np.array(sorted({0, 127, 128, 255, 256, n // 2, n - 256, n - 1}
+                           | set(rng.choice(n, 2).tolist())))
+    orc = eo.class_array(m.cartesian_unit_cell_coords, m.lattice_matrix, cells,
+                         sysm.alpha, sysm.r_cut, sysm.k_cut, m.dielectric_constant,
+                         rows=rows)
+    ref = sysm.get_precomputed_array_device("fp64")
+    assert sysm.last_build_info["n_kvec"] == 4097
+    idx = torch.as_tensor(rows, device=ref.device)
+    assert np.abs(ref[idx].cpu().numpy() - orc).max() < TOL_HA
+    run = wl.run_for(sysm, 1)
+    for precision in ("bf16x3", "tf32x3"):
+        A = sysm.get_precomputed_array_device(precision)
+        got = A[idx].cpu().numpy()
+        assert np.isfinite(got).all()
+        assert np.abs(got - orc).max() < SPLIT_TOL_HA, precision
+        err_all = (A - ref).abs().max().item()
+        assert err_all < SPLIT_TOL_HA, (precision, err_all / K.EV2HARTREE)
+        de_max, _ = ew.hop_energy_error(ref, A, run.site_nbr, 16, 16, samples=1024,
+                                        seed=2)
+        assert de_max < 1e-3 * run.temp, precision
+        del A
+    del ref
+    torch.cuda.empty_cache()
+
+
 @pytest.mark.parametrize("precision", ["bf16x3", "tf32x3"])
 def test_split_real_space_table_equals_pair_pass(cuda_ready, monkeypatch, precision):
     """On a described supercell the split modes take the real-space and self
