@@ -216,9 +216,6 @@ __device__ __forceinline__ uint32_t smem_u32(const void* p) {
   return (uint32_t)__cvta_generic_to_shared(p);
 }
 
-__device__ __forceinline__ double2 cmul2(double2 a, double2 b) {
-  return make_double2(fma(a.x, b.x, -__dmul_rn(a.y, b.y)), fma(a.x, b.y, __dmul_rn(a.y, b.x)));
-}
 __device__ __forceinline__ float2 cmulf(float2 a, float2 b) {
   return make_float2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x));
 }
@@ -1131,6 +1128,38 @@ __global__ void weight_sum_kernel(const double* __restrict__ k2,
   if (threadIdx.x == 0) *out = red[0];
 }
 
+// Float-float numbers (hi, lo) with |lo| <= ulp(hi)/2, about 44 bits:
+// FP32 instructions only (GB300's FP32 pipe runs ~60x its FP64 pipe), with
+// every rounding explicit so that no contraction changes the error terms.
+__device__ __forceinline__ float2 ff_from(double v) {
+  const float h = __double2float_rn(v);
+  return make_float2(h, __double2float_rn(__dsub_rn(v, (double)h)));
+}
+// a * b: the exact product of the high parts (FMA), the cross terms, one
+// renormalisation; relative error ~2^-46
+__device__ __forceinline__ float2 ff_mul(float2 a, float2 b) {
+  const float p = __fmul_rn(a.x, b.x);
+  const float e = fmaf(a.x, b.y, fmaf(a.y, b.x, fmaf(a.x, b.x, -p)));
+  const float s = __fadd_rn(p, e);
+  return make_float2(s, __fsub_rn(e, __fsub_rn(s, p)));
+}
+// a + b: TwoSum of the high parts plus the low parts, one renormalisation
+__device__ __forceinline__ float2 ff_add(float2 a, float2 b) {
+  float e;
+  const float s = two_sum(a.x, b.x, e);
+  e = __fadd_rn(e, __fadd_rn(a.y, b.y));
+  const float r = __fadd_rn(s, e);
+  return make_float2(r, __fsub_rn(e, __fsub_rn(r, s)));
+}
+// complex float-float: (re.hi, re.lo, im.hi, im.lo)
+__device__ __forceinline__ float4 ffc_mul(float4 a, float4 b) {
+  const float2 ar = make_float2(a.x, a.y), ai = make_float2(a.z, a.w);
+  const float2 br = make_float2(b.x, b.y), bi = make_float2(b.z, b.w);
+  const float2 re = ff_add(ff_mul(ar, br), ff_mul(ai, make_float2(-bi.x, -bi.y)));
+  const float2 im = ff_add(ff_mul(ar, bi), ff_mul(ai, br));
+  return make_float4(re.x, re.y, im.x, im.y);
+}
+
 // Feature rows F_i = [sqrt(w_k) cos(k.r_i), sqrt(w_k) sin(k.r_i)]_k,
 // w_k = 2 c_k / (k^2 eps), written directly as the hi + lo operands of the
 // split contraction (no FP64 copy of F), zero-padded to `ld` columns.
@@ -1138,8 +1167,9 @@ __global__ void weight_sum_kernel(const double* __restrict__ k2,
 // e^{i k.r} is the product of per-site tables e^{i m phi_d}, phi_d = b_d . r,
 // built with FP64 sincos.  The BF16 split keeps ~16 bits of each feature,
 // so its two complex products run in FP32 (accurate to ~2e-7, far inside
-// the split); the TF32 split keeps ~22 bits and takes them in FP64.  A block
-// whose tables would not fit evaluates sincos(k . r) in FP64.
+// the split); the TF32 split keeps ~22 bits and takes them in float-float
+// (~44 bits, FP32 instructions only).  A block whose tables would not fit
+// evaluates sincos(k . r) in FP64.
 constexpr int kSfSites = 16;
 constexpr int kSfThreads = 256;
 constexpr int kSfSmem = 96 * 1024;
@@ -1151,7 +1181,9 @@ split_features_direct_kernel(const double* __restrict__ cart, int64_t n,
                              const double* __restrict__ kc, const double* __restrict__ k2,
                              const double* __restrict__ ck, int64_t K, double eps,
                              int64_t ld, void* __restrict__ hi, void* __restrict__ lo) {
-  extern __shared__ double2 tab[];  // [kSfSites][T], float2 pairs for BF16
+  // [kSfSites][T]: float-float complex entries (float4) for TF32, float2
+  // for BF16
+  extern __shared__ float4 tab[];
   __shared__ int mmax[3];
   __shared__ double phi[kSfSites][3];
   const int tid = threadIdx.x;
@@ -1176,7 +1208,7 @@ split_features_direct_kernel(const double* __restrict__ cart, int64_t n,
   __syncthreads();
   const int M0 = mmax[0], M1 = mmax[1], M2 = mmax[2];
   const int off1 = 2 * M0 + 1, off2 = off1 + 2 * M1 + 1, T = off2 + 2 * M2 + 1;
-  const int64_t esz = TF32 ? sizeof(double2) : sizeof(float2);
+  const int64_t esz = TF32 ? sizeof(float4) : sizeof(float2);
   const bool use_tab = (int64_t)T * kSfSites * esz <= kSfSmem;
   float2* tabf = (float2*)tab;
   if (use_tab) {
@@ -1186,8 +1218,12 @@ split_features_direct_kernel(const double* __restrict__ cart, int64_t n,
       const int m = j - (d == 0 ? M0 : (d == 1 ? off1 + M1 : off2 + M2));
       double sv, cv;
       sincos(__dmul_rn((double)m, phi[si][d]), &sv, &cv);
-      if (TF32) tab[e] = make_double2(cv, sv);
-      else tabf[e] = make_float2((float)cv, (float)sv);
+      if (TF32) {
+        const float2 c2 = ff_from(cv), s2 = ff_from(sv);
+        tab[e] = make_float4(c2.x, c2.y, s2.x, s2.y);
+      } else {
+        tabf[e] = make_float2((float)cv, (float)sv);
+      }
     }
   }
   __syncthreads();
@@ -1205,22 +1241,30 @@ split_features_direct_kernel(const double* __restrict__ cart, int64_t n,
     for (int si = 0; si < ns; ++si) {
       const int64_t at = (site0 + si) * ld + c;
       if (TF32) {
-        double2 z = make_double2(0.0, 0.0);
+        float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
         if (live) {
           if (use_tab) {
-            const double2* t = tab + si * T;
-            z = cmul2(cmul2(t[M0 + m0], t[off1 + M1 + m1]), t[off2 + M2 + m2]);
+            const float4* t = tab + si * T;
+            z = ffc_mul(ffc_mul(t[M0 + m0], t[off1 + M1 + m1]), t[off2 + M2 + m2]);
           } else {
             const double* r = cart + (site0 + si) * 3;
-            sincos(kc[k * 3] * r[0] + kc[k * 3 + 1] * r[1] + kc[k * 3 + 2] * r[2], &z.y, &z.x);
+            double sv, cv;
+            sincos(kc[k * 3] * r[0] + kc[k * 3 + 1] * r[1] + kc[k * 3 + 2] * r[2], &sv, &cv);
+            const float2 c2 = ff_from(cv), s2 = ff_from(sv);
+            z = make_float4(c2.x, c2.y, s2.x, s2.y);
           }
         }
-        const double f0 = w * z.x, f1 = w * z.y;
+        const float2 wf = ff_from(w);
+        const float2 f0 = ff_mul(wf, make_float2(z.x, z.y));
+        const float2 f1 = ff_mul(wf, make_float2(z.z, z.w));
+        // hi = TF32(f), lo = TF32(f - hi); f.hi - hi is exact in FP32
         uint32_t h0, h1, l0, l1;
-        asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(h0) : "f"((float)f0));
-        asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(h1) : "f"((float)f1));
-        asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(l0) : "f"((float)(f0 - (double)__uint_as_float(h0))));
-        asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(l1) : "f"((float)(f1 - (double)__uint_as_float(h1))));
+        asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(h0) : "f"(f0.x));
+        asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(h1) : "f"(f1.x));
+        const float r0 = __fadd_rn(__fsub_rn(f0.x, __uint_as_float(h0)), f0.y);
+        const float r1 = __fadd_rn(__fsub_rn(f1.x, __uint_as_float(h1)), f1.y);
+        asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(l0) : "f"(r0));
+        asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(l1) : "f"(r1));
         // c is even and ld a multiple of 32: 8-byte aligned pairs
         *(float2*)((float*)hi + at) = make_float2(__uint_as_float(h0), __uint_as_float(h1));
         *(float2*)((float*)lo + at) = make_float2(__uint_as_float(l0), __uint_as_float(l1));
