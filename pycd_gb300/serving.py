@@ -374,6 +374,25 @@ class KmcServer(object):
         and every bucket's chunk lasts about as long."""
         return max(500, int(self.chunk_steps * 8 / max(8, b.nc_bound)))
 
+    def warm_up(self, jobs, steps=1000):
+        """Serve a short copy of one job per carrier class of `jobs` (each
+        alone in its bucket, so the block launch forms run too) and discard
+        it, so that one-time costs of the first admission, launch and
+        retirement (first use of device code and host libraries) fall before
+        traffic is taken.  Buckets stay allocated; the lattice cache and the
+        served-job list are left as they were."""
+        if self.pending or any(self.waiting.values()):
+            raise RuntimeError("warm_up() runs before jobs are submitted")
+        sample = {}
+        for j in jobs:
+            sample.setdefault(_pow2(j["carriers"]), j)
+        done = self.done
+        self.done = []
+        self.run([dict(j, steps=min(int(j["steps"]), int(steps)), arrival=0.0)
+                  for j in sample.values()])
+        self.done = done
+        return len(sample)
+
     def busy(self):
         return (bool(self.pending) or any(self.waiting.values())
                 or any(b.jobs for b in self.buckets.values()))

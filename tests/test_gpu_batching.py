@@ -73,6 +73,10 @@ def test_server_results_equal_alone_runs(cuda_ready):
     jobs = poisson_jobs(24, rate=400.0, seed=5, median_sites=400, max_sites=2000,
                         max_carriers=8, min_steps=2000, max_steps=20000)
     server = KmcServer(budget_bytes=20e9, chunk_steps=1500, slots_per_bucket=8, seed=9)
+    # warm-up jobs pass through the same buckets first and are discarded
+    n_warm = server.warm_up(jobs, steps=700)
+    assert n_warm == len({int(j["carriers"] - 1).bit_length() for j in jobs})
+    assert server.done == [] and all(not b.jobs for b in server.buckets.values())
     stats = server.run([dict(j) for j in jobs], max_seconds=300)
     assert stats["jobs"] == 24 and stats["unfinished"] == 0
     assert stats["latency_p99_s"] >= stats["latency_p50_s"] > 0
