@@ -60,6 +60,8 @@
 // Every mbarrier wait is bounded; on time-out the CTA records an error,
 // stops issuing, waits (bounded) for its own copies and MMAs, frees its
 // tensor memory and returns.
+#include <atomic>
+
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
@@ -1426,12 +1428,25 @@ int ewald_build_split(const PycdEwaldDesc* d, int mode, double* out,
   if (d->split_form != 2 &&
       cudaFuncSetAttribute(pair_fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            (int)kPairSmemBytes) == cudaSuccess) {
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(2 * (unsigned)n_tiles);
-    cfg.blockDim = dim3(kThreads);
-    cfg.dynamicSmemBytes = kPairSmemBytes;
-    cfg.stream = s;
-    if (cudaOccupancyMaxActiveClusters(&pairs, pair_fn, &cfg) != cudaSuccess) pairs = 0;
+    // the count depends on the kernel, its block and its shared memory alone:
+    // asked once per device and variant (stored as count + 1)
+    static std::atomic<int> known[kMaxDevices][2];
+    int dev = -1;
+    if (cudaGetDevice(&dev) != cudaSuccess) dev = -1;
+    const bool keep = dev >= 0 && dev < kMaxDevices;
+    const int k = keep ? known[dev][tf32 ? 1 : 0].load(std::memory_order_relaxed) : 0;
+    if (k > 0) {
+      pairs = k - 1;
+    } else {
+      cudaLaunchConfig_t cfg = {};
+      cfg.gridDim = dim3(2 * (unsigned)n_tiles);
+      cfg.blockDim = dim3(kThreads);
+      cfg.dynamicSmemBytes = kPairSmemBytes;
+      cfg.stream = s;
+      if (cudaOccupancyMaxActiveClusters(&pairs, pair_fn, &cfg) != cudaSuccess) pairs = 0;
+      if (keep && pairs >= 0)
+        known[dev][tf32 ? 1 : 0].store(pairs + 1, std::memory_order_relaxed);
+    }
   }
   (void)cudaGetLastError();  // a device without such clusters takes single CTAs
   if (pairs > 0) {

@@ -47,11 +47,29 @@ def half_space_k_vectors(recip, k_max, k_cut):
     return np.ascontiguousarray(half.astype(np.int32)), keep
 
 
+_KV_CACHE = {}      # (recip, k_max, k_cut) values -> kept k list
+_KV_CACHE_MAX = 64
+
+
 def effective_k_vectors(recip, k_max, k_cut):
     """Half-space integer k list kept by the reference, in its order: the
-    k-vectors of ``half_space_k_vectors`` inside the cut."""
-    half, keep = half_space_k_vectors(recip, k_max, k_cut)
-    return np.ascontiguousarray(half[keep])
+    k-vectors of ``half_space_k_vectors`` inside the cut.
+
+    The list depends on the values of the three arguments alone; the last
+    64 lists are kept (as read-only arrays), so that rebuilding an array, or
+    scanning alpha at a fixed cut, does not enumerate the k grid again
+    (0.65 ms of host time at K = 4,095)."""
+    key = (np.asarray(recip, dtype=np.float64).tobytes(),
+           tuple(int(v) for v in np.ravel(k_max)), float(k_cut))
+    kv = _KV_CACHE.get(key)
+    if kv is None:
+        half, keep = half_space_k_vectors(recip, k_max, k_cut)
+        kv = np.ascontiguousarray(half[keep])
+        kv.flags.writeable = False
+        if len(_KV_CACHE) >= _KV_CACHE_MAX:
+            _KV_CACHE.pop(next(iter(_KV_CACHE)))
+        _KV_CACHE[key] = kv
+    return kv
 
 
 def pmiv_is_lattice_consistent(system, pmiv, tol=1e-8):
@@ -172,7 +190,7 @@ def make_desc(system, alpha, r_cut, k_cut, pmiv=None, kvecs=None):
     if pmiv is not None:  # the real-space term uses |pmiv_ij| as given
         d_pmiv = torch.as_tensor(np.ascontiguousarray(pmiv, dtype=np.float64)
                                  ).to(dev)
-    d_kv = torch.as_tensor(kv).to(dev) if len(kv) else torch.zeros(
+    d_kv = torch.tensor(kv).to(dev) if len(kv) else torch.zeros(  # kv may be read-only
         (1, 3), dtype=torch.int32, device=dev)
     desc = nat.EwaldDesc()
     desc.n_sites = n

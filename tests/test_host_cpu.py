@@ -172,6 +172,26 @@ def test_k_vectors_match_oracle(name):
     assert np.array_equal(np.frombuffer(buf, np.int32).reshape(-1, 3), ours)
 
 
+def test_k_vector_cache_returns_the_enumerated_list():
+    """effective_k_vectors keeps the last 64 lists by argument value: a kept
+    list equals a fresh enumeration, comes back as the same read-only array
+    and the cache stays bounded."""
+    recip = np.array([[0.31, 0.0, 0.0], [0.02, 0.27, 0.0], [0.0, 0.0, 0.41]])
+    km = np.array([4, 5, 3])
+    first = {}
+    for kc in (0.9, 1.3, 0.9):
+        kv = ew.effective_k_vectors(recip, km, kc)
+        half, keep = ew.half_space_k_vectors(recip, km, kc)
+        assert np.array_equal(kv, half[keep]) and not kv.flags.writeable
+        assert first.setdefault(kc, kv) is kv
+    with pytest.raises(ValueError):
+        kv[0, 0] = 1
+    assert ew.effective_k_vectors(recip * 1.001, km, 1.3) is not first[1.3]
+    for i in range(70):
+        ew.effective_k_vectors(recip, km, 0.5 + 0.01 * i)
+    assert len(ew._KV_CACHE) <= ew._KV_CACHE_MAX
+
+
 def test_half_space_k_vectors_match_reference_k_vector_log():
     """The k-vectors listed by the reference's return_k_vector_data report
     (every half-space vector of the k_max box, those outside k_cut at zero)
