@@ -233,8 +233,8 @@ def supercell_layout(system, pmiv=None, tol=1e-6):
     nb = len(uc)
     if nb == 0 or len(cart) != nb * int(np.prod(ss)):
         return None
-    cells = np.stack(np.meshgrid(np.arange(ss[0]), np.arange(ss[1]), np.arange(ss[2]),
-                                 indexing="ij"), -1).reshape(-1, 3)
+    # cell indices in C order, as doubles (an integer matmul misses BLAS)
+    cells = np.indices(tuple(int(v) for v in ss), dtype=np.float64).reshape(3, -1).T
     want = (cells @ np.asarray(m.lattice_matrix, dtype=np.float64))[:, None, :] + uc[None]
     if np.abs(want.reshape(-1, 3) - cart).max() > tol:
         return None
