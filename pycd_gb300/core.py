@@ -655,6 +655,7 @@ class Run(object):
                     if attrs.get("write") and kind in arrays:
                         with open(tr["dir"] / attrs["file_name"], "ab") as fh:
                             np.save(fh, arrays[kind])
+                self._write_hdf5(tr["dir"], output_data, unwrapped, res["time"], every_step)
                 if self.doping_active:
                     np.save(tr["dir"] / "occupancy.npy",
                             np.asarray(tr["occupancy_list"], dtype=int))
@@ -674,6 +675,49 @@ class Run(object):
             prefix = self._drift_mobility_report(drift, dst_path)
         generate_report(self.start_time, dst_path, "Run", 1, prefix)
         return None
+
+    def _write_hdf5(self, traj_dir, output_data, unwrapped, time_data, every_step):
+        """The optional HDF5 trajectory file of one trajectory
+        (PyCD/core.py:2677-2691, 2882-2902; layout in hdf5_io).  It is written
+        when output_data['hdf5_output']['enabled'] is true, the unwrapped rows
+        are written and h5py can be imported; without h5py it is left out
+        silently, as the reference does.  Failures print the reference's
+        warnings and the run goes on.
+
+        /time holds each frame's simulation time.  Per-step rows
+        (write_every_step): row k is appended at the end of step k + 1
+        (core.py:2832-2845), so its time is time_data[k + 1].  Grid rows: row
+        r is the state at r * time_interval.  The reference passes its whole
+        time list (steps + 1 values) for the frames, which h5py refuses in
+        both cases (its /time stays zero-filled, with a warning), or, when
+        the time output is off, the frame indices 0, 1, ... as times; its
+        coordinates are the ones written here."""
+        cfg = output_data.get("hdf5_output")
+        if not (cfg and cfg.get("enabled", False)
+                and output_data.get("unwrapped_traj", {}).get("write", False)):
+            return
+        try:
+            from .hdf5_io import HDF5TrajectoryWriter
+        except ImportError:
+            return
+        try:
+            writer = HDF5TrajectoryWriter(Path(traj_dir) / cfg["file_name"],
+                                          self.total_species, len(self.species_count))
+        except Exception as e:
+            print(f"Warning: Could not initialize HDF5 writer: {e}")
+            return
+        try:
+            n = len(unwrapped)
+            t = np.asarray(time_data, dtype=np.float64)
+            times = (t[1:] if every_step and len(t) == n + 1
+                     else np.arange(n) * self.time_interval)
+            writer.write_frames(unwrapped, times)
+        except Exception as e:
+            print(f"Warning: Failed to write HDF5 trajectory data: {e}")
+        try:
+            writer.close()
+        except Exception as e:
+            print(f"Warning: Failed to close HDF5 writer: {e}")
 
     def _advance_group(self, group, num_path, want):
         """Advance the trajectories of `group` together to the end of their

@@ -40,6 +40,14 @@ produced by the reference's code or ships with it:
       (every half-space k-vector of the k_max box, sorted by decreasing
       energy contribution, zero outside k_cut) and the k_max / k-vector
       count lines of precomputed_array.log.
+  hdf5.json/.npz
+      the reference's HDF5TrajectoryWriter (PyCD/hdf5_io.py) and its use in
+      do_kmc_steps, run against the h5py stand-in tests/fake_h5py.py (h5py is
+      not installed here): write_frame + write_frames and
+      save_trajectory_hdf5 of 2-D and 1-D arrays on seeded coordinates, and
+      the file do_kmc_steps writes for examples/Hematite's first ~2,000
+      steps with hdf5_output enabled, per step (write_every_step = 1) and
+      on the time grid (its coordinates, its warning and its /time).
   msd.json/.npz
       Analysis.compute_msd of the reference on the shipped Hematite
       trajectory (examples/Hematite/traj1, with the example's MSD parameters)
@@ -767,10 +775,97 @@ def kvector_data(core):
     (HERE / "kvector_data.json").write_text(json.dumps(cfg, indent=1))
 
 
+def _h5_record(path, prefix, out_json, out_arrays):
+    """Flatten a stand-in HDF5 file into the fixture: structure and
+    attributes into out_json[prefix], dataset values into out_arrays."""
+    import fake_h5py
+    rec = {}
+    for key, v in sorted(fake_h5py.load(path).items()):
+        if v.get("group"):
+            rec[key] = {"group": True, "attrs": v["attrs"]}
+            continue
+        d = v["data"]
+        rec[key] = {"dtype": d.dtype.str, "shape": list(d.shape),
+                    "maxshape": [None if m is None else int(m) for m in v["maxshape"]],
+                    "chunks": v["chunks"],
+                    "compression": v["compression"], "attrs": v["attrs"]}
+        out_arrays[prefix + key] = d
+    out_json[prefix] = rec
+
+
+def hdf5(core):
+    """HDF5 output of the reference against the h5py stand-in (installed in
+    main() before PyCD.core is imported, so that its HDF5_AVAILABLE holds)."""
+    import contextlib
+    import copy
+    import io as _io
+    from PyCD import hdf5_io
+    rng = np.random.default_rng(7)
+    rec, arrays = {}, {}
+    tmp = Path(tempfile.mkdtemp())
+    coords = rng.random((4, 3, 3)) * 10.0
+    with hdf5_io.HDF5TrajectoryWriter(tmp / "frames.h5", 3, 1) as w:
+        w.write_frame(coords[0].ravel(), 0.5)
+        w.write_frames(coords[1:].reshape(3, 9), np.array([1.5, 2.5, 4.0]))
+    _h5_record(tmp / "frames.h5", "frames", rec, arrays)
+    arrays["frames_in_coords"] = coords
+    c2 = rng.random((4, 6)) * 5.0
+    hdf5_io.save_trajectory_hdf5(tmp / "save2d.h5", c2, np.arange(4, dtype=float), n_atoms=2)
+    _h5_record(tmp / "save2d.h5", "save2d", rec, arrays)
+    arrays["save2d_in_coords"] = c2
+    c1 = rng.random(6)
+    hdf5_io.save_trajectory_hdf5(tmp / "save1d.h5", c1)
+    _h5_record(tmp / "save1d.h5", "save1d", rec, arrays)
+    arrays["save1d_in_coords"] = c1
+    # do_kmc_steps with hdf5_output ('write': 0 keeps the reference's output
+    # loop, which reads every entry's 'write' (core.py:2864-2866), from
+    # raising KeyError on the hdf5_output entry)
+    name, params, t_final = "Hematite", HEMATITE, 6e-7
+    ex = REF / "examples" / name
+    poscar = (ex / "InputFiles" / "POSCAR").read_text()
+    mat, nb = material_objects(core, params, poscar, [2, 2, 1], [1, 1, 1], tempfile.mkdtemp())
+    hop = np.load(ex / "InputFiles" / "hop_neighbor_list.npy", allow_pickle=True)[()]
+    pmiv = np.load(ex / "InputFiles" / "pairwise_min_image_vector_data.npy")
+    A_shipped = np.load(ex / "InputFiles" / "precomputed_array.npy")
+    system = make_system(core, mat, nb, hop, pmiv, params)
+    runs = {}
+    for label, every in (("run_every_step", 1), ("run_grid", 0)):
+        run_p = copy.deepcopy(dict(RUN_COMMON, t_final=t_final))
+        run_p["output_data"]["unwrapped_traj"]["write_every_step"] = every
+        run_p["output_data"]["hdf5_output"] = {"enabled": True, "file_name": "trajectory.h5",
+                                               "write": 0}
+        run = core.Run(system, A_shipped, run_p["temp"], run_p["ion_charge_type"],
+                       run_p["species_charge_type"], 1, t_final, run_p["time_interval"],
+                       np.asarray(run_p["species_count"]), run_p["initial_occupancy"],
+                       run_p["relative_energies"], run_p["external_field"], run_p["doping"])
+        d = Path(tempfile.mkdtemp())
+        shutil.copy(ex / "traj1" / "initial_rnd_state.dump", d / "initial_rnd_state.dump")
+        out = _io.StringIO()
+        with contextlib.redirect_stdout(out):
+            run.do_kmc_steps(d, run_p["output_data"], run_p["random_seed"], "parallel")
+        _h5_record(d / "trajectory.h5", label, rec, arrays)
+        u = np.load(d / "unwrapped_traj.npy")
+        t = np.load(d / "time_data.npy")
+        runs[label] = {"output_data": run_p["output_data"], "rows": int(len(u)),
+                       "n_steps": int(len(t) - 1),
+                       "warnings": [l for l in out.getvalue().splitlines()
+                                    if l.startswith("Warning")]}
+        print(f"hdf5 {label}: {len(u)} rows, {len(t) - 1} steps, "
+              f"warnings {runs[label]['warnings']}")
+    cfg = {"t_final": t_final, "records": rec, "runs": runs}
+    np.savez_compressed(HERE / "hdf5.npz", **{k.replace("/", "|"): v for k, v in arrays.items()})
+    (HERE / "hdf5.json").write_text(json.dumps(cfg, indent=1))
+
+
 def main(parts):
     if REF is None:
         raise SystemExit("set PYCD_REFERENCE to the root of a reference checkout")
+    if "hdf5" in parts:
+        import fake_h5py
+        sys.modules["h5py"] = fake_h5py  # before PyCD.core reads HDF5_AVAILABLE
     core = install_shims()
+    if "hdf5" in parts:
+        hdf5(core)
     if "kvector_data" in parts:
         kvector_data(core)
     if "ewald_params" in parts:
@@ -795,4 +890,5 @@ def main(parts):
 
 if __name__ == "__main__":
     main(sys.argv[1:] or ["hematite", "every_step", "hematite_outputs", "bvo", "bvo_doped",
-                          "corundum324", "corundum3600", "msd", "ewald_params", "kvector_data"])
+                          "corundum324", "corundum3600", "msd", "ewald_params", "kvector_data",
+                          "hdf5"])

@@ -111,6 +111,48 @@ def test_do_kmc_steps_write_every_step_matches_reference(cuda_ready):
     assert np.abs(t[1:] / fix["time"][1:] - 1).max() < TIME_RTOL
 
 
+def test_do_kmc_steps_hdf5_output_matches_reference(cuda_ready, monkeypatch):
+    """hdf5_output enabled (core.py:2677-2691, 2882-2902), per step and on
+    the time grid, written through the h5py stand-in: the layout, topology
+    and float32 coordinates of the file the reference's own run of
+    examples/Hematite wrote (tests/golden/hdf5.*), bit for bit.  /time holds
+    each frame's time (the reference's is zero-filled: h5py refuses the
+    time list it passes, as its recorded warning shows)."""
+    import sys
+    import fake_h5py
+    monkeypatch.setitem(sys.modules, "h5py", fake_h5py)
+    monkeypatch.delitem(sys.modules, "pycd_gb300.hdf5_io", raising=False)
+    ref, arr = gio.load("hdf5")
+    arrays = {k.replace("|", "/"): v for k, v in arr.items()}
+    try:
+        for label, every in (("run_every_step", 1), ("run_grid", 0)):
+            meta = ref["runs"][label]
+            assert meta["warnings"] and "Can't broadcast" in meta["warnings"][0]
+            cfg, _, run = _example_run("hematite", t_final=ref["t_final"])
+            d = Path(tempfile.mkdtemp())
+            st = cfg["rnd_state"]
+            with open(d / "initial_rnd_state.dump", "wb") as fh:
+                pickle.dump((st[0], tuple(st[1]), st[2]), fh)
+            run.do_kmc_steps(d, meta["output_data"], cfg["run"]["random_seed"], "parallel")
+            got = fake_h5py.load(d / "trajectory.h5")
+            rec = ref["records"][label]
+            assert sorted(got) == sorted(rec)
+            for key, want in rec.items():
+                if want.get("group"):
+                    continue
+                assert got[key]["data"].dtype.str == want["dtype"], key
+                assert list(got[key]["data"].shape) == want["shape"], key
+                assert got[key]["attrs"] == want["attrs"], key
+                if key != "/time":
+                    assert np.array_equal(got[key]["data"], arrays[label + key]), key
+            t = np.load(d / "time_data.npy")
+            n = meta["rows"]
+            want_t = (t[1:] if every else np.arange(n) * run.time_interval) * K.AUTIME2PS
+            assert np.array_equal(got["/time"]["data"], want_t)
+    finally:
+        sys.modules.pop("pycd_gb300.hdf5_io", None)
+
+
 def test_do_kmc_steps_doped_bvo_matches_reference(cuda_ready):
     """examples/BVO with two W dopants (charge 6) and shell-indexed site
     energies read from site_indices.npy, the electron starting on a dopant
