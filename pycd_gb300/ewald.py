@@ -233,10 +233,12 @@ def supercell_layout(system, pmiv=None, tol=1e-6):
     nb = len(uc)
     if nb == 0 or len(cart) != nb * int(np.prod(ss)):
         return None
-    # cell indices in C order, as doubles (an integer matmul misses BLAS)
+    # cell indices in C order, as doubles (an integer matmul misses BLAS);
+    # translation + basis position, site by site, as one contiguous addition
     cells = np.indices(tuple(int(v) for v in ss), dtype=np.float64).reshape(3, -1).T
-    want = (cells @ np.asarray(m.lattice_matrix, dtype=np.float64))[:, None, :] + uc[None]
-    if np.abs(want.reshape(-1, 3) - cart).max() > tol:
+    trans = cells @ np.asarray(m.lattice_matrix, dtype=np.float64)
+    want = np.repeat(trans, nb, axis=0) + np.tile(uc, (len(trans), 1))
+    if np.abs(want - cart).max() > tol:
         return None
     return [int(v) for v in ss], int(nb)
 
