@@ -32,7 +32,7 @@ constexpr int kNbrCache = 4;
 struct CtaShared {
   double wsum[4];
   double de_sel, k_sel;
-  int sel, n_sel, o_sel;
+  int sel, n_sel, o_sel, c_sel;
   int stop;  // cooperative stop status for this step (0 = go on), from thread 0
   int nb[kNbrCache];  // neighbours of n_sel (from the selected process' cache)
   // rebuilt processes of the moved carrier: job i < S is slot i, job S its Q
@@ -152,14 +152,12 @@ __device__ void advance_trajectory_cta(const KmcArgs& a, int64_t t, CtaShared& s
   }
   const KmcSysDev& sd = a.systems[sys_id];
   const PycdKmcSystem& sy = sd.pub;
-  const int64_t N = sy.n_sites;
   const int S = sy.n_slots;
   const int NC = sy.n_carriers;
   const int NP = NC * S;
   const int MC = st.max_carriers;
   const double q = sy.carrier_charge;
   const double two_q = dmul(2.0, q);
-  const double* __restrict__ A = sy.d_A;
   const double2* __restrict__ coef = sd.coef;
   const double2* __restrict__ slotc = sd.slotc;
   const double dt_grid = sy.time_interval;
@@ -333,7 +331,7 @@ __device__ void advance_trajectory_cta(const KmcArgs& a, int64_t t, CtaShared& s
       }
       const int jsel = node - MAXP;
       double term_s = 0.0, dslot_s = 0.0, k_s = 0.0;
-      int n_s = 0, o_s = 0;
+      int n_s = 0, o_s = 0, c_s = 0;
 #pragma unroll
       for (int j = 0; j < MAXP; ++j) {
         const double d = __shfl_sync(full, term[j], base);
@@ -341,7 +339,8 @@ __device__ void advance_trajectory_cta(const KmcArgs& a, int64_t t, CtaShared& s
         const double kk = __shfl_sync(full, kp[j], base);
         const int ns = __shfl_sync(full, pc.newsite[j], base);
         const int os = __shfl_sync(full, pc.oldsite[j], base);
-        if (j == jsel) { term_s = d; dslot_s = e; k_s = kk; n_s = ns; o_s = os; }
+        const int cs = __shfl_sync(full, pc.carrier[j], base);  // sel / S
+        if (j == jsel) { term_s = d; dslot_s = e; k_s = kk; n_s = ns; o_s = os; c_s = cs; }
       }
       const double de_s = fma(two_q, term_s, dslot_s);  // dE0 of the event
       int cand[kNbrCache];
@@ -361,12 +360,13 @@ __device__ void advance_trajectory_cta(const KmcArgs& a, int64_t t, CtaShared& s
         sh.k_sel = k_s;
         sh.n_sel = n_s;
         sh.o_sel = o_s;
+        sh.c_sel = c_s;
       }
     }
     __syncthreads();
     const int sel = sh.sel;
     const double de_sel = sh.de_sel, k_sel = sh.k_sel;
-    const int n_sel = sh.n_sel, o_sel = sh.o_sel;
+    const int n_sel = sh.n_sel, o_sel = sh.o_sel, c_sel = sh.c_sel;
     if (sel >= NP) { status = PYCD_TRAJ_NO_EVENT; break; }
 
     // ---- residence time (every warp, identical values) -------------------
@@ -377,7 +377,7 @@ __device__ void advance_trajectory_cta(const KmcArgs& a, int64_t t, CtaShared& s
       const double tq = ddiv(sim_time, dt_grid);
       end_path = (tq < 9.0e18) ? (int64_t)tq : INT64_MAX;
     }
-    const int c_sel = sel / S, s_sel = sel - c_sel * S;
+    const int s_sel = sel - c_sel * S;
 
     if (a.out.d_delg0_grid) {
       const int64_t e = end_path < n_path ? end_path : n_path;

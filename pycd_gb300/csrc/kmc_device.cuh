@@ -224,7 +224,6 @@ __device__ __forceinline__ bool setup_processes(const PycdKmcSystem& sy,
   const int64_t N = sy.n_sites;
   const int S = sy.n_slots;
   const int NP = sy.n_carriers * S;
-  const double* __restrict__ A = sy.d_A;
   bool bad = false;
 #pragma unroll
   for (int j = 0; j < MAXP; ++j) {
@@ -587,14 +586,6 @@ __device__ __forceinline__ void process_rates(const ProcCache<MAXP>& pc, double 
 // the G subtractions in step order: the same doubles as one division and one
 // subtraction per step, at about a G-th of the FP64 divisions.
 // ---------------------------------------------------------------------------
-// float >= x for a double x >= 0 (integer operations only)
-__device__ __forceinline__ float f32_above(double x) {
-  const unsigned hi = (unsigned)__double2hiint(x) & 0x7fffffffu;
-  const int e = (int)(hi >> 20) - 1023 + 127;
-  if (e >= 255) return INFINITY;
-  if (e <= 0) return (hi == 0 && __double2loint(x) == 0) ? 0.0f : 0x1p-126f;
-  return __uint_as_float((((unsigned)e << 23) | ((hi & 0xfffffu) << 3)) + 1u);
-}
 // float <= x for a double x >= 0 (integer operations only)
 __device__ __forceinline__ float f32_below(double x) {
   const unsigned hi = (unsigned)__double2hiint(x) & 0x7fffffffu;
@@ -629,10 +620,18 @@ struct TimeChain {
                                        int64_t c) {
     if (g == npend) { kt = ktot; nlu2 = lu2; col = c; }
     ++npend;
-    // -lu2 / ktot <= above(-lu2) / below(ktot), rounded up, with room for
-    // the rounding of the double quotient
-    const float inc = __fmul_ru(__fdiv_ru(f32_above(-lu2), f32_below(ktot)),
-                                1.0f + 0x1p-20f);
+    // From the exponent fields alone: -lu2 < 2^(a - 1022) (a = its biased
+    // exponent; also for +0 and subnormals, a = 0) and ktot >= 2^(b - 1023)
+    // for a normal ktot (b >= 1), so the double quotient RN(-lu2 / ktot) <=
+    // 2^(a - b + 1); +inf for a subnormal ktot or beyond the float range,
+    // 2^-126 below it.  The bound is loose by at most 4, which only brings
+    // an exact flush nearer a grid boundary sooner (same values).
+    const int a_exp = (__double2hiint(lu2) >> 20) & 0x7ff;  // lu2 <= 0
+    const int b_exp = (__double2hiint(ktot) >> 20) & 0x7ff;
+    const int k2 = a_exp - b_exp + 1;
+    const float inc = (b_exp == 0 || k2 > 127)
+                          ? INFINITY
+                          : __int_as_float(((k2 < -126 ? -126 : k2) + 127) << 23);
     bound = __fadd_ru(bound, inc);
     return force || npend == G || !(bound < slack);
   }
@@ -866,7 +865,7 @@ __device__ void advance_trajectory(const KmcArgs& a, int64_t t, int g,
 
     // broadcast the selected process' data from its owner lane
     double term_sel = 0.0, de_slot = 0.0, k_sel = 0.0;
-    int n_sel = 0, o_sel = 0;
+    int n_sel = 0, o_sel = 0, c_sel = 0;
 #pragma unroll
     for (int j = 0; j < MAXP; ++j) {
       const double d = gshfl<G>(gmask, term[j], base);
@@ -874,10 +873,13 @@ __device__ void advance_trajectory(const KmcArgs& a, int64_t t, int g,
       const double kk = gshfl<G>(gmask, kp[j], base);
       const int ns = gshfl<G>(gmask, pc.newsite[j], base);
       const int os = gshfl<G>(gmask, pc.oldsite[j], base);
-      if (j == jsel) { term_sel = d; de_slot = e; k_sel = kk; n_sel = ns; o_sel = os; }
+      const int cs = gshfl<G>(gmask, pc.carrier[j], base);  // sel / S, without a division
+      if (j == jsel) {
+        term_sel = d; de_slot = e; k_sel = kk; n_sel = ns; o_sel = os; c_sel = cs;
+      }
     }
     const double de_sel = fma(two_q, term_sel, de_slot);  // dE0 of the event
-    const int c_sel = sel / S, s_sel = sel - c_sel * S;
+    const int s_sel = sel - c_sel * S;
 
     // delG0 grid rows [start, end) (core.py:2807-2809)
     if (a.out.d_delg0_grid) {
