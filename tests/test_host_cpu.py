@@ -64,6 +64,46 @@ def test_exp_table_is_correctly_rounded():
         assert abs(lo[j]) < math.ulp(hi[j]) / 2 and hi[j] + lo[j] == hi[j], j
 
 
+def _exponent_bound(lu2, ktot):
+    """The KMC kernels' per-step residence-time bound (TimeChain::push),
+    restated: 2^(a - b + 1) as a float from the biased exponents a of lu2 and
+    b of ktot; +inf for a subnormal ktot or above the float range, 2^-126
+    below it."""
+    a = (lu2.view(np.uint64) >> np.uint64(52)) & np.uint64(0x7FF)
+    b = (ktot.view(np.uint64) >> np.uint64(52)) & np.uint64(0x7FF)
+    k = a.astype(np.int64) - b.astype(np.int64) + 1
+    out = np.ldexp(np.float32(1.0), np.clip(k, -126, 127).astype(np.int32)).astype(np.float32)
+    out[(b == 0) | (k > 127)] = np.inf
+    return out
+
+
+def test_residence_time_bound_holds():
+    """RN(-lu2 / ktot) <= the exponent-field bound for lu2 = log(u2), u2 in
+    (0, 1], and ktot over the positive doubles (normal and subnormal): the
+    deferred time chain may skip the exact time only while the summed bounds
+    stay below the gap to the next grid row."""
+    rng = np.random.default_rng(11)
+    u2 = np.concatenate([rng.random(400_000), 1.0 - rng.random(2000) * 2.0 ** -40,
+                         [1.0, np.nextafter(1.0, 0.0), 2.0 ** -53, 5e-324]])
+    u2 = u2[u2 > 0]
+    lu2 = np.log(u2)
+    n = len(lu2)
+    ktot = np.concatenate([
+        np.exp(rng.uniform(np.log(1e-300), np.log(1e300), n // 2)),
+        np.exp(rng.uniform(-40.0, 5.0, n - n // 2 - 4)),
+        [5e-324, 2.2250738585072014e-308, 1.0, 1.7976931348623157e308]])
+    rng.shuffle(ktot)
+    with np.errstate(over="ignore"):  # tiny ktot: the quotient overflows, the bound is +inf
+        q = (-lu2) / ktot
+    bound = _exponent_bound(lu2, ktot).astype(np.float64)
+    finite = np.isfinite(q)
+    assert np.all(q[finite] <= bound[finite])
+    assert np.all(np.isinf(bound[~finite]))
+    # at most 4x loose where the bound is a normal float and the quotient is not tiny
+    tight = np.isfinite(bound) & (bound > 2.0 ** -126) & (q > 0)
+    assert np.all(bound[tight] <= 4.0 * q[tight])
+
+
 def test_exp_fixed_table_is_correctly_rounded():
     """The integer exp's table: 2^(j/4096) 2^62 rounded to the nearest
     integer, built by the library from the (hi, lo) pairs with integer
